@@ -1,0 +1,194 @@
+/*
+ * nrg_gpu.h - C ABI of the GB300 NRG iteration engine.
+ *
+ * Plain C types only (pointers, sizes, doubles); no CUDA or torch types cross
+ * this boundary.  Every call returns 0 on success or a positive NRG_E_* code;
+ * nrg_last_error() returns the message of the last failure on this thread.
+ * Host buffers passed in are copied before the call returns; host buffers
+ * passed out must hold the sizes the matching *_info / count call reported.
+ *
+ * Each entry point names the reference interface it replaces
+ * (paths relative to the srbhp/nrgplusplus tree).
+ */
+#ifndef NRG_GPU_H
+#define NRG_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* error codes */
+#define NRG_OK 0
+#define NRG_E_ARG 1        /* invalid argument (reference: std::runtime_error) */
+#define NRG_E_STATE 2      /* call out of order */
+#define NRG_E_CUDA 3       /* CUDA runtime error */
+#define NRG_E_NOMEM 4      /* device memory or HBM budget exhausted */
+#define NRG_E_EIG 5        /* block eigensolver did not converge in its sweep cap */
+#define NRG_E_NOCUDA 6     /* no usable CUDA device */
+
+/* precision modes */
+#define NRG_PREC_FP64 0    /* plain FP64 path */
+#define NRG_PREC_MIXED 1   /* FP32 bulk + FP64-accurate refinement */
+
+typedef struct nrg_engine nrg_engine;
+typedef struct nrg_run nrg_run;
+typedef struct nrg_opset nrg_opset;
+typedef struct nrg_fdm nrg_fdm;
+typedef struct nrg_thermo nrg_thermo;
+
+typedef struct {
+  int device;                 /* CUDA device ordinal */
+  int precision;              /* NRG_PREC_* */
+  uint64_t hbm_budget_bytes;  /* 0 = no budget */
+  int verbose;                /* 0 = silent */
+} nrg_engine_opts;
+
+/*
+ * One site model (impurity or Wilson site): what nrgcore reads from a model
+ * (nrgcore.hpp:44-53, 68-70): get_basis(), get_eigenvaluesQ(), get_chi_Q(),
+ * f_dag_operator.  Operator blocks are dense row-major dims[row] x dims[col].
+ */
+typedef struct {
+  int nq;                     /* quantum numbers per sector */
+  int nsect;                  /* number of sectors */
+  const int *qnum;            /* nsect * nq */
+  const int *dims;            /* nsect */
+  const double *energies;     /* sum(dims), sector by sector, ascending */
+  const double *chi;          /* nsect (bath parity; may be NULL for impurity) */
+  int nops;                   /* number of operators (f-dagger list) */
+  int nblk;                   /* number of stored operator blocks */
+  const int *blk_op;          /* nblk: operator index */
+  const int *blk_row;         /* nblk: row sector */
+  const int *blk_col;         /* nblk: column sector */
+  const double *blk_data;     /* concatenated block data */
+} nrg_site_desc;
+
+/* Block-sparse operator list in a run's sector basis (qOperator, qOperator.hpp:18-19). */
+typedef struct {
+  int nops;
+  int nblk;
+  const int *blk_op;
+  const int *blk_row;
+  const int *blk_col;
+  const int *blk_rows;        /* rows of each block */
+  const int *blk_cols;        /* columns of each block */
+  const double *blk_data;
+} nrg_op_desc;
+
+typedef struct {
+  int64_t iteration;          /* nrg_iterations_cnt (nrgcore.hpp:536) */
+  int64_t iteration_min;      /* nrg_iterations_min (nrgcore.hpp:538) */
+  int64_t n_pre_sectors;      /* pre_sysmQ.size() */
+  int64_t n_cur_sectors;      /* current_sysmQ.size() */
+  int64_t n_all;              /* all_eigenvalue.size() */
+  int64_t n_kept;             /* no_of_kept_states */
+  int64_t n_relgs;            /* relativeGroundStateEnergy.size() */
+  int64_t nq;                 /* quantum numbers per sector */
+  int64_t n_device_blocks;    /* non-empty sectors held on the device */
+  int64_t max_block;          /* largest block dimension this iteration */
+  int64_t n_snapshots;
+  int64_t device_bytes;       /* device memory held by this run */
+} nrg_run_info;
+
+/* ---- engine ------------------------------------------------------------ */
+const char *nrg_last_error(void);
+int nrg_engine_create(const nrg_engine_opts *opts, nrg_engine **out);
+int nrg_engine_destroy(nrg_engine *eng);
+/* Wall time of the device phases of the last step, milliseconds:
+ * out[0] assemble, out[1] eigensolve, out[2] truncate, out[3] rotate,
+ * out[4] operators; n = entries written. */
+int nrg_engine_phase_times(nrg_engine *eng, double *out, int cap, int *n);
+/* Number of kernel launches issued by the engine so far. */
+int nrg_engine_launch_count(nrg_engine *eng, uint64_t *out);
+int nrg_engine_sync(nrg_engine *eng);
+
+/* ---- one NRG run (nrgcore<Imp,Bath>) ---------------------------------- */
+/* nrgcore(im, bath) + set_parameters(nkeep): nrgcore.hpp:44-53, :336-342 */
+int nrg_run_create(nrg_engine *eng, const nrg_site_desc *impurity, const nrg_site_desc *bath,
+                   uint64_t nkeep, nrg_run **out);
+int nrg_run_destroy(nrg_run *run);
+/* set_parameters(n): nrgcore.hpp:336-342 (resets the run to iteration 0) */
+int nrg_run_set_parameters(nrg_run *run, uint64_t nkeep);
+/* bath refresh, nrgcore.hpp:68-70 (dynamic baths); takes effect at the next add_site */
+int nrg_run_set_bath(nrg_run *run, const nrg_site_desc *bath);
+/* add_bath_site(t, rescale): nrgcore.hpp:65-97 (assembly a2, eigensolve a3,
+ * f-dagger rotation a4; the truncation of this site is computed but only
+ * published by nrg_run_update_state, as in the reference) */
+int nrg_run_add_site(nrg_run *run, const double *t, int nt, double rescale);
+/* update_internal_state(): nrgcore.hpp:105-109 (truncation a5) */
+int nrg_run_update_state(nrg_run *run);
+/* checkHigherEnergyDiscarded(): nrgcore.hpp:384-386 */
+int nrg_run_check_discarded(nrg_run *run, int *out);
+int nrg_run_get_info(nrg_run *run, nrg_run_info *info);
+/* all_eigenvalue (nrgcore.hpp:520), sorted, unshifted */
+int nrg_run_get_all_eigenvalues(nrg_run *run, double *out, uint64_t cap);
+/* relativeGroundStateEnergy (nrgcore.hpp:522) */
+int nrg_run_get_relgs(nrg_run *run, double *out, uint64_t cap);
+/* current_sysmQ / pre_sysmQ (nrgcore.hpp:528-530): which = 0 current, 1 pre */
+int nrg_run_get_sectors(nrg_run *run, int which, int *qnum, uint64_t cap_sectors);
+/* eigenvaluesQ (nrgcore.hpp:532) per current sector: dims[nsect] and the
+ * concatenated values (shifted after update_state, as in the reference) */
+int nrg_run_get_eigenvalues_q(nrg_run *run, uint64_t *dims, double *values, uint64_t cap_values);
+/* eigenvaluesQ_kept_indices sizes per pre sector (nrgcore.hpp:524); the
+ * kept indices are always the prefix 0..k-1 of each sector */
+int nrg_run_get_kept(nrg_run *run, uint64_t *kept, uint64_t cap);
+/* coupled_nQ_index (nrgcore.hpp:534): counts[n_cur] and flattened entries */
+int nrg_run_get_coupled(nrg_run *run, uint64_t *counts, uint64_t *entries, uint64_t cap_entries);
+/* current_hamiltonQ[sector] (nrgcore.hpp:526): eigenvectors as columns,
+ * row-major n x n; n = dims[sector] */
+int nrg_run_get_eigenvectors(nrg_run *run, int64_t sector, double *out, uint64_t cap);
+/* get_f_dag_operator() / getPreWilsonSiteOperators() (nrgcore.hpp:377, :548):
+ * block (ip, i, j) of the rotated f-dagger.  The engine keeps the kept x kept
+ * part (all the next site reads, nrgcore.hpp:199-203); rows/cols report it. */
+int nrg_run_get_fdag_block(nrg_run *run, int ip, int64_t i, int64_t j, double *out, uint64_t cap,
+                           int64_t *rows, int64_t *cols);
+
+/* ---- tracked operators: update_system_operator (sysOperator.hpp:36-133) -- */
+/* ops given in the run's current "previous" basis (pre_sysmQ sectors) */
+int nrg_opset_create(nrg_run *run, const nrg_op_desc *ops, nrg_opset **out);
+int nrg_opset_destroy(nrg_opset *ops);
+/* update_system_operator(nrg, ops): call after add_site, before update_state */
+int nrg_opset_update(nrg_opset *ops);
+/* block (ip, i, j) of the tracked operator in the current basis */
+int nrg_opset_get_block(nrg_opset *ops, int ip, int64_t i, int64_t j, double *out, uint64_t cap,
+                        int64_t *rows, int64_t *cols);
+
+/* ---- device-resident snapshots (NrgData, nrgData.hpp:134-293) ---------- */
+/* saveCurrentData + saveqOperator: keep this site's U, eigenvalues, kept
+ * counts, sectors and the tracked operators on the device */
+int nrg_run_snapshot(nrg_run *run, nrg_opset *ops);
+/* loadCurrentData(iteration): select a stored snapshot for the backward pass */
+int nrg_run_load_snapshot(nrg_run *run, int64_t iteration);
+
+/* ---- FDM spectral function, T = 0 (fdmSpectrum.hpp) ------------------- */
+int nrg_fdm_create(nrg_run *run, int nops, nrg_fdm **out);     /* ctor + setOperator */
+int nrg_fdm_destroy(nrg_fdm *f);
+int nrg_fdm_calc(nrg_fdm *f, double energy_scale);               /* calcSpectrum :55-63 */
+/* saveFinalData (:322-337): energy points and the positive/negative weights,
+ * each nops x npts; npts = 100000 */
+int nrg_fdm_get(nrg_fdm *f, double *energy_points, double *positive, double *negative,
+                uint64_t npts);
+/* log-Gaussian broadening (examples/fdmSpectrumSiam/spec.py:27-44):
+ * out[k] = (1/w_k) sum_i weight_i exp(-(ln(w_k/e_i)/b - b/4)^2) / (b sqrt(pi)) */
+int nrg_broaden(nrg_engine *eng, const double *energies, const double *weights, uint64_t nbins,
+                const double *omegas, uint64_t nomega, double b, double *out);
+
+/* ---- thermodynamics (fdmThermodynamics.hpp) ---------------------------- */
+/* ctor (:26-38): nrg_iterations from the run, bath dimension from the bath */
+int nrg_thermo_create(nrg_run *run, const double *temps, int nt, nrg_thermo **out);
+int nrg_thermo_destroy(nrg_thermo *t);
+int nrg_thermo_calc(nrg_thermo *t, double energy_scale);        /* calcThermodynamics :42-89 */
+int nrg_thermo_final(nrg_thermo *t, double *entropy, double *specific_heat); /* :101-236 */
+
+/* ---- batched stepping of independent runs (one launch per phase) ------- */
+int nrg_batch_add_site(nrg_run *const *runs, int nruns, const double *t, int nt,
+                       const double *rescale);
+int nrg_batch_update_state(nrg_run *const *runs, int nruns);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* NRG_GPU_H */

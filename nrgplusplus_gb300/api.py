@@ -1,0 +1,458 @@
+"""Python host mirror of the reference's NRG API over the C ABI (libnrggpu.so).
+
+Names and argument meaning follow the reference:
+  NrgCore          nrgcore<Imp,Bath>                   nrgcore/nrgcore.hpp:25-551
+  update_system_operator                               nrgcore/sysOperator.hpp:36-133
+  NrgData          NrgData (device-resident snapshots)  nrgcore/nrgData.hpp:31-302
+  FdmSpectrum      fdmSpectrum<N>                        dynamics/fdmSpectrum.hpp:24-364
+  FdmThermodynamics fdmThermodynamics<N>                 static/fdmThermodynamics.hpp:16-260
+Errors raise RuntimeError like the reference's std::runtime_error.  There is
+no CPU fallback: without the library or a CUDA device every call raises.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIBPATH = os.path.join(_HERE, "libnrggpu.so")
+_lib = None
+
+PREC_FP64, PREC_MIXED = 0, 1
+FDM_POINTS = 100000
+
+
+class NrgError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("nrg error %d: %s" % (code, msg))
+        self.code = code
+
+
+class _EngineOpts(C.Structure):
+    _fields_ = [("device", C.c_int), ("precision", C.c_int), ("hbm_budget_bytes", C.c_uint64),
+                ("verbose", C.c_int)]
+
+
+class _SiteDesc(C.Structure):
+    _fields_ = [("nq", C.c_int), ("nsect", C.c_int), ("qnum", C.POINTER(C.c_int)),
+                ("dims", C.POINTER(C.c_int)), ("energies", C.POINTER(C.c_double)),
+                ("chi", C.POINTER(C.c_double)), ("nops", C.c_int), ("nblk", C.c_int),
+                ("blk_op", C.POINTER(C.c_int)), ("blk_row", C.POINTER(C.c_int)),
+                ("blk_col", C.POINTER(C.c_int)), ("blk_data", C.POINTER(C.c_double))]
+
+
+class _OpDesc(C.Structure):
+    _fields_ = [("nops", C.c_int), ("nblk", C.c_int), ("blk_op", C.POINTER(C.c_int)),
+                ("blk_row", C.POINTER(C.c_int)), ("blk_col", C.POINTER(C.c_int)),
+                ("blk_rows", C.POINTER(C.c_int)), ("blk_cols", C.POINTER(C.c_int)),
+                ("blk_data", C.POINTER(C.c_double))]
+
+
+class RunInfo(C.Structure):
+    _fields_ = [(n, C.c_int64) for n in (
+        "iteration", "iteration_min", "n_pre_sectors", "n_cur_sectors", "n_all", "n_kept",
+        "n_relgs", "nq", "n_device_blocks", "max_block", "n_snapshots", "device_bytes")]
+
+
+EXPORTS = [
+    "nrg_last_error", "nrg_engine_create", "nrg_engine_destroy", "nrg_engine_phase_times",
+    "nrg_engine_launch_count", "nrg_engine_sync", "nrg_run_create", "nrg_run_destroy",
+    "nrg_run_set_parameters", "nrg_run_set_bath", "nrg_run_add_site", "nrg_run_update_state",
+    "nrg_run_check_discarded", "nrg_run_get_info", "nrg_run_get_all_eigenvalues",
+    "nrg_run_get_relgs", "nrg_run_get_sectors", "nrg_run_get_eigenvalues_q", "nrg_run_get_kept",
+    "nrg_run_get_coupled", "nrg_run_get_eigenvectors", "nrg_run_get_fdag_block",
+    "nrg_opset_create", "nrg_opset_destroy", "nrg_opset_update", "nrg_opset_get_block",
+    "nrg_run_snapshot", "nrg_run_load_snapshot", "nrg_fdm_create", "nrg_fdm_destroy",
+    "nrg_fdm_calc", "nrg_fdm_get", "nrg_broaden", "nrg_thermo_create", "nrg_thermo_destroy",
+    "nrg_thermo_calc", "nrg_thermo_final", "nrg_batch_add_site", "nrg_batch_update_state",
+]
+
+
+def lib():
+    """Load libnrggpu.so (built in-tree by nrgplusplus_gb300.build).  Raises if
+    it is missing: the engine has no CPU fallback."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(_LIBPATH):
+            raise NrgError(6, "libnrggpu.so not built (run nrgplusplus_gb300.build)")
+        L = C.CDLL(_LIBPATH)
+        L.nrg_last_error.restype = C.c_char_p
+        for name in EXPORTS:
+            getattr(L, name)
+        _lib = L
+    return _lib
+
+
+def _call(fn, *args):
+    rc = fn(*args)
+    if rc != 0:
+        raise NrgError(rc, lib().nrg_last_error().decode())
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _ip(a):
+    return a.ctypes.data_as(C.POINTER(C.c_int))
+
+
+class _SiteBuffers:
+    """Keeps the numpy arrays behind one nrg_site_desc alive."""
+
+    def __init__(self, site, need_chi):
+        self.q = np.ascontiguousarray(np.array(site.qnums, dtype=np.int32).reshape(len(site.qnums), -1))
+        self.dims = np.array([len(e) for e in site.energies], dtype=np.int32)
+        self.E = np.ascontiguousarray(np.concatenate([np.asarray(e, float) for e in site.energies]))
+        self.chi = np.ascontiguousarray(np.asarray(site.chi, float)) if need_chi else None
+        ops, rows, cols, data = [], [], [], []
+        for ip, d in enumerate(site.fdag):
+            for (i, j), m in sorted(d.items()):
+                ops.append(ip)
+                rows.append(i)
+                cols.append(j)
+                data.append(np.ascontiguousarray(m, float).ravel())
+        self.op = np.array(ops, dtype=np.int32)
+        self.row = np.array(rows, dtype=np.int32)
+        self.col = np.array(cols, dtype=np.int32)
+        self.data = np.ascontiguousarray(np.concatenate(data) if data else np.zeros(1))
+        self.desc = _SiteDesc(self.q.shape[1], len(self.dims), _ip(self.q), _ip(self.dims), _dp(self.E),
+                              _dp(self.chi) if self.chi is not None else None, len(site.fdag),
+                              len(self.op), _ip(self.op), _ip(self.row), _ip(self.col), _dp(self.data))
+
+
+class Engine:
+    """One GPU engine: device context, stream and allocator (nrg_engine)."""
+
+    def __init__(self, precision=PREC_FP64, device=0, hbm_budget_bytes=0):
+        self.h = C.c_void_p()
+        opts = _EngineOpts(device, precision, hbm_budget_bytes, 0)
+        _call(lib().nrg_engine_create, C.byref(opts), C.byref(self.h))
+        self.precision = precision
+
+    def close(self):
+        if self.h:
+            lib().nrg_engine_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def phase_times(self):
+        out = (C.c_double * 8)()
+        n = C.c_int()
+        _call(lib().nrg_engine_phase_times, self.h, out, 8, C.byref(n))
+        return list(out)[:n.value]
+
+    def launch_count(self):
+        v = C.c_uint64()
+        _call(lib().nrg_engine_launch_count, self.h, C.byref(v))
+        return v.value
+
+    def sync(self):
+        _call(lib().nrg_engine_sync, self.h)
+
+    def broaden(self, energies, weights, omegas, b):
+        e = np.ascontiguousarray(energies, float)
+        w = np.ascontiguousarray(weights, float)
+        o = np.ascontiguousarray(omegas, float)
+        out = np.zeros(len(o))
+        _call(lib().nrg_broaden, self.h, _dp(e), _dp(w), C.c_uint64(len(e)), _dp(o),
+              C.c_uint64(len(o)), C.c_double(b), _dp(out))
+        return out
+
+
+class NrgCore:
+    """nrgcore<Imp,Bath> on the GPU (nrgcore/nrgcore.hpp)."""
+
+    def __init__(self, engine, impurity, bath, nkeep=1024):
+        self.engine = engine
+        self._imp = _SiteBuffers(impurity, False)
+        self._bath = _SiteBuffers(bath, True)
+        self.nops = len(impurity.fdag)
+        self.h = C.c_void_p()
+        _call(lib().nrg_run_create, engine.h, C.byref(self._imp.desc), C.byref(self._bath.desc),
+              C.c_uint64(nkeep), C.byref(self.h))
+
+    def close(self):
+        if self.h:
+            lib().nrg_run_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- the iteration (nrgcore.hpp:65-109, 336-342)
+    def set_parameters(self, n=1024):
+        _call(lib().nrg_run_set_parameters, self.h, C.c_uint64(n))
+
+    def set_bath(self, bath):
+        self._bath_next = _SiteBuffers(bath, True)
+        _call(lib().nrg_run_set_bath, self.h, C.byref(self._bath_next.desc))
+
+    def add_bath_site(self, t, rescale):
+        t = np.ascontiguousarray(t, float)
+        _call(lib().nrg_run_add_site, self.h, _dp(t), len(t), C.c_double(rescale))
+
+    def update_internal_state(self):
+        _call(lib().nrg_run_update_state, self.h)
+
+    def checkHigherEnergyDiscarded(self):
+        v = C.c_int()
+        _call(lib().nrg_run_check_discarded, self.h, C.byref(v))
+        return bool(v.value)
+
+    # -- public state (nrgcore.hpp:518-550)
+    def info(self):
+        i = RunInfo()
+        _call(lib().nrg_run_get_info, self.h, C.byref(i))
+        return i
+
+    @property
+    def nrg_iterations_cnt(self):
+        return self.info().iteration
+
+    @property
+    def nrg_iterations_min(self):
+        return self.info().iteration_min
+
+    @property
+    def all_eigenvalue(self):
+        n = self.info().n_all
+        out = np.zeros(n)
+        _call(lib().nrg_run_get_all_eigenvalues, self.h, _dp(out), C.c_uint64(n))
+        return out
+
+    @property
+    def relativeGroundStateEnergy(self):
+        n = self.info().n_relgs
+        out = np.zeros(max(n, 1))
+        _call(lib().nrg_run_get_relgs, self.h, _dp(out), C.c_uint64(n))
+        return out[:n]
+
+    def _sectors(self, which):
+        inf = self.info()
+        n = inf.n_cur_sectors if which == 0 else inf.n_pre_sectors
+        out = np.zeros((max(n, 1), inf.nq), dtype=np.int32)
+        _call(lib().nrg_run_get_sectors, self.h, which, _ip(out), C.c_uint64(n))
+        return [tuple(int(x) for x in r) for r in out[:n]]
+
+    @property
+    def current_sysmQ(self):
+        return self._sectors(0)
+
+    @property
+    def pre_sysmQ(self):
+        return self._sectors(1)
+
+    @property
+    def eigenvaluesQ(self):
+        inf = self.info()
+        nsec = inf.n_cur_sectors if inf.n_cur_sectors else inf.n_pre_sectors
+        dims = np.zeros(max(nsec, 1), dtype=np.uint64)
+        _call(lib().nrg_run_get_eigenvalues_q, self.h, dims.ctypes.data_as(C.POINTER(C.c_uint64)),
+              None, C.c_uint64(0))
+        tot = int(dims[:nsec].sum())
+        vals = np.zeros(max(tot, 1))
+        _call(lib().nrg_run_get_eigenvalues_q, self.h, dims.ctypes.data_as(C.POINTER(C.c_uint64)),
+              _dp(vals), C.c_uint64(tot))
+        out, o = [], 0
+        for d in dims[:nsec]:
+            out.append(vals[o:o + int(d)].copy())
+            o += int(d)
+        return out
+
+    @property
+    def kept_counts(self):
+        """Sizes of eigenvaluesQ_kept_indices (each is the prefix 0..k-1)."""
+        n = self.info().n_pre_sectors
+        out = np.zeros(max(n, 1), dtype=np.uint64)
+        _call(lib().nrg_run_get_kept, self.h, out.ctypes.data_as(C.POINTER(C.c_uint64)), C.c_uint64(n))
+        return [int(x) for x in out[:n]]
+
+    @property
+    def eigenvaluesQ_kept_indices(self):
+        return [list(range(k)) for k in self.kept_counts]
+
+    @property
+    def coupled_nQ_index(self):
+        n = self.info().n_cur_sectors or len(self.current_sysmQ)
+        counts = np.zeros(max(n, 1), dtype=np.uint64)
+        _call(lib().nrg_run_get_coupled, self.h, counts.ctypes.data_as(C.POINTER(C.c_uint64)), None,
+              C.c_uint64(0))
+        tot = int(counts[:n].sum())
+        ent = np.zeros(max(tot, 1), dtype=np.uint64)
+        _call(lib().nrg_run_get_coupled, self.h, counts.ctypes.data_as(C.POINTER(C.c_uint64)),
+              ent.ctypes.data_as(C.POINTER(C.c_uint64)), C.c_uint64(tot))
+        out, o = [], 0
+        for c in counts[:n]:
+            out.append([int(x) for x in ent[o:o + int(c)]])
+            o += int(c)
+        return out
+
+    def current_hamiltonQ(self, sector):
+        """Eigenvectors (columns) of one sector, row-major n x n."""
+        dims = [len(e) for e in self.eigenvaluesQ]
+        n = dims[sector]
+        out = np.zeros((n, n))
+        if n:
+            _call(lib().nrg_run_get_eigenvectors, self.h, C.c_int64(sector), _dp(out), C.c_uint64(n * n))
+        return out
+
+    def fdag_block(self, ip, i, j):
+        """Kept x kept block (i, j) of the rotated f-dagger (get_f_dag_operator)."""
+        r, c = C.c_int64(), C.c_int64()
+        _call(lib().nrg_run_get_fdag_block, self.h, ip, C.c_int64(i), C.c_int64(j), None,
+              C.c_uint64(0), C.byref(r), C.byref(c))
+        if r.value == 0 or c.value == 0:
+            return None
+        out = np.zeros((r.value, c.value))
+        _call(lib().nrg_run_get_fdag_block, self.h, ip, C.c_int64(i), C.c_int64(j), _dp(out),
+              C.c_uint64(out.size), C.byref(r), C.byref(c))
+        return out
+
+
+class OperatorSet:
+    """Block-sparse operators tracked through the iteration (a device-resident
+    vector<qOperator>), given in the run's current previous basis."""
+
+    def __init__(self, run, ops):
+        self.run = run
+        self.nops = len(ops)
+        opi, rows, cols, nr, nc, data = [], [], [], [], [], []
+        for ip, d in enumerate(ops):
+            for (i, j), m in sorted(d.items()):
+                m = np.ascontiguousarray(m, float)
+                opi.append(ip)
+                rows.append(i)
+                cols.append(j)
+                nr.append(m.shape[0])
+                nc.append(m.shape[1])
+                data.append(m.ravel())
+        arrs = [np.array(x, dtype=np.int32) for x in (opi, rows, cols, nr, nc)]
+        self._keep = arrs + [np.ascontiguousarray(np.concatenate(data) if data else np.zeros(1))]
+        desc = _OpDesc(self.nops, len(opi), *[_ip(a) for a in arrs], _dp(self._keep[-1]))
+        self.h = C.c_void_p()
+        _call(lib().nrg_opset_create, run.h, C.byref(desc), C.byref(self.h))
+
+    def block(self, ip, i, j):
+        r, c = C.c_int64(), C.c_int64()
+        _call(lib().nrg_opset_get_block, self.h, ip, C.c_int64(i), C.c_int64(j), None, C.c_uint64(0),
+              C.byref(r), C.byref(c))
+        if r.value == 0 or c.value == 0:
+            return None
+        out = np.zeros((r.value, c.value))
+        _call(lib().nrg_opset_get_block, self.h, ip, C.c_int64(i), C.c_int64(j), _dp(out),
+              C.c_uint64(out.size), C.byref(r), C.byref(c))
+        return out
+
+    def close(self):
+        if self.h:
+            lib().nrg_opset_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def update_system_operator(run, opset):
+    """update_system_operator(nrg, ops) (sysOperator.hpp:36-133)."""
+    _call(lib().nrg_opset_update, opset.h)
+
+
+class NrgData:
+    """Device-resident stand-in for NrgData (nrgData.hpp): saveCurrentData /
+    saveqOperator keep the site on the device; loadCurrentData selects it."""
+
+    def __init__(self, run):
+        self.run = run
+
+    def saveCurrentData(self, opset=None):
+        _call(lib().nrg_run_snapshot, self.run.h, opset.h if opset is not None else None)
+
+    def loadCurrentData(self, iteration=None):
+        it = self.run.nrg_iterations_cnt if iteration is None else iteration
+        _call(lib().nrg_run_load_snapshot, self.run.h, C.c_int64(it))
+
+
+class FdmSpectrum:
+    """fdmSpectrum<N> at T = 0 (dynamics/fdmSpectrum.hpp)."""
+
+    def __init__(self, run, nops):
+        self.run = run
+        self.nops = nops
+        self.h = C.c_void_p()
+        _call(lib().nrg_fdm_create, run.h, nops, C.byref(self.h))
+
+    def calcSpectrum(self, energy_scale):
+        _call(lib().nrg_fdm_calc, self.h, C.c_double(energy_scale))
+
+    def saveFinalData(self):
+        e = np.zeros(FDM_POINTS)
+        p = np.zeros((self.nops, FDM_POINTS))
+        n = np.zeros((self.nops, FDM_POINTS))
+        _call(lib().nrg_fdm_get, self.h, _dp(e), _dp(p), _dp(n), C.c_uint64(FDM_POINTS))
+        return {"GreenFnEnergyPoints": e, "GreenFnPositiveWeight": p, "GreenFnNegativeWeight": n}
+
+    def close(self):
+        if self.h:
+            lib().nrg_fdm_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class FdmThermodynamics:
+    """fdmThermodynamics<N> (static/fdmThermodynamics.hpp)."""
+
+    def __init__(self, run, temps):
+        self.run = run
+        self.temps = np.ascontiguousarray(temps, float)
+        self.h = C.c_void_p()
+        _call(lib().nrg_thermo_create, run.h, _dp(self.temps), len(self.temps), C.byref(self.h))
+
+    def calcThermodynamics(self, energy_scale):
+        _call(lib().nrg_thermo_calc, self.h, C.c_double(energy_scale))
+
+    def saveFinalData(self):
+        s = np.zeros(len(self.temps))
+        c = np.zeros(len(self.temps))
+        _call(lib().nrg_thermo_final, self.h, _dp(s), _dp(c))
+        return {"temperatureArray": self.temps.copy(), "entropy": s, "specificHeat": c}
+
+    def close(self):
+        if self.h:
+            lib().nrg_thermo_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def batch_add_site(runs, t, rescale):
+    """One add_bath_site for many independent runs with one launch per phase."""
+    arr = (C.c_void_p * len(runs))(*[r.h.value for r in runs])
+    t = np.ascontiguousarray(t, float).reshape(len(runs), -1)
+    rs = np.ascontiguousarray(rescale, float)
+    _call(lib().nrg_batch_add_site, arr, len(runs), _dp(t), t.shape[1], _dp(rs))
+
+
+def batch_update_state(runs):
+    arr = (C.c_void_p * len(runs))(*[r.h.value for r in runs])
+    _call(lib().nrg_batch_update_state, arr, len(runs))

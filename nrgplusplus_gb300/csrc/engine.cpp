@@ -1,0 +1,633 @@
+// Host side of the GB300 NRG engine: basis bookkeeping, descriptor tables and
+// the launch sequence of one NRG site for a batch of independent runs.
+//
+// Reference correspondence (srbhp/nrgplusplus):
+//   create_next_basis         nrgcore.hpp:238-261   -> build_basis()
+//   create_next_hamiltonians  nrgcore.hpp:146-230   -> k_assemble (k_assemble.cu)
+//   qmatrix::diag per block   nrgcore.hpp:85-89     -> k_eig (k_eig.cu)
+//   discard_higher_energies   nrgcore.hpp:269-327   -> k_rank/k_select (k_trunc.cu)
+//   set_current_fdag_operator nrgcore.hpp:401-477   -> grouped GEMM (k_gemm.cu)
+//   update_internal_state     nrgcore.hpp:105-109   -> nrg_run_update_state
+//
+// Empty sectors (no kept states) stay in the API-level sector lists exactly as
+// the reference keeps them, but never reach the device.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+#include <stdexcept>
+
+#include "engine_core.h"
+
+namespace nrg {
+
+thread_local std::string g_err;
+
+[[noreturn]] void fail(int code, const std::string &msg) { throw Error{code, msg}; }
+
+void check_cuda(cudaError_t e, const char *what) {
+  if (e != cudaSuccess)
+    fail(e == cudaErrorMemoryAllocation ? NRG_E_NOMEM : NRG_E_CUDA,
+         std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+DevMem::~DevMem() {
+  if (ptr) {
+    cudaFreeAsync(ptr, eng->stream);
+    eng->used -= bytes;
+  }
+}
+
+static DevPtr dalloc(nrg_engine *e, size_t bytes) {
+  auto m = std::make_shared<DevMem>();
+  m->eng = e;
+  if (bytes == 0) return m;
+  bytes = (bytes + 255) & ~size_t(255);
+  if (e->budget && e->used + bytes > e->budget)
+    fail(NRG_E_NOMEM, "HBM budget exhausted (" + std::to_string(e->used + bytes) + " > " +
+                          std::to_string(e->budget) + " bytes)");
+  check_cuda(cudaMallocAsync(&m->ptr, bytes, e->stream), "cudaMallocAsync");
+  m->bytes = bytes;
+  e->used += bytes;
+  return m;
+}
+
+// Host staging of the descriptor tables of one launch phase: one device
+// buffer and one copy per phase.
+struct Arena {
+  std::vector<char> buf;
+  template <class T> size_t add(const std::vector<T> &v) {
+    size_t off = (buf.size() + 255) & ~size_t(255);
+    buf.resize(off + v.size() * sizeof(T) + 16);
+    if (!v.empty()) std::memcpy(buf.data() + off, v.data(), v.size() * sizeof(T));
+    return off;
+  }
+  char *push(nrg_engine *e, DevPtr &hold) {
+    hold = dalloc(e, buf.size());
+    if (!buf.empty())
+      check_cuda(cudaMemcpyAsync(hold->ptr, buf.data(), buf.size(), cudaMemcpyHostToDevice, e->stream),
+                 "descriptor upload");
+    return static_cast<char *>(hold->ptr);
+  }
+};
+
+template <class T> static T *at(char *base, size_t off) { return reinterpret_cast<T *>(base + off); }
+
+static void count_launch(nrg_engine *e, int n = 1) { e->launches += n; }
+
+static void post_launch(const char *what) { check_cuda(cudaGetLastError(), what); }
+
+// ---------------------------------------------------------------- models
+static SiteModel parse_site(const nrg_site_desc *d, bool need_chi) {
+  if (!d) fail(NRG_E_ARG, "null site description");
+  if (d->nq <= 0 || d->nsect <= 0) fail(NRG_E_ARG, "site needs nq > 0 and nsect > 0");
+  if (!d->qnum || !d->dims || !d->energies) fail(NRG_E_ARG, "site arrays missing");
+  if (need_chi && !d->chi) fail(NRG_E_ARG, "bath site needs chi (fermion parity per sector)");
+  SiteModel m;
+  m.nq = d->nq;
+  m.q.resize(d->nsect);
+  m.E.resize(d->nsect);
+  int64_t eo = 0;
+  for (int s = 0; s < d->nsect; ++s) {
+    m.q[s].assign(d->qnum + int64_t(s) * d->nq, d->qnum + int64_t(s + 1) * d->nq);
+    if (d->dims[s] < 0) fail(NRG_E_ARG, "negative sector dimension");
+    m.E[s].assign(d->energies + eo, d->energies + eo + d->dims[s]);
+    eo += d->dims[s];
+  }
+  if (d->chi) m.chi.assign(d->chi, d->chi + d->nsect);
+  m.nops = d->nops;
+  m.op.resize(std::max(0, d->nops));
+  int64_t bo = 0;
+  for (int b = 0; b < d->nblk; ++b) {
+    int ip = d->blk_op[b], r = d->blk_row[b], c = d->blk_col[b];
+    if (ip < 0 || ip >= d->nops || r < 0 || r >= d->nsect || c < 0 || c >= d->nsect)
+      fail(NRG_E_ARG, "operator block index out of range");
+    HostMat hm;
+    hm.rows = d->dims[r];
+    hm.cols = d->dims[c];
+    hm.v.assign(d->blk_data + bo, d->blk_data + bo + int64_t(hm.rows) * hm.cols);
+    bo += int64_t(hm.rows) * hm.cols;
+    if (m.op[ip].count({r, c})) fail(NRG_E_ARG, "Found operator already");  // qOperator.hpp:58
+    m.op[ip][{r, c}] = std::move(hm);
+  }
+  return m;
+}
+
+static void upload_bath(nrg_engine *e, SiteModel &m) {
+  std::vector<double> flat;
+  m.e_off.clear();
+  for (auto &v : m.E) {
+    m.e_off.push_back(int64_t(flat.size()));
+    flat.insert(flat.end(), v.begin(), v.end());
+  }
+  m.op_off.assign(m.op.size(), {});
+  for (size_t ip = 0; ip < m.op.size(); ++ip)
+    for (auto &kv : m.op[ip]) {
+      m.op_off[ip][kv.first] = int64_t(flat.size());
+      flat.insert(flat.end(), kv.second.v.begin(), kv.second.v.end());
+    }
+  m.dev = dalloc(e, flat.size() * sizeof(double) + 8);
+  check_cuda(cudaMemcpyAsync(m.dev->ptr, flat.data(), flat.size() * sizeof(double),
+                             cudaMemcpyHostToDevice, e->stream),
+             "bath upload");
+  check_cuda(cudaStreamSynchronize(e->stream), "bath upload");
+}
+
+static const double *bath_ptr(const SiteModel &m, int64_t off) {
+  return static_cast<const double *>(m.dev->ptr) + off;
+}
+
+// --------------------------------------------------------------- step
+struct RunStep {          // per-run working data of one batched add_site
+  nrg_run *run;
+  std::shared_ptr<SiteData> site;
+  std::vector<double> t;
+  double rescale;
+  std::map<std::pair<int, int>, std::pair<int, int>> sub_of;  // (ii,bb) -> (sector, off)
+  int b0 = 0, e0 = 0, e1 = 0;  // device block / element ranges in the batch
+};
+
+static void reference_discard(nrg_run *r, std::vector<std::vector<double>> &E) {
+  // host restatement of discard_higher_energies for the impurity step (cnt == 0)
+  std::vector<double> all;
+  for (auto &v : E) all.insert(all.end(), v.begin(), v.end());
+  std::sort(all.begin(), all.end());
+  r->all_eig = all;
+  r->kept.clear();
+  const double emin = all.empty() ? 0.0 : all[0];
+  if (all.size() <= r->nkeep) {
+    for (auto &v : E) r->kept.push_back(int64_t(v.size()));
+  } else {
+    const double thr = all[r->nkeep];
+    for (auto &v : E) {
+      int64_t k = 0;
+      for (double x : v)
+        if (x < thr + 1e-8) ++k;
+      r->kept.push_back(k);
+    }
+  }
+  r->no_of_kept = std::accumulate(r->kept.begin(), r->kept.end(), int64_t(0));
+  r->prev_shift = 0.0;
+  if (r->no_of_kept <= int64_t(r->nkeep)) {
+    r->cnt_min = r->cnt;
+  } else {
+    r->relgs.push_back(emin);
+    r->prev_shift = emin;
+  }
+}
+
+static void init_from_impurity(nrg_run *r) {
+  nrg_engine *e = r->eng;
+  r->pre_q = r->imp.q;
+  auto E = r->imp.E;
+  reference_discard(r, E);
+  // previous-site device data: impurity energies and kept f-dagger blocks
+  auto sd = std::make_shared<SiteData>();
+  std::vector<double> flat;
+  std::vector<int64_t> eoff;
+  for (auto &v : r->imp.E) {
+    eoff.push_back(int64_t(flat.size()));
+    flat.insert(flat.end(), v.begin(), v.end());
+  }
+  std::vector<int64_t> foff;
+  std::vector<OpKey> fkeys;
+  std::vector<std::pair<int, int>> fdims;
+  for (int ip = 0; ip < r->imp.nops; ++ip)
+    for (auto &kv : r->imp.op[ip]) {
+      int ii = kv.first.first, jj = kv.first.second;
+      int k = int(r->kept[ii]), kp = int(r->kept[jj]);
+      if (k == 0 || kp == 0) continue;
+      fkeys.push_back({ip, ii, jj});
+      fdims.push_back({k, kp});
+      foff.push_back(int64_t(flat.size()));
+      for (int a = 0; a < k; ++a)
+        for (int b = 0; b < kp; ++b) flat.push_back(kv.second.v[int64_t(a) * kv.second.cols + b]);
+    }
+  sd->mem_E = dalloc(e, flat.size() * sizeof(double) + 8);
+  check_cuda(cudaMemcpyAsync(sd->mem_E->ptr, flat.data(), flat.size() * sizeof(double),
+                             cudaMemcpyHostToDevice, e->stream),
+             "impurity upload");
+  double *base = static_cast<double *>(sd->mem_E->ptr);
+  r->prevE.assign(r->imp.E.size(), nullptr);
+  for (size_t s = 0; s < r->imp.E.size(); ++s)
+    if (!r->imp.E[s].empty()) r->prevE[s] = base + eoff[s];
+  sd->E_host = r->imp.E;
+  r->prev_site = sd;
+  r->fprev.clear();
+  for (size_t i = 0; i < fkeys.size(); ++i)
+    r->fprev[fkeys[i]] = FBlock{base + foff[i], fdims[i].first, fdims[i].second, fdims[i].second};
+  r->fprev_mem = sd->mem_E;
+  r->prevE_host = r->imp.E;
+  for (auto &v : r->prevE_host)
+    for (auto &x : v) x -= r->prev_shift;
+  check_cuda(cudaStreamSynchronize(e->stream), "impurity upload");
+}
+
+static void build_basis(RunStep &st) {
+  nrg_run *r = st.run;
+  const SiteModel &bath = r->bath;
+  auto sd = std::make_shared<SiteData>();
+  sd->iteration = r->cnt;
+  sd->pre_q = r->pre_q;
+  sd->kept_prev = r->kept;
+  const int nb = int(bath.q.size());
+  std::map<std::vector<int>, int> where;
+  for (size_t i = 0; i < r->pre_q.size(); ++i)
+    for (int j = 0; j < nb; ++j) {
+      std::vector<int> tm = r->pre_q[i];
+      if (tm.size() != bath.q[j].size()) fail(NRG_E_ARG, "quantum number count differs between impurity and bath");
+      for (size_t x = 0; x < tm.size(); ++x) tm[x] += bath.q[j][x];
+      auto it = where.find(tm);
+      if (it != where.end()) {
+        sd->coupled[it->second].push_back(uint64_t(i) * nb + j);
+      } else {
+        where[tm] = int(sd->cur_q.size());
+        sd->cur_q.push_back(tm);
+        sd->coupled.push_back({uint64_t(i) * nb + j});
+      }
+    }
+  sd->sectors.resize(sd->cur_q.size());
+  for (size_t s = 0; s < sd->cur_q.size(); ++s) {
+    int off = 0;
+    Sector &S = sd->sectors[s];
+    for (uint64_t kidx : sd->coupled[s]) {
+      int ii = int(kidx / nb), bb = int(kidx % nb);
+      int k = int(r->kept[ii]), d = int(bath.E[bb].size());
+      if (k * d > 0) {
+        S.subs.push_back({ii, bb, off, k, d});
+        st.sub_of[{ii, bb}] = {int(s), off};
+      }
+      off += k * d;
+    }
+    S.n = off;
+  }
+  st.site = sd;
+}
+
+static int round_up(int x, int m) { return (x + m - 1) / m * m; }
+
+static void batch_add_site(nrg_run *const *runs, int nruns, const double *t, int nt,
+                           const double *rescale) {
+  if (nruns <= 0) return;
+  nrg_engine *e = runs[0]->eng;
+  for (int i = 0; i < nruns; ++i) {
+    if (!runs[i]) fail(NRG_E_ARG, "null run");
+    if (runs[i]->eng != e) fail(NRG_E_ARG, "runs of one batch must share an engine");
+    if (runs[i]->have_site) fail(NRG_E_STATE, "add_site called twice without update_state");
+  }
+  cudaStream_t s = e->stream;
+  std::vector<RunStep> steps(nruns);
+  for (int i = 0; i < nruns; ++i) {
+    nrg_run *r = runs[i];
+    if (r->bath_pending) {  // bath refresh, nrgcore.hpp:68-70
+      r->bath = std::move(r->bath_next);
+      r->bath_pending = false;
+      upload_bath(e, r->bath);
+    }
+    if (nt != r->bath.nops || nt != int(r->imp.nops))
+      fail(NRG_E_ARG, "t_hopping " + std::to_string(nt) + " =! pre_fdag_oparator " +
+                          std::to_string(r->imp.nops));  // nrgcore.hpp:148-152
+    if (r->cnt == 0) init_from_impurity(r);
+    steps[i].run = r;
+    steps[i].t.assign(t + int64_t(i) * nt, t + int64_t(i + 1) * nt);
+    steps[i].rescale = rescale[i];
+    build_basis(steps[i]);
+  }
+  // ---- device blocks and buffers
+  std::vector<AsmBlock> ablk;
+  std::vector<AsmSub> asub;
+  std::vector<int2> apair;
+  std::vector<AsmTerm> aterm;
+  std::vector<EigBlock> eblk;
+  std::vector<TruncRun> trun;
+  std::vector<TruncBlock> tblk;
+  std::vector<int> elem_block, block_run;
+  int64_t chunks = 0;
+  int max_n = 0;
+  int nblk_total = 0, nelem_total = 0;
+  std::vector<DevPtr> hold;
+  for (int i = 0; i < nruns; ++i) {
+    RunStep &st = steps[i];
+    nrg_run *r = st.run;
+    SiteData &sd = *st.site;
+    int64_t hsz = 0, esz = 0;
+    for (size_t sidx = 0; sidx < sd.sectors.size(); ++sidx) {
+      Sector &S = sd.sectors[sidx];
+      if (S.n == 0) continue;
+      DevBlock db;
+      db.sector = int(sidx);
+      db.n = S.n;
+      db.ld = round_up(S.n, 2);
+      S.dev = int(sd.blocks.size());
+      sd.blocks.push_back(db);
+      hsz += int64_t(db.n) * db.ld;
+      esz += db.n;
+    }
+    auto memH = dalloc(e, hsz * sizeof(double));
+    sd.mem_U = dalloc(e, hsz * sizeof(double));
+    sd.mem_E = dalloc(e, esz * sizeof(double) + 8);
+    r->mem_H = memH;
+    int64_t ho = 0, eo = 0;
+    for (auto &db : sd.blocks) {
+      db.H = static_cast<double *>(memH->ptr) + ho;
+      db.U = static_cast<double *>(sd.mem_U->ptr) + ho;
+      db.E = static_cast<double *>(sd.mem_E->ptr) + eo;
+      ho += int64_t(db.n) * db.ld;
+      eo += db.n;
+    }
+    r->mem_sorted = dalloc(e, esz * sizeof(double) + 8);
+    st.b0 = nblk_total;
+    st.e0 = nelem_total;
+    // assembly descriptors
+    for (auto &db : sd.blocks) {
+      const Sector &S = sd.sectors[db.sector];
+      AsmBlock ab{};
+      ab.H = db.H;
+      ab.n = db.n;
+      ab.ld = db.ld;
+      ab.sub0 = int(asub.size());
+      ab.nsub = int(S.subs.size());
+      ab.pair0 = int(apair.size());
+      ab.chunk0 = chunks;
+      ab.rescale = st.rescale;
+      ab.shift = r->prev_shift;
+      chunks += (int64_t(db.n) * db.n + 1023) / 1024;
+      for (auto &sb : S.subs) {
+        AsmSub a{};
+        a.off = sb.off;
+        a.k = sb.k;
+        a.d = sb.d;
+        a.eprev = r->prevE[sb.ii];
+        a.ebath = bath_ptr(r->bath, r->bath.e_off[sb.bb]);
+        asub.push_back(a);
+      }
+      const int ns = int(S.subs.size());
+      for (int sa = 0; sa < ns; ++sa)
+        for (int sb = 0; sb < ns; ++sb) {
+          int2 rg;
+          rg.x = int(aterm.size());
+          const Sub &A = S.subs[sa], &B = S.subs[sb];
+          for (int ip = 0; ip < r->bath.nops; ++ip) {
+            auto f = r->fprev.find(OpKey{ip, A.ii, B.ii});
+            if (f == r->fprev.end()) continue;
+            auto fb = r->bath.op_off[ip].find({B.bb, A.bb});
+            if (fb == r->bath.op_off[ip].end()) continue;
+            AsmTerm tm{};
+            tm.F = f->second.p;
+            tm.ldf = f->second.ld;
+            tm.fb = bath_ptr(r->bath, fb->second);
+            tm.chi = r->bath.chi[B.bb];
+            tm.t = st.t[ip];
+            aterm.push_back(tm);
+          }
+          rg.y = int(aterm.size());
+          apair.push_back(rg);
+        }
+      ablk.push_back(ab);
+      EigBlock eb{};
+      eb.H = db.H;
+      eb.U = db.U;
+      eb.E = db.E;
+      eb.W = nullptr;
+      eb.n = db.n;
+      eb.ld = db.ld;
+      eb.ldu = db.ld;
+      eblk.push_back(eb);
+      max_n = std::max(max_n, db.n);
+      TruncBlock tb{};
+      tb.E = db.E;
+      tb.n = db.n;
+      tb.e0 = nelem_total;
+      for (int x = 0; x < db.n; ++x) elem_block.push_back(nblk_total);
+      block_run.push_back(i);
+      tblk.push_back(tb);
+      nelem_total += db.n;
+      ++nblk_total;
+    }
+    st.e1 = nelem_total;
+    TruncRun tr{};
+    tr.b0 = st.b0;
+    tr.b1 = nblk_total;
+    tr.e0 = st.e0;
+    tr.e1 = st.e1;
+    tr.nkeep = int64_t(r->nkeep);
+    tr.sorted = static_cast<double *>(r->mem_sorted->ptr);
+    trun.push_back(tr);
+    if (st.e1 == st.e0) fail(NRG_E_STATE, "no states left in the basis");
+  }
+  // eigensolver order: largest blocks first
+  std::vector<int> order(eblk.size());
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return eblk[a].n > eblk[b].n; });
+  std::vector<EigBlock> eblk_sorted;
+  for (int o : order) eblk_sorted.push_back(eblk[o]);
+  elem_block.insert(elem_block.end(), block_run.begin(), block_run.end());
+
+  Arena ar;
+  size_t o_ablk = ar.add(ablk), o_asub = ar.add(asub), o_apair = ar.add(apair),
+         o_aterm = ar.add(aterm), o_eblk = ar.add(eblk_sorted), o_trun = ar.add(trun),
+         o_tblk = ar.add(tblk), o_elem = ar.add(elem_block);
+  std::vector<int> zeros(nblk_total + 1, 0);
+  size_t o_kept = ar.add(zeros);
+  std::vector<TruncResult> tres(nruns);
+  size_t o_tres = ar.add(tres);
+  std::vector<int> stat(eblk_sorted.size() + 1, 0);
+  size_t o_stat = ar.add(stat);
+  DevPtr desc;
+  char *d = ar.push(e, desc);
+  hold.push_back(desc);
+
+  check_cuda(cudaEventRecord(e->ev[0], s), "event");
+  launch_assemble(at<AsmBlock>(d, o_ablk), int(ablk.size()), chunks, at<AsmSub>(d, o_asub),
+                  at<int2>(d, o_apair), at<AsmTerm>(d, o_aterm), s);
+  count_launch(e);
+  post_launch("assemble");
+  check_cuda(cudaEventRecord(e->ev[1], s), "event");
+  if (e->precision == NRG_PREC_FP64) {
+    launch_eig_f64(at<EigBlock>(d, o_eblk), int(eblk_sorted.size()), max_n, e->eig_smem_f64,
+                   at<int>(d, o_stat), s);
+  } else {
+    fail(NRG_E_ARG, "mixed precision path not available in this build");
+  }
+  count_launch(e);
+  post_launch("eigensolve");
+  check_cuda(cudaEventRecord(e->ev[2], s), "event");
+  launch_truncate(at<TruncRun>(d, o_trun), nruns, at<TruncBlock>(d, o_tblk), nblk_total,
+                  at<int>(d, o_elem), nelem_total, at<int>(d, o_kept), at<TruncResult>(d, o_tres), s);
+  count_launch(e, 2);
+  post_launch("truncate");
+  check_cuda(cudaEventRecord(e->ev[3], s), "event");
+  // results back to the host: kept per block, run results, solver status,
+  // sorted eigenvalues and per-block eigenvalues
+  std::vector<int> kept_blk(nblk_total);
+  check_cuda(cudaMemcpyAsync(kept_blk.data(), d + o_kept, nblk_total * sizeof(int),
+                             cudaMemcpyDeviceToHost, s), "kept D2H");
+  check_cuda(cudaMemcpyAsync(tres.data(), d + o_tres, nruns * sizeof(TruncResult),
+                             cudaMemcpyDeviceToHost, s), "result D2H");
+  check_cuda(cudaMemcpyAsync(stat.data(), d + o_stat, eblk_sorted.size() * sizeof(int),
+                             cudaMemcpyDeviceToHost, s), "status D2H");
+  std::vector<std::vector<double>> sorted(nruns), evals(nruns);
+  for (int i = 0; i < nruns; ++i) {
+    RunStep &st = steps[i];
+    sorted[i].resize(st.e1 - st.e0);
+    evals[i].resize(st.e1 - st.e0);
+    check_cuda(cudaMemcpyAsync(sorted[i].data(), st.run->mem_sorted->ptr,
+                               sorted[i].size() * sizeof(double), cudaMemcpyDeviceToHost, s),
+               "sorted D2H");
+    check_cuda(cudaMemcpyAsync(evals[i].data(), st.site->mem_E->ptr, evals[i].size() * sizeof(double),
+                               cudaMemcpyDeviceToHost, s),
+               "eigenvalues D2H");
+  }
+  check_cuda(cudaStreamSynchronize(s), "site step");
+  for (size_t b = 0; b < eblk_sorted.size(); ++b)
+    if (stat[b]) fail(NRG_E_EIG, "block eigensolver did not converge (n = " +
+                                     std::to_string(eblk_sorted[b].n) + ")");
+  // ---- pending truncation per run + rotation descriptors
+  std::vector<GemmGroup> groups;
+  std::vector<GemmContrib> contribs;
+  std::vector<GemmTile> tiles;
+  for (int i = 0; i < nruns; ++i) {
+    RunStep &st = steps[i];
+    nrg_run *r = st.run;
+    SiteData &sd = *st.site;
+    r->tres = tres[i];
+    r->all_eig_pending = std::move(sorted[i]);
+    r->kept_new.assign(sd.sectors.size(), 0);
+    sd.E_host.assign(sd.sectors.size(), {});
+    int64_t eo = 0;
+    for (size_t b = 0; b < sd.blocks.size(); ++b) {
+      const DevBlock &db = sd.blocks[b];
+      r->kept_new[db.sector] = kept_blk[st.b0 + int(b)];
+      sd.E_host[db.sector].assign(evals[i].begin() + eo, evals[i].begin() + eo + db.n);
+      eo += db.n;
+    }
+    // f-dagger rotation into the new basis, kept x kept part only
+    // (nrgcore.hpp:409-476; the next site reads only this part, :199-203)
+    std::map<OpKey, std::vector<GemmContrib>> outs;
+    for (int ip = 0; ip < r->bath.nops; ++ip)
+      for (auto &kv : r->bath.op[ip]) {
+        const int bb = kv.first.first, bbp = kv.first.second;
+        const HostMat &fb = kv.second;
+        for (size_t ii = 0; ii < r->kept.size(); ++ii) {
+          const int k = int(r->kept[ii]);
+          if (k == 0) continue;
+          auto ia = st.sub_of.find({int(ii), bb});
+          auto ja = st.sub_of.find({int(ii), bbp});
+          if (ia == st.sub_of.end() || ja == st.sub_of.end()) continue;
+          const int si = ia->second.first, sj = ja->second.first;
+          const DevBlock &bi = sd.blocks[sd.sectors[si].dev];
+          const DevBlock &bj = sd.blocks[sd.sectors[sj].dev];
+          auto &lst = outs[OpKey{ip, si, sj}];
+          for (int il = 0; il < fb.rows; ++il)
+            for (int ilp = 0; ilp < fb.cols; ++ilp) {
+              const double v = fb.v[int64_t(il) * fb.cols + ilp];
+              if (v == 0.0) continue;
+              GemmContrib c{};
+              c.A = bi.U + int64_t(ia->second.second + il * k) * bi.ld;
+              c.lda = bi.ld;
+              c.B = bj.U + int64_t(ja->second.second + ilp * k) * bj.ld;
+              c.ldb = bj.ld;
+              c.K = k;
+              c.trans = 1;  // A stored K x M
+              c.alpha = v;
+              lst.push_back(c);
+            }
+        }
+      }
+    int64_t fsz = 0;
+    for (auto &kv : outs) {
+      const int si = std::get<1>(kv.first), sj = std::get<2>(kv.first);
+      fsz += r->kept_new[si] * r->kept_new[sj];
+    }
+    r->fcur_mem = dalloc(e, fsz * sizeof(double) + 8);
+    r->fcur.clear();
+    int64_t fo = 0;
+    for (auto &kv : outs) {
+      const int si = std::get<1>(kv.first), sj = std::get<2>(kv.first);
+      const int M = int(r->kept_new[si]), N = int(r->kept_new[sj]);
+      if (M == 0 || N == 0) continue;
+      FBlock fbk{static_cast<double *>(r->fcur_mem->ptr) + fo, M, N, N};
+      fo += int64_t(M) * N;
+      r->fcur[kv.first] = fbk;
+      GemmGroup g{};
+      g.C = fbk.p;
+      g.ldc = N;
+      g.M = M;
+      g.N = N;
+      g.accumulate = 0;
+      g.c0 = int(contribs.size());
+      contribs.insert(contribs.end(), kv.second.begin(), kv.second.end());
+      g.c1 = int(contribs.size());
+      const int gi = int(groups.size());
+      groups.push_back(g);
+      for (int tm = 0; tm < (M + GEMM_TILE - 1) / GEMM_TILE; ++tm)
+        for (int tn = 0; tn < (N + GEMM_TILE - 1) / GEMM_TILE; ++tn) tiles.push_back({gi, tm, tn, 0});
+    }
+  }
+  if (!tiles.empty()) {
+    Arena ag;
+    size_t o_t = ag.add(tiles), o_g = ag.add(groups), o_c = ag.add(contribs);
+    DevPtr gd;
+    char *gp = ag.push(e, gd);
+    hold.push_back(gd);
+    check_cuda(cudaEventRecord(e->ev[4], s), "event");
+    launch_gemm_f64(at<GemmTile>(gp, o_t), int(tiles.size()), at<GemmGroup>(gp, o_g),
+                    at<GemmContrib>(gp, o_c), s);
+    count_launch(e);
+    post_launch("rotate");
+    check_cuda(cudaEventRecord(e->ev[5], s), "event");
+  } else {
+    check_cuda(cudaEventRecord(e->ev[4], s), "event");
+    check_cuda(cudaEventRecord(e->ev[5], s), "event");
+  }
+  for (int i = 0; i < nruns; ++i) {
+    nrg_run *r = steps[i].run;
+    r->site = steps[i].site;
+    r->have_site = true;
+  }
+  // descriptor buffers are released stream-ordered when `hold` goes out of scope
+}
+
+static void update_state(nrg_run *r) {
+  if (!r->have_site) fail(NRG_E_STATE, "update_state without add_site");
+  SiteData &sd = *r->site;
+  r->cnt += 1;
+  r->all_eig = std::move(r->all_eig_pending);
+  r->kept = r->kept_new;
+  r->no_of_kept = r->tres.kept_total;
+  double shift = 0.0;
+  if (r->no_of_kept <= int64_t(r->nkeep)) {
+    r->cnt_min = r->cnt;
+  } else {
+    r->relgs.push_back(r->tres.emin);
+    shift = r->tres.emin;
+  }
+  r->prev_shift = shift;
+  r->prevE.assign(sd.sectors.size(), nullptr);
+  for (auto &db : sd.blocks) r->prevE[db.sector] = db.E;
+  r->prevE_host = sd.E_host;
+  for (auto &v : r->prevE_host)
+    for (auto &x : v) x -= shift;
+  r->prev_site = r->site;
+  r->pre_q = sd.cur_q;
+  r->fprev = r->fcur;
+  r->fprev_mem = r->fcur_mem;
+  r->mem_H.reset();
+  r->mem_sorted.reset();
+  r->have_site = false;
+}
+
+}  // namespace nrg
+
+namespace nrg {
+// entry points used by engine_api.cpp
+DevPtr engine_alloc(nrg_engine *e, size_t bytes) { return dalloc(e, bytes); }
+SiteModel engine_parse_site(const nrg_site_desc *d, bool need_chi) { return parse_site(d, need_chi); }
+void engine_upload_bath(nrg_engine *e, SiteModel &m) { upload_bath(e, m); }
+void engine_batch_add_site(nrg_run *const *runs, int nruns, const double *t, int nt,
+                           const double *rescale) {
+  batch_add_site(runs, nruns, t, nt, rescale);
+}
+void engine_update_state(nrg_run *r) { update_state(r); }
+void engine_count_launch(nrg_engine *e, int n) { count_launch(e, n); }
+}  // namespace nrg

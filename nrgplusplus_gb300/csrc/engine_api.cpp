@@ -1,0 +1,879 @@
+// C ABI of the engine (include/nrg_gpu.h): argument checking, the tracked
+// operators (update_system_operator), device-resident snapshots (NrgData),
+// the FDM spectral pass (fdmSpectrum) and thermodynamics (fdmThermodynamics).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+
+#include "engine_core.h"
+
+namespace nrg {
+extern thread_local std::string g_err;
+DevPtr engine_alloc(nrg_engine *e, size_t bytes);
+SiteModel engine_parse_site(const nrg_site_desc *d, bool need_chi);
+void engine_upload_bath(nrg_engine *e, SiteModel &m);
+void engine_batch_add_site(nrg_run *const *runs, int nruns, const double *t, int nt,
+                           const double *rescale);
+void engine_update_state(nrg_run *r);
+void engine_count_launch(nrg_engine *e, int n);
+
+constexpr int kFdmPts = 100000;                  // fdmSpectrum.hpp:351
+constexpr double kFdmMin = 1e-10, kFdmMax = 10;  // fdmSpectrum.hpp:352-353
+constexpr double kFdmEnergyErrorbar = 1e-5;      // fdmSpectrum.hpp:363
+
+static double fdm_delE() { return (kFdmPts - 1.0) / (std::log(kFdmMax / kFdmMin)); }
+
+template <class F> static int guard(F &&f) {
+  try {
+    f();
+    return NRG_OK;
+  } catch (const Error &e) {
+    g_err = e.msg;
+    return e.code;
+  } catch (const std::exception &e) {
+    g_err = e.what();
+    return NRG_E_ARG;
+  }
+}
+
+struct Staged {  // descriptor tables of one launch phase
+  std::vector<char> buf;
+  template <class T> size_t add(const std::vector<T> &v) {
+    size_t off = (buf.size() + 255) & ~size_t(255);
+    buf.resize(off + v.size() * sizeof(T) + 16);
+    if (!v.empty()) std::memcpy(buf.data() + off, v.data(), v.size() * sizeof(T));
+    return off;
+  }
+  char *push(nrg_engine *e, DevPtr &hold) {
+    hold = engine_alloc(e, buf.size());
+    check_cuda(cudaMemcpyAsync(hold->ptr, buf.data(), buf.size(), cudaMemcpyHostToDevice, e->stream),
+               "descriptor upload");
+    return static_cast<char *>(hold->ptr);
+  }
+};
+template <class T> static T *at(char *b, size_t o) { return reinterpret_cast<T *>(b + o); }
+
+// Grouped GEMM launch helper: one output per group.
+struct GemmBatch {
+  std::vector<GemmGroup> groups;
+  std::vector<GemmContrib> contribs;
+  std::vector<GemmTile> tiles;
+  void out(double *C, int ldc, int M, int N, bool accumulate,
+           const std::vector<GemmContrib> &cs) {
+    GemmGroup g{};
+    g.C = C;
+    g.ldc = ldc;
+    g.M = M;
+    g.N = N;
+    g.accumulate = accumulate ? 1 : 0;
+    g.c0 = int(contribs.size());
+    contribs.insert(contribs.end(), cs.begin(), cs.end());
+    g.c1 = int(contribs.size());
+    int gi = int(groups.size());
+    groups.push_back(g);
+    for (int tm = 0; tm < (M + GEMM_TILE - 1) / GEMM_TILE; ++tm)
+      for (int tn = 0; tn < (N + GEMM_TILE - 1) / GEMM_TILE; ++tn) tiles.push_back({gi, tm, tn, 0});
+  }
+  void run(nrg_engine *e) {
+    if (tiles.empty()) return;
+    Staged st;
+    size_t ot = st.add(tiles), og = st.add(groups), oc = st.add(contribs);
+    DevPtr hold;
+    char *d = st.push(e, hold);
+    launch_gemm_f64(at<GemmTile>(d, ot), int(tiles.size()), at<GemmGroup>(d, og),
+                    at<GemmContrib>(d, oc), e->stream);
+    engine_count_launch(e, 1);
+    check_cuda(cudaGetLastError(), "grouped gemm");
+  }
+};
+static GemmContrib gc(const double *A, int lda, const double *B, int ldb, int K, int trans,
+                      double alpha) {
+  GemmContrib c{};
+  c.A = A;
+  c.lda = lda;
+  c.B = B;
+  c.ldb = ldb;
+  c.K = K;
+  c.trans = trans;
+  c.alpha = alpha;
+  return c;
+}
+
+// --------------------------------------------------- update_system_operator
+// O_new(i,j) = sum over sub-block pairs with the same bath sector bb of
+// U_i[rows (ii,bb,il)]^T O_prev(ii,ii')[:k,:k'] U_j[rows (ii',bb,il)]
+// (sysOperator.hpp:36-133), as two grouped-GEMM passes through Y = O U_j.
+static void opset_update(nrg_opset *o) {
+  nrg_run *r = o->run;
+  if (!r->have_site) fail(NRG_E_STATE, "update_system_operator needs add_site first");
+  nrg_engine *e = r->eng;
+  SiteData &sd = *r->site;
+  const SiteModel &bath = r->bath;
+  const int nb = int(bath.q.size());
+  std::map<std::pair<int, int>, std::pair<int, int>> sub_of;
+  for (size_t s = 0; s < sd.sectors.size(); ++s)
+    for (auto &sb : sd.sectors[s].subs) sub_of[{sb.ii, sb.bb}] = {int(s), sb.off};
+  struct YTask {
+    int ip, si, sj, off_i, k;
+    double *Y;
+    int ldy;
+  };
+  std::vector<YTask> yt;
+  GemmBatch p1, p2;
+  int64_t ysz = 0;
+  std::vector<std::tuple<const FBlock *, int, int, int, int, int, int>> pend;  // block, ip, ii, iip, bb, il
+  std::map<OpKey, int> outs;
+  for (auto &kv : o->blocks) {
+    const int ip = std::get<0>(kv.first), ii = std::get<1>(kv.first), iip = std::get<2>(kv.first);
+    const int k = int(r->kept[ii]), kp = int(r->kept[iip]);
+    for (int bb = 0; bb < nb; ++bb) {
+      auto a = sub_of.find({ii, bb});
+      auto b = sub_of.find({iip, bb});
+      // the output block exists whenever both sub-blocks do (hasValue, :244-248)
+      const int si = a != sub_of.end() ? a->second.first : -1;
+      const int sj = b != sub_of.end() ? b->second.first : -1;
+      if (si < 0 || sj < 0) continue;
+      outs.emplace(OpKey{ip, si, sj}, 0);
+      if (k == 0 || kp == 0) continue;
+      for (int il = 0; il < int(bath.E[bb].size()); ++il) {
+        pend.emplace_back(&kv.second, ip, ii, iip, bb, il, 0);
+        ysz += int64_t(k) * sd.blocks[sd.sectors[sj].dev].n;
+      }
+    }
+  }
+  DevPtr ymem = engine_alloc(e, ysz * sizeof(double) + 8);
+  int64_t yo = 0;
+  std::map<OpKey, std::vector<GemmContrib>> p2c;
+  for (auto &t : pend) {
+    const FBlock *F = std::get<0>(t);
+    const int ip = std::get<1>(t), ii = std::get<2>(t), iip = std::get<3>(t), bb = std::get<4>(t),
+              il = std::get<5>(t);
+    const int k = int(r->kept[ii]), kp = int(r->kept[iip]);
+    auto a = sub_of.at({ii, bb});
+    auto b = sub_of.at({iip, bb});
+    const DevBlock &bi = sd.blocks[sd.sectors[a.first].dev];
+    const DevBlock &bj = sd.blocks[sd.sectors[b.first].dev];
+    double *Y = static_cast<double *>(ymem->ptr) + yo;
+    yo += int64_t(k) * bj.n;
+    // pass 1: Y (k x n_j) = O[:k,:k'] U_j[rows (iip,bb,il), :]
+    p1.out(Y, bj.n, k, bj.n, false,
+           {gc(F->p, F->ld, bj.U + int64_t(b.second + il * kp) * bj.ld, bj.ld, kp, 0, 1.0)});
+    // pass 2: O_new(i,j) += U_i[rows (ii,bb,il), :]^T Y
+    p2c[OpKey{ip, a.first, b.first}].push_back(
+        gc(bi.U + int64_t(a.second + il * k) * bi.ld, bi.ld, Y, bj.n, k, 1, 1.0));
+  }
+  int64_t osz = 0;
+  for (auto &kv : outs) {
+    const DevBlock &bi = sd.blocks[sd.sectors[std::get<1>(kv.first)].dev];
+    const DevBlock &bj = sd.blocks[sd.sectors[std::get<2>(kv.first)].dev];
+    osz += int64_t(bi.n) * bj.n;
+  }
+  DevPtr omem = engine_alloc(e, osz * sizeof(double) + 8);
+  std::map<OpKey, FBlock> nb_blocks;
+  int64_t oo = 0;
+  for (auto &kv : outs) {
+    const DevBlock &bi = sd.blocks[sd.sectors[std::get<1>(kv.first)].dev];
+    const DevBlock &bj = sd.blocks[sd.sectors[std::get<2>(kv.first)].dev];
+    FBlock fb{static_cast<double *>(omem->ptr) + oo, bi.n, bj.n, bj.n};
+    oo += int64_t(bi.n) * bj.n;
+    nb_blocks[kv.first] = fb;
+    auto it = p2c.find(kv.first);
+    p2.out(fb.p, fb.ld, bi.n, bj.n, false, it == p2c.end() ? std::vector<GemmContrib>{} : it->second);
+  }
+  p1.run(e);
+  p2.run(e);
+  o->blocks = std::move(nb_blocks);
+  o->mem = omem;
+  o->updated_this_site = true;
+}
+
+// ------------------------------------------------------------- FDM (T = 0)
+static void fdm_calc(nrg_fdm *f, double scale) {
+  nrg_run *r = f->run;
+  if (!r->loaded) fail(NRG_E_STATE, "calcSpectrum needs a loaded snapshot");
+  nrg_engine *e = r->eng;
+  cudaStream_t s = e->stream;
+  Snapshot &S = *r->loaded;
+  SiteData &sd = *S.site;
+  const int nsec = int(sd.cur_q.size());
+  // setCurrentIndex (fdmSpectrum.hpp:289-298)
+  if (!f->have_cur) {
+    f->cur_kept.assign(nsec, 0);
+    f->have_cur = true;
+  } else {
+    f->cur_kept = f->prev_kept;
+  }
+  f->prev_kept = sd.kept_prev;
+  if (int(f->cur_kept.size()) != nsec) fail(NRG_E_STATE, "snapshot order does not match the backward pass");
+  // setRhoZero (:165-199)
+  std::vector<std::vector<double>> boltz;
+  if (f->last) {  // setLocalPartitionFunction (:122-155)
+    double gs = 0;
+    for (auto &v : sd.E_host)
+      if (!v.empty()) gs = std::min(gs, *std::min_element(v.begin(), v.end()));
+    double z = 0;
+    for (auto &v : sd.E_host)
+      for (double x : v)
+        if (std::fabs(x - gs) < kFdmEnergyErrorbar) z += 1.0;
+    boltz.resize(nsec);
+    for (int i = 0; i < nsec; ++i) {
+      boltz[i].resize(sd.E_host[i].size());
+      for (size_t x = 0; x < sd.E_host[i].size(); ++x)
+        boltz[i][x] = std::fabs(sd.E_host[i][x] - gs) < kFdmEnergyErrorbar ? 1.0 / z : 0.0;
+    }
+    f->local_gs = gs;
+    f->local_z = z;
+  }
+  f->partitions.push_back(f->local_z);
+  int64_t rsz = 0;
+  for (auto &db : sd.blocks) rsz += int64_t(db.n) * db.n;
+  DevPtr rho = engine_alloc(e, rsz * sizeof(double) + 8);
+  check_cuda(cudaMemsetAsync(rho->ptr, 0, rsz * sizeof(double), s), "rho zero");
+  std::vector<double *> rp(sd.blocks.size());
+  int64_t ro = 0;
+  for (size_t b = 0; b < sd.blocks.size(); ++b) {
+    const DevBlock &db = sd.blocks[b];
+    rp[b] = static_cast<double *>(rho->ptr) + ro;
+    ro += int64_t(db.n) * db.n;
+    if (f->last)
+      check_cuda(cudaMemcpy2DAsync(rp[b], (db.n + 1) * sizeof(double), boltz[db.sector].data(),
+                                   sizeof(double), sizeof(double), db.n, cudaMemcpyHostToDevice, s),
+                 "rho diag");
+    if (f->have_reduced) {
+      const int kc = int(f->cur_kept[db.sector]);
+      if (kc > 0) {
+        if (f->reduced_k[db.sector] != kc) fail(NRG_E_STATE, "reduced density matrix size mismatch");
+        check_cuda(cudaMemcpy2DAsync(rp[b], db.n * sizeof(double), f->reduced[db.sector],
+                                     kc * sizeof(double), kc * sizeof(double), kc,
+                                     cudaMemcpyDeviceToDevice, s),
+                   "rho kept block");
+      }
+    }
+  }
+  // rhoDotOperators (:207-277): B rho_j and rho_i B, then binning
+  GemmBatch g;
+  std::vector<FdmPair> pairs;
+  int64_t psz = 0;
+  for (auto &kv : S.ops) {
+    const int i = std::get<1>(kv.first), j = std::get<2>(kv.first);
+    if (sd.sectors[i].dev < 0 || sd.sectors[j].dev < 0) continue;
+    psz += 2 * int64_t(sd.blocks[sd.sectors[i].dev].n) * sd.blocks[sd.sectors[j].dev].n;
+  }
+  DevPtr pm = engine_alloc(e, psz * sizeof(double) + 8);
+  int64_t po = 0, chunk = 0;
+  for (auto &kv : S.ops) {
+    const int ip = std::get<0>(kv.first), i = std::get<1>(kv.first), j = std::get<2>(kv.first);
+    if (sd.sectors[i].dev < 0 || sd.sectors[j].dev < 0) continue;
+    const int bi = sd.sectors[i].dev, bj = sd.sectors[j].dev;
+    const DevBlock &Bi = sd.blocks[bi], &Bj = sd.blocks[bj];
+    const FBlock &B = kv.second;
+    double *rhoA = static_cast<double *>(pm->ptr) + po;
+    po += int64_t(Bi.n) * Bj.n;
+    double *ARho = static_cast<double *>(pm->ptr) + po;
+    po += int64_t(Bi.n) * Bj.n;
+    g.out(rhoA, Bj.n, Bi.n, Bj.n, false, {gc(B.p, B.ld, rp[bj], Bj.n, Bj.n, 0, 1.0)});
+    g.out(ARho, Bj.n, Bi.n, Bj.n, false, {gc(rp[bi], Bi.n, B.p, B.ld, Bi.n, 0, 1.0)});
+    FdmPair fp{};
+    fp.rhoA = rhoA;
+    fp.ARho = ARho;
+    fp.B = B.p;
+    fp.Ei = Bi.E;
+    fp.Ej = Bj.E;
+    fp.ni = Bi.n;
+    fp.nj = Bj.n;
+    fp.kci = int(f->cur_kept[i]);
+    fp.kcj = int(f->cur_kept[j]);
+    fp.op = ip;
+    fp.chunk0 = chunk;
+    chunk += (int64_t(Bi.n) * Bj.n + 255) / 256;
+    pairs.push_back(fp);
+    if (B.ld != Bj.n) fail(NRG_E_STATE, "operator block layout");
+  }
+  g.run(e);
+  if (!pairs.empty()) {
+    Staged st;
+    size_t op = st.add(pairs);
+    DevPtr hold;
+    char *d = st.push(e, hold);
+    double *hist = static_cast<double *>(f->hist->ptr);
+    launch_fdm_bin(at<FdmPair>(d, op), int(pairs.size()), chunk, scale, fdm_delE(), hist,
+                   hist + int64_t(f->nops) * kFdmPts, kFdmPts, s);
+    engine_count_launch(e, 1);
+    check_cuda(cudaGetLastError(), "fdm binning");
+  }
+  // setReduceDensityMatrix (:71-114): rho <- U rho U^T, then the partial trace
+  DevPtr xm = engine_alloc(e, rsz * sizeof(double) + 8), rm = engine_alloc(e, rsz * sizeof(double) + 8);
+  GemmBatch g1, g2;
+  std::vector<double *> rot(sd.blocks.size());
+  int64_t xo = 0;
+  for (size_t b = 0; b < sd.blocks.size(); ++b) {
+    const DevBlock &db = sd.blocks[b];
+    double *X = static_cast<double *>(xm->ptr) + xo;
+    rot[b] = static_cast<double *>(rm->ptr) + xo;
+    xo += int64_t(db.n) * db.n;
+    g1.out(X, db.n, db.n, db.n, false, {gc(rp[b], db.n, db.U, db.ld, db.n, 2, 1.0)});  // rho U^T
+    g2.out(rot[b], db.n, db.n, db.n, false, {gc(db.U, db.ld, X, db.n, db.n, 0, 1.0)});  // U X
+  }
+  g1.run(e);
+  g2.run(e);
+  const int npre = int(sd.pre_q.size());
+  std::vector<DevPtr> red_mem(npre);
+  std::vector<double *> red(npre, nullptr);
+  std::vector<int64_t> red_k(npre, 0);
+  std::vector<std::vector<TraceIn>> ins(npre);
+  for (int i = 0; i < nsec; ++i) {
+    const Sector &Sc = sd.sectors[i];
+    if (Sc.dev < 0) continue;
+    for (auto &sb : Sc.subs) ins[sb.ii].push_back({rot[Sc.dev], sd.blocks[Sc.dev].n, sb.off, sb.d, 0});
+  }
+  std::vector<TraceTask> tasks;
+  std::vector<TraceIn> flat;
+  int maxk = 0;
+  for (int ii = 0; ii < npre; ++ii) {
+    const int k = int(sd.kept_prev[ii]);
+    red_k[ii] = k;
+    if (k == 0) continue;
+    red_mem[ii] = engine_alloc(e, int64_t(k) * k * sizeof(double));
+    red[ii] = static_cast<double *>(red_mem[ii]->ptr);
+    TraceTask t{};
+    t.out = red[ii];
+    t.k = k;
+    t.in0 = int(flat.size());
+    flat.insert(flat.end(), ins[ii].begin(), ins[ii].end());
+    t.in1 = int(flat.size());
+    tasks.push_back(t);
+    maxk = std::max(maxk, k);
+  }
+  if (!tasks.empty()) {
+    Staged st;
+    size_t ot = st.add(tasks), oi = st.add(flat);
+    DevPtr hold;
+    char *d = st.push(e, hold);
+    launch_partial_trace(at<TraceTask>(d, ot), int(tasks.size()), at<TraceIn>(d, oi), maxk, s);
+    engine_count_launch(e, 1);
+    check_cuda(cudaGetLastError(), "partial trace");
+  }
+  f->reduced_mem = std::move(red_mem);
+  f->reduced = std::move(red);
+  f->reduced_k = std::move(red_k);
+  f->have_reduced = true;
+  f->last = false;
+  check_cuda(cudaStreamSynchronize(s), "fdm step");
+}
+
+}  // namespace nrg
+
+using namespace nrg;
+
+extern "C" {
+
+const char *nrg_last_error(void) { return g_err.c_str(); }
+
+int nrg_engine_create(const nrg_engine_opts *opts, nrg_engine **out) {
+  return guard([&] {
+    if (!out) fail(NRG_E_ARG, "null out");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+      cudaGetLastError();
+      fail(NRG_E_NOCUDA, "no CUDA device available: the NRG engine has no CPU fallback");
+    }
+    auto *e = new nrg_engine();
+    if (opts) {
+      e->device = opts->device;
+      e->precision = opts->precision;
+      e->budget = opts->hbm_budget_bytes;
+      e->verbose = opts->verbose;
+    }
+    if (e->precision != NRG_PREC_FP64 && e->precision != NRG_PREC_MIXED) {
+      delete e;
+      fail(NRG_E_ARG, "unknown precision mode");
+    }
+    check_cuda(cudaSetDevice(e->device), "cudaSetDevice");
+    check_cuda(cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking), "stream");
+    for (auto &ev : e->ev) check_cuda(cudaEventCreate(&ev), "event");
+    e->eig_smem_f64 = eig_smem_limit_f64();
+    e->eig_smem_f32 = eig_smem_limit_f32();
+    *out = e;
+  });
+}
+
+int nrg_engine_destroy(nrg_engine *e) {
+  return guard([&] {
+    if (!e) return;
+    cudaStreamSynchronize(e->stream);
+    for (auto &ev : e->ev) cudaEventDestroy(ev);
+    cudaStreamDestroy(e->stream);
+    delete e;
+  });
+}
+
+int nrg_engine_phase_times(nrg_engine *e, double *out, int cap, int *n) {
+  return guard([&] {
+    if (!e || !out) fail(NRG_E_ARG, "null argument");
+    check_cuda(cudaEventSynchronize(e->ev[5]), "event sync");
+    float ms[5] = {0, 0, 0, 0, 0};
+    cudaEventElapsedTime(&ms[0], e->ev[0], e->ev[1]);
+    cudaEventElapsedTime(&ms[1], e->ev[1], e->ev[2]);
+    cudaEventElapsedTime(&ms[2], e->ev[2], e->ev[3]);
+    cudaEventElapsedTime(&ms[3], e->ev[4], e->ev[5]);
+    int m = std::min(cap, 4);
+    for (int i = 0; i < m; ++i) out[i] = ms[i];
+    if (n) *n = m;
+  });
+}
+
+int nrg_engine_launch_count(nrg_engine *e, uint64_t *out) {
+  return guard([&] {
+    if (!e || !out) fail(NRG_E_ARG, "null argument");
+    *out = e->launches;
+  });
+}
+
+int nrg_engine_sync(nrg_engine *e) {
+  return guard([&] {
+    if (!e) fail(NRG_E_ARG, "null engine");
+    check_cuda(cudaStreamSynchronize(e->stream), "sync");
+  });
+}
+
+int nrg_run_create(nrg_engine *e, const nrg_site_desc *imp, const nrg_site_desc *bath, uint64_t nkeep,
+                   nrg_run **out) {
+  return guard([&] {
+    if (!e || !out) fail(NRG_E_ARG, "null argument");
+    auto r = std::make_unique<nrg_run>();
+    r->eng = e;
+    r->imp = engine_parse_site(imp, false);
+    r->bath = engine_parse_site(bath, true);
+    if (r->imp.q[0].size() != r->bath.q[0].size())  // nrgcore.hpp:119-122
+      fail(NRG_E_ARG, "Number of quantum number is different on model and impurity!");
+    if (r->imp.nops != r->bath.nops)  // nrgcore.hpp:124-133
+      fail(NRG_E_ARG, "f_dag_operator.size is different on model and impurity!");
+    engine_upload_bath(e, r->bath);
+    r->nkeep = nkeep;
+    r->no_of_kept = int64_t(nkeep);
+    *out = r.release();
+  });
+}
+
+int nrg_run_destroy(nrg_run *r) {
+  return guard([&] {
+    if (!r) return;
+    nrg_engine *e = r->eng;
+    delete r;
+    cudaStreamSynchronize(e->stream);
+  });
+}
+
+int nrg_run_set_parameters(nrg_run *r, uint64_t nkeep) {
+  return guard([&] {
+    if (!r) fail(NRG_E_ARG, "null run");
+    r->nkeep = nkeep;
+    r->no_of_kept = int64_t(nkeep);
+    r->cnt = 0;
+    r->cnt_min = 0;
+    r->have_site = false;
+  });
+}
+
+int nrg_run_set_bath(nrg_run *r, const nrg_site_desc *bath) {
+  return guard([&] {
+    if (!r) fail(NRG_E_ARG, "null run");
+    r->bath_next = engine_parse_site(bath, true);
+    if (r->bath_next.nops != r->imp.nops) fail(NRG_E_ARG, "bath operator count changed");
+    r->bath_pending = true;
+  });
+}
+
+int nrg_run_add_site(nrg_run *r, const double *t, int nt, double rescale) {
+  return guard([&] {
+    if (!r || (!t && nt > 0)) fail(NRG_E_ARG, "null argument");
+    nrg_run *rs[1] = {r};
+    engine_batch_add_site(rs, 1, t, nt, &rescale);
+  });
+}
+
+int nrg_run_update_state(nrg_run *r) {
+  return guard([&] {
+    if (!r) fail(NRG_E_ARG, "null run");
+    engine_update_state(r);
+  });
+}
+
+int nrg_batch_add_site(nrg_run *const *runs, int nruns, const double *t, int nt, const double *rescale) {
+  return guard([&] {
+    if (!runs || nruns < 0 || !rescale || (!t && nt > 0)) fail(NRG_E_ARG, "null argument");
+    engine_batch_add_site(runs, nruns, t, nt, rescale);
+  });
+}
+
+int nrg_batch_update_state(nrg_run *const *runs, int nruns) {
+  return guard([&] {
+    if (!runs || nruns < 0) fail(NRG_E_ARG, "null argument");
+    for (int i = 0; i < nruns; ++i) engine_update_state(runs[i]);
+  });
+}
+
+int nrg_run_check_discarded(nrg_run *r, int *out) {
+  return guard([&] {
+    if (!r || !out) fail(NRG_E_ARG, "null argument");
+    *out = r->no_of_kept >= int64_t(r->nkeep) ? 1 : 0;  // nrgcore.hpp:384-386
+  });
+}
+
+int nrg_run_get_info(nrg_run *r, nrg_run_info *info) {
+  return guard([&] {
+    if (!r || !info) fail(NRG_E_ARG, "null argument");
+    std::memset(info, 0, sizeof(*info));
+    info->iteration = r->cnt;
+    info->iteration_min = r->cnt_min;
+    info->n_pre_sectors = int64_t(r->pre_q.size());
+    info->n_cur_sectors = r->have_site && r->site ? int64_t(r->site->cur_q.size()) : 0;
+    info->n_all = int64_t(r->all_eig.size());
+    info->n_kept = r->no_of_kept;
+    info->n_relgs = int64_t(r->relgs.size());
+    info->nq = r->imp.nq;
+    if (r->site) {
+      info->n_device_blocks = int64_t(r->site->blocks.size());
+      for (auto &b : r->site->blocks) info->max_block = std::max<int64_t>(info->max_block, b.n);
+    }
+    info->n_snapshots = int64_t(r->snaps.size());
+    info->device_bytes = int64_t(r->eng->used);
+  });
+}
+
+int nrg_run_get_all_eigenvalues(nrg_run *r, double *out, uint64_t cap) {
+  return guard([&] {
+    if (!r || (!out && cap)) fail(NRG_E_ARG, "null argument");
+    if (cap < r->all_eig.size()) fail(NRG_E_ARG, "buffer too small");
+    std::copy(r->all_eig.begin(), r->all_eig.end(), out);
+  });
+}
+
+int nrg_run_get_relgs(nrg_run *r, double *out, uint64_t cap) {
+  return guard([&] {
+    if (!r || (!out && cap)) fail(NRG_E_ARG, "null argument");
+    if (cap < r->relgs.size()) fail(NRG_E_ARG, "buffer too small");
+    std::copy(r->relgs.begin(), r->relgs.end(), out);
+  });
+}
+
+int nrg_run_get_sectors(nrg_run *r, int which, int *qnum, uint64_t cap) {
+  return guard([&] {
+    if (!r || !qnum) fail(NRG_E_ARG, "null argument");
+    const auto *q = which == 0 ? (r->have_site ? &r->site->cur_q : nullptr) : &r->pre_q;
+    if (!q) return;
+    if (cap < q->size()) fail(NRG_E_ARG, "buffer too small");
+    int64_t o = 0;
+    for (auto &v : *q)
+      for (int x : v) qnum[o++] = x;
+  });
+}
+
+int nrg_run_get_eigenvalues_q(nrg_run *r, uint64_t *dims, double *values, uint64_t cap) {
+  return guard([&] {
+    if (!r || !dims) fail(NRG_E_ARG, "null argument");
+    // between add_site and update_state: the new, unshifted eigenvalues;
+    // afterwards the shifted ones (nrgcore.hpp:317-326)
+    const auto &E = r->have_site ? r->site->E_host : r->prevE_host;
+    uint64_t o = 0;
+    for (size_t s = 0; s < E.size(); ++s) {
+      dims[s] = E[s].size();
+      if (values) {
+        if (o + E[s].size() > cap) fail(NRG_E_ARG, "buffer too small");
+        std::copy(E[s].begin(), E[s].end(), values + o);
+      }
+      o += E[s].size();
+    }
+  });
+}
+
+int nrg_run_get_kept(nrg_run *r, uint64_t *kept, uint64_t cap) {
+  return guard([&] {
+    if (!r || !kept) fail(NRG_E_ARG, "null argument");
+    if (cap < r->kept.size()) fail(NRG_E_ARG, "buffer too small");
+    for (size_t i = 0; i < r->kept.size(); ++i) kept[i] = uint64_t(r->kept[i]);
+  });
+}
+
+int nrg_run_get_coupled(nrg_run *r, uint64_t *counts, uint64_t *entries, uint64_t cap) {
+  return guard([&] {
+    if (!r || !counts) fail(NRG_E_ARG, "null argument");
+    if (!r->site) fail(NRG_E_STATE, "no site yet");
+    uint64_t o = 0;
+    for (size_t s = 0; s < r->site->coupled.size(); ++s) {
+      counts[s] = r->site->coupled[s].size();
+      for (uint64_t x : r->site->coupled[s]) {
+        if (entries) {
+          if (o >= cap) fail(NRG_E_ARG, "buffer too small");
+          entries[o] = x;
+        }
+        ++o;
+      }
+    }
+  });
+}
+
+int nrg_run_get_eigenvectors(nrg_run *r, int64_t sector, double *out, uint64_t cap) {
+  return guard([&] {
+    if (!r || !out) fail(NRG_E_ARG, "null argument");
+    if (!r->site || sector < 0 || sector >= int64_t(r->site->sectors.size()))
+      fail(NRG_E_ARG, "sector out of range");
+    const Sector &S = r->site->sectors[sector];
+    if (S.dev < 0) return;
+    const DevBlock &b = r->site->blocks[S.dev];
+    if (cap < uint64_t(b.n) * b.n) fail(NRG_E_ARG, "buffer too small");
+    check_cuda(cudaMemcpy2DAsync(out, b.n * sizeof(double), b.U, b.ld * sizeof(double),
+                                 b.n * sizeof(double), b.n, cudaMemcpyDeviceToHost, r->eng->stream),
+               "eigenvectors D2H");
+    check_cuda(cudaStreamSynchronize(r->eng->stream), "eigenvectors D2H");
+  });
+}
+
+static void copy_block(nrg_engine *e, const FBlock &b, double *out, uint64_t cap) {
+  if (cap < uint64_t(b.rows) * b.cols) fail(NRG_E_ARG, "buffer too small");
+  if (b.rows && b.cols)
+    check_cuda(cudaMemcpy2DAsync(out, b.cols * sizeof(double), b.p, b.ld * sizeof(double),
+                                 b.cols * sizeof(double), b.rows, cudaMemcpyDeviceToHost, e->stream),
+               "block D2H");
+  check_cuda(cudaStreamSynchronize(e->stream), "block D2H");
+}
+
+int nrg_run_get_fdag_block(nrg_run *r, int ip, int64_t i, int64_t j, double *out, uint64_t cap,
+                           int64_t *rows, int64_t *cols) {
+  return guard([&] {
+    if (!r || !rows || !cols) fail(NRG_E_ARG, "null argument");
+    const auto &m = r->have_site ? r->fcur : r->fprev;
+    auto it = m.find(OpKey{ip, int(i), int(j)});
+    *rows = *cols = 0;
+    if (it == m.end()) return;
+    *rows = it->second.rows;
+    *cols = it->second.cols;
+    if (out) copy_block(r->eng, it->second, out, cap);
+  });
+}
+
+int nrg_opset_create(nrg_run *r, const nrg_op_desc *ops, nrg_opset **out) {
+  return guard([&] {
+    if (!r || !ops || !out) fail(NRG_E_ARG, "null argument");
+    auto o = std::make_unique<nrg_opset>();
+    o->run = r;
+    o->nops = ops->nops;
+    int64_t tot = 0;
+    for (int b = 0; b < ops->nblk; ++b) tot += int64_t(ops->blk_rows[b]) * ops->blk_cols[b];
+    o->mem = engine_alloc(r->eng, tot * sizeof(double) + 8);
+    check_cuda(cudaMemcpyAsync(o->mem->ptr, ops->blk_data, tot * sizeof(double), cudaMemcpyHostToDevice,
+                               r->eng->stream),
+               "opset upload");
+    int64_t off = 0;
+    for (int b = 0; b < ops->nblk; ++b) {
+      FBlock fb{static_cast<double *>(o->mem->ptr) + off, ops->blk_rows[b], ops->blk_cols[b],
+                ops->blk_cols[b]};
+      off += int64_t(fb.rows) * fb.cols;
+      OpKey key{ops->blk_op[b], ops->blk_row[b], ops->blk_col[b]};
+      if (o->blocks.count(key)) fail(NRG_E_ARG, "Found operator already");
+      o->blocks[key] = fb;
+    }
+    check_cuda(cudaStreamSynchronize(r->eng->stream), "opset upload");
+    *out = o.release();
+  });
+}
+
+int nrg_opset_destroy(nrg_opset *o) {
+  return guard([&] { delete o; });
+}
+
+int nrg_opset_update(nrg_opset *o) {
+  return guard([&] {
+    if (!o) fail(NRG_E_ARG, "null opset");
+    opset_update(o);
+  });
+}
+
+int nrg_opset_get_block(nrg_opset *o, int ip, int64_t i, int64_t j, double *out, uint64_t cap,
+                        int64_t *rows, int64_t *cols) {
+  return guard([&] {
+    if (!o || !rows || !cols) fail(NRG_E_ARG, "null argument");
+    auto it = o->blocks.find(OpKey{ip, int(i), int(j)});
+    *rows = *cols = 0;
+    if (it == o->blocks.end()) return;
+    *rows = it->second.rows;
+    *cols = it->second.cols;
+    if (out) copy_block(o->run->eng, it->second, out, cap);
+  });
+}
+
+int nrg_run_snapshot(nrg_run *r, nrg_opset *ops) {
+  return guard([&] {
+    if (!r) fail(NRG_E_ARG, "null run");
+    if (!r->have_site) fail(NRG_E_STATE, "snapshot needs add_site first");
+    auto s = std::make_shared<Snapshot>();
+    s->site = r->site;
+    if (ops) {
+      s->ops = ops->blocks;
+      s->nops = ops->nops;
+      s->ops_mem = ops->mem;
+    }
+    r->snaps[r->cnt] = s;
+  });
+}
+
+int nrg_run_load_snapshot(nrg_run *r, int64_t iteration) {
+  return guard([&] {
+    if (!r) fail(NRG_E_ARG, "null run");
+    auto it = r->snaps.find(iteration);
+    if (it == r->snaps.end()) fail(NRG_E_ARG, "no snapshot for iteration " + std::to_string(iteration));
+    r->loaded = it->second;
+    r->cnt = iteration;  // loadCurrentData sets nrg_iterations_cnt (nrgData.hpp:273)
+  });
+}
+
+int nrg_fdm_create(nrg_run *r, int nops, nrg_fdm **out) {
+  return guard([&] {
+    if (!r || !out || nops <= 0) fail(NRG_E_ARG, "bad argument");
+    auto f = std::make_unique<nrg_fdm>();
+    f->run = r;
+    f->nops = nops;
+    f->hist = engine_alloc(r->eng, 2 * int64_t(nops) * kFdmPts * sizeof(double));
+    check_cuda(cudaMemsetAsync(f->hist->ptr, 0, 2 * int64_t(nops) * kFdmPts * sizeof(double), r->eng->stream),
+               "fdm hist");
+    *out = f.release();
+  });
+}
+
+int nrg_fdm_destroy(nrg_fdm *f) {
+  return guard([&] { delete f; });
+}
+
+int nrg_fdm_calc(nrg_fdm *f, double scale) {
+  return guard([&] {
+    if (!f) fail(NRG_E_ARG, "null fdm");
+    fdm_calc(f, scale);
+  });
+}
+
+int nrg_fdm_get(nrg_fdm *f, double *energy_points, double *positive, double *negative, uint64_t npts) {
+  return guard([&] {
+    if (!f) fail(NRG_E_ARG, "null fdm");
+    if (npts != uint64_t(kFdmPts)) fail(NRG_E_ARG, "npts must be 100000");
+    const double de = fdm_delE();
+    if (energy_points)
+      for (int i = 0; i < kFdmPts; ++i) energy_points[i] = kFdmMin * std::exp(i * 1. / de);
+    nrg_engine *e = f->run->eng;
+    const double *h = static_cast<const double *>(f->hist->ptr);
+    if (positive)
+      check_cuda(cudaMemcpyAsync(positive, h, int64_t(f->nops) * kFdmPts * sizeof(double),
+                                 cudaMemcpyDeviceToHost, e->stream), "fdm D2H");
+    if (negative)
+      check_cuda(cudaMemcpyAsync(negative, h + int64_t(f->nops) * kFdmPts,
+                                 int64_t(f->nops) * kFdmPts * sizeof(double), cudaMemcpyDeviceToHost,
+                                 e->stream), "fdm D2H");
+    check_cuda(cudaStreamSynchronize(e->stream), "fdm D2H");
+  });
+}
+
+int nrg_broaden(nrg_engine *e, const double *energies, const double *weights, uint64_t nbins,
+                const double *omegas, uint64_t nomega, double b, double *out) {
+  return guard([&] {
+    if (!e || !energies || !weights || !omegas || !out) fail(NRG_E_ARG, "null argument");
+    std::vector<double> ee, ww;
+    for (uint64_t i = 0; i < nbins; ++i)
+      if (weights[i] != 0.0) {
+        ee.push_back(energies[i]);
+        ww.push_back(weights[i]);
+      }
+    std::vector<double> om(omegas, omegas + nomega);
+    Staged st;
+    size_t oe = st.add(ee), ow = st.add(ww), oo = st.add(om);
+    std::vector<double> res(nomega, 0.0);
+    size_t orr = st.add(res);
+    DevPtr hold;
+    char *d = st.push(e, hold);
+    launch_broaden(at<double>(d, oe), at<double>(d, ow), int64_t(ee.size()), at<double>(d, oo),
+                   int64_t(nomega), b, at<double>(d, orr), e->stream);
+    engine_count_launch(e, 1);
+    check_cuda(cudaGetLastError(), "broaden");
+    check_cuda(cudaMemcpyAsync(out, d + orr, nomega * sizeof(double), cudaMemcpyDeviceToHost, e->stream),
+               "broaden D2H");
+    check_cuda(cudaStreamSynchronize(e->stream), "broaden");
+  });
+}
+
+int nrg_thermo_create(nrg_run *r, const double *temps, int nt, nrg_thermo **out) {
+  return guard([&] {
+    if (!r || !out || (!temps && nt > 0)) fail(NRG_E_ARG, "null argument");
+    auto t = std::make_unique<nrg_thermo>();
+    t->run = r;
+    t->nmax = r->cnt;  // nrgMaxIterations (fdmThermodynamics.hpp:30)
+    for (auto &v : r->bath.E) t->bathdim += double(v.size());
+    t->temps.assign(temps, temps + nt);
+    *out = t.release();
+  });
+}
+
+int nrg_thermo_destroy(nrg_thermo *t) {
+  return guard([&] { delete t; });
+}
+
+int nrg_thermo_calc(nrg_thermo *t, double scale) {
+  return guard([&] {
+    if (!t) fail(NRG_E_ARG, "null thermo");
+    nrg_run *r = t->run;
+    if (!r->loaded) fail(NRG_E_STATE, "calcThermodynamics needs a loaded snapshot");
+    SiteData &sd = *r->loaded->site;
+    const int nsec = int(sd.cur_q.size());
+    if (!t->have_cur) {
+      t->cur_kept.assign(nsec, 0);
+      t->have_cur = true;
+    } else {
+      t->cur_kept = t->prev_kept;
+    }
+    t->prev_kept = sd.kept_prev;
+    std::vector<double> disc, all;
+    for (int i = 0; i < nsec; ++i)  // discarded states only (:47-52)
+      for (size_t j = size_t(t->cur_kept[i]); j < sd.E_host[i].size(); ++j)
+        disc.push_back(sd.E_host[i][j] * scale);
+    for (int i = 0; i < nsec; ++i)
+      for (double x : sd.E_host[i]) all.push_back(x * scale);
+    t->disc.push_back(std::move(disc));
+    t->allv.push_back(std::move(all));
+  });
+}
+
+int nrg_thermo_final(nrg_thermo *t, double *entropy, double *cv) {
+  return guard([&] {
+    if (!t || !entropy || !cv) fail(NRG_E_ARG, "null argument");
+    nrg_engine *e = t->run->eng;
+    const int nsh = int(t->allv.size());
+    if (nsh == 0) fail(NRG_E_STATE, "no shells");
+    std::vector<double> gs(nsh), flat;
+    std::vector<int64_t> off(nsh + 1, 0);
+    for (int it = 0; it < nsh; ++it) {  // :114-131
+      const double m = *std::min_element(t->allv[it].begin(), t->allv[it].end());
+      gs[it] = m;
+      off[it] = int64_t(flat.size());
+      for (double x : t->disc[it]) flat.push_back(x - m);
+    }
+    off[nsh] = int64_t(flat.size());
+    for (int it = 0; it + 1 < nsh; ++it) gs[it] += gs[it + 1];  // one-step correction :133-135
+    const double g0 = gs[0];
+    for (auto &x : gs) x -= g0;
+    const int nt = int(t->temps.size());
+    Staged st;
+    size_t of = st.add(flat), oo = st.add(off), og = st.add(gs), ot = st.add(t->temps);
+    std::vector<double> scratch(size_t(2) * nsh * nt + 2 * nt, 0.0);
+    size_t os = st.add(scratch);
+    DevPtr hold;
+    char *d = st.push(e, hold);
+    double *ent = at<double>(d, os) + size_t(2) * nsh * nt;
+    launch_thermo(at<double>(d, of), at<int64_t>(d, oo), at<double>(d, og), nsh, at<double>(d, ot), nt,
+                  t->bathdim, at<double>(d, os), ent, ent + nt, e->stream);
+    engine_count_launch(e, 1);
+    check_cuda(cudaGetLastError(), "thermo");
+    check_cuda(cudaMemcpyAsync(entropy, ent, nt * sizeof(double), cudaMemcpyDeviceToHost, e->stream), "D2H");
+    check_cuda(cudaMemcpyAsync(cv, ent + nt, nt * sizeof(double), cudaMemcpyDeviceToHost, e->stream), "D2H");
+    check_cuda(cudaStreamSynchronize(e->stream), "thermo");
+  });
+}
+
+}  // extern "C"

@@ -1,0 +1,181 @@
+// Host-side engine state (C++).  Internal to libnrggpu; the public surface is
+// the C ABI in include/nrg_gpu.h.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <map>
+#include <memory>
+#include <string>
+#include <tuple>
+#include <unordered_map>
+#include <vector>
+
+#include "nrg_gpu.h"
+#include "nrg_internal.h"
+
+namespace nrg {
+
+struct Error {
+  int code;
+  std::string msg;
+};
+[[noreturn]] void fail(int code, const std::string &msg);
+void check_cuda(cudaError_t e, const char *what);
+
+// Device allocation owned by shared_ptr so snapshots and operator sets can
+// keep a site's buffers alive after the run moves on.
+struct DevMem {
+  void *ptr = nullptr;
+  size_t bytes = 0;
+  nrg_engine *eng = nullptr;
+  ~DevMem();
+};
+using DevPtr = std::shared_ptr<DevMem>;
+
+struct HostMat {
+  int rows = 0, cols = 0;
+  std::vector<double> v;
+};
+
+struct SiteModel {
+  int nq = 0;
+  std::vector<std::vector<int>> q;
+  std::vector<std::vector<double>> E;
+  std::vector<double> chi;
+  int nops = 0;
+  std::vector<std::map<std::pair<int, int>, HostMat>> op;  // per operator: (row, col) -> block
+  // device copies (bath only): energies per sector and f-dagger blocks
+  DevPtr dev;
+  std::vector<int64_t> e_off;                                      // energies offset per sector
+  std::vector<std::map<std::pair<int, int>, int64_t>> op_off;      // block data offsets
+};
+
+struct Sub {          // sub-block (ii, bb) of a sector
+  int ii, bb, off, k, d;
+};
+
+struct Sector {       // one sector of the current basis
+  std::vector<Sub> subs;  // only sub-blocks with k*d > 0
+  int n = 0;
+  int dev = -1;           // device block index, -1 if empty
+};
+
+struct DevBlock {     // non-empty sector on the device
+  int sector = 0;
+  int n = 0, ld = 0;
+  double *H = nullptr, *U = nullptr, *E = nullptr;
+};
+
+struct FBlock {       // one operator block on the device
+  double *p = nullptr;
+  int rows = 0, cols = 0, ld = 0;
+};
+using OpKey = std::tuple<int, int, int>;  // (op, row sector, col sector)
+
+// A site's device data that later passes need: the eigenvectors U, the
+// eigenvalues E (unshifted) and the sector layout.
+struct SiteData {
+  int64_t iteration = 0;
+  std::vector<std::vector<int>> cur_q, pre_q;
+  std::vector<std::vector<uint64_t>> coupled;
+  std::vector<Sector> sectors;
+  std::vector<DevBlock> blocks;
+  std::vector<int64_t> kept_prev;  // eigenvaluesQ_kept_indices sizes (pre sectors)
+  DevPtr mem_U, mem_E;
+  std::vector<std::vector<double>> E_host;  // eigenvalues per sector (unshifted)
+};
+
+struct Snapshot {
+  std::shared_ptr<SiteData> site;
+  std::map<OpKey, FBlock> ops;
+  int nops = 0;
+  DevPtr ops_mem;
+};
+
+}  // namespace nrg
+
+struct nrg_engine {
+  int device = 0;
+  int precision = NRG_PREC_FP64;
+  uint64_t budget = 0;
+  uint64_t used = 0;
+  int verbose = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev[8] = {};
+  double phase_ms[5] = {0, 0, 0, 0, 0};
+  uint64_t launches = 0;
+  int eig_smem_f64 = 0, eig_smem_f32 = 0;
+  int *d_status = nullptr;
+  size_t status_cap = 0;
+};
+
+struct nrg_run {
+  nrg_engine *eng = nullptr;
+  nrg::SiteModel imp, bath;
+  bool bath_pending = false;
+  nrg::SiteModel bath_next;
+  uint64_t nkeep = 1024;
+  // API-visible state, mirroring nrgcore's public members
+  int64_t cnt = 0, cnt_min = 0;
+  std::vector<std::vector<int>> pre_q;
+  std::vector<int64_t> kept;              // per pre sector
+  int64_t no_of_kept = 0;
+  std::vector<double> relgs;
+  std::vector<double> all_eig;
+  // previous basis on the device
+  std::vector<const double *> prevE;      // per pre sector (null when empty)
+  double prev_shift = 0.0;
+  std::vector<std::vector<double>> prevE_host;  // eigenvaluesQ of the previous site (shifted view)
+  std::shared_ptr<nrg::SiteData> prev_site;     // keeps prevE alive
+  std::map<nrg::OpKey, nrg::FBlock> fprev;      // kept x kept f-dagger blocks
+  nrg::DevPtr fprev_mem;
+  // current site (after add_site)
+  bool have_site = false;
+  std::shared_ptr<nrg::SiteData> site;
+  nrg::DevPtr mem_H;
+  std::map<nrg::OpKey, nrg::FBlock> fcur;
+  nrg::DevPtr fcur_mem;
+  // pending truncation of the current site
+  std::vector<int64_t> kept_new;          // per current sector
+  std::vector<double> all_eig_pending;    // sorted eigenvalues of the current site
+  nrg::TruncResult tres{};
+  nrg::DevPtr mem_sorted;
+  // snapshots for the backward passes
+  std::map<int64_t, std::shared_ptr<nrg::Snapshot>> snaps;
+  std::shared_ptr<nrg::Snapshot> loaded;
+  int64_t device_bytes = 0;
+};
+
+struct nrg_opset {
+  nrg_run *run = nullptr;
+  int nops = 0;
+  std::map<nrg::OpKey, nrg::FBlock> blocks;  // in the basis of the run's pre sectors
+  nrg::DevPtr mem;
+  bool updated_this_site = false;
+};
+
+struct nrg_fdm {
+  nrg_run *run = nullptr;
+  int nops = 0;
+  bool last = true;
+  bool have_cur = false;
+  std::vector<int64_t> cur_kept, prev_kept;
+  std::vector<nrg::DevPtr> reduced_mem;   // per sector of the next (earlier) shell
+  std::vector<double *> reduced;          // device pointers, k x k
+  std::vector<int64_t> reduced_k;
+  bool have_reduced = false;
+  nrg::DevPtr hist;                        // 2 * nops * npts
+  double local_gs = 0, local_z = 0;
+  std::vector<double> partitions;
+};
+
+struct nrg_thermo {
+  nrg_run *run = nullptr;
+  int64_t nmax = 0;
+  double bathdim = 0;
+  std::vector<double> temps;
+  bool have_cur = false;
+  std::vector<int64_t> cur_kept, prev_kept;
+  std::vector<std::vector<double>> disc, allv;
+};

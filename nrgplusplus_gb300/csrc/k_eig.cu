@@ -1,0 +1,358 @@
+// Batched dense symmetric eigensolver for the NRG sector blocks
+// (replaces qmatrix::diag -> LAPACKE_dsyevd, qmatrix.hpp:375-404, called per
+// block from nrgcore.hpp:85-89).
+//
+// One CTA solves one block:
+//   1. Householder reduction to tridiagonal form, keeping the full symmetric
+//      matrix so every access is a row (coalesced in global memory, bank-
+//      friendly in shared memory); the reflector u is kept in row i and u/h
+//      in column i for step 2.
+//   2. Accumulation of the orthogonal transform Q in place.
+//   3. Implicit QL with Wilkinson shifts on the tridiagonal (d, e).  One
+//      thread runs the Givens chain of a QL sweep and records (c, s); all
+//      threads then apply the sweep's rotations to their rows of Q, carrying
+//      the running column in a register.
+//   4. Eigenvalues ascending with eigenvectors as columns (the LAPACK
+//      row-major layout the reference publishes in current_hamiltonQ).
+// The matrix lives in shared memory when it fits, otherwise in the block's
+// own global buffer (L2 resident).  The QL sweep count per eigenvalue is
+// capped; a block that hits the cap sets status[b] = 1 and stops.
+#include "nrg_internal.h"
+
+#include <algorithm>
+
+namespace nrg {
+namespace {
+
+constexpr int kThreads = 512;
+constexpr int kWarps = kThreads / 32;
+constexpr int kMaxQlIter = 60;
+constexpr int kSmemBytes = 225 * 1024;
+
+template <typename T> __device__ __forceinline__ T tabs(T x) { return x < T(0) ? -x : x; }
+__device__ __forceinline__ double thypot(double a, double b) { return hypot(a, b); }
+__device__ __forceinline__ float thypot(float a, float b) { return hypotf(a, b); }
+__device__ __forceinline__ double tsqrt(double a) { return sqrt(a); }
+__device__ __forceinline__ float tsqrt(float a) { return sqrtf(a); }
+
+template <typename T> __device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Deterministic CTA-wide sum; red needs kWarps + 1 entries.
+template <typename T> __device__ T block_sum(T v, T *red) {
+  v = warp_sum(v);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  __syncthreads();
+  if (l == 0) red[w] = v;
+  __syncthreads();
+  if (w == 0) {
+    T s = (l < kWarps) ? red[l] : T(0);
+    s = warp_sum(s);
+    if (l == 0) red[kWarps] = s;
+  }
+  __syncthreads();
+  return red[kWarps];
+}
+
+struct Ctl {
+  int m, istop, done, err;
+};
+
+// Core solver on matrix a (n x n, leading dimension lda, either memory space).
+// d, e, u, p: shared arrays of n; cs/sn alias u/p during the QL stage.
+template <typename T>
+__device__ void solve_block(T *a, int lda, int n, T *d, T *e, T *u, T *p, T *red, Ctl *ctl) {
+  const int tid = threadIdx.x;
+  const int warp = tid >> 5, lane = tid & 31;
+#define A(i, j) a[int64_t(i) * lda + (j)]
+  // ---------------- 1. Householder tridiagonalisation
+  for (int i = n - 1; i >= 1; --i) {
+    const int l = i - 1;
+    T scale = T(0);
+    for (int k = tid; k <= l; k += kThreads) scale += tabs(A(i, k));
+    scale = block_sum(scale, red);
+    if (l == 0 || scale == T(0)) {
+      if (tid == 0) { e[i] = A(i, l); d[i] = T(0); }
+      __syncthreads();
+      continue;
+    }
+    T hs = T(0);
+    for (int k = tid; k <= l; k += kThreads) {
+      T x = A(i, k) / scale;
+      A(i, k) = x;
+      u[k] = x;
+      hs += x * x;
+    }
+    T h = block_sum(hs, red);
+    if (tid == 0) {
+      T f = A(i, l);
+      T g = (f >= T(0)) ? -tsqrt(h) : tsqrt(h);
+      e[i] = scale * g;
+      h -= f * g;
+      A(i, l) = f - g;
+      u[l] = f - g;
+      red[kWarps] = h;
+    }
+    __syncthreads();
+    h = red[kWarps];
+    __syncthreads();
+    // p_j = (A u)_j / h, and u_j / h stored in column i
+    for (int j = warp; j <= l; j += kWarps) {
+      T s = T(0);
+      for (int k = lane; k <= l; k += 32) s += A(j, k) * u[k];
+      s = warp_sum(s);
+      if (lane == 0) {
+        p[j] = s / h;
+        A(j, i) = u[j] / h;
+      }
+    }
+    __syncthreads();
+    T fs = T(0);
+    for (int j = tid; j <= l; j += kThreads) fs += p[j] * u[j];
+    const T f = block_sum(fs, red);
+    const T hh = f / (h + h);
+    for (int j = tid; j <= l; j += kThreads) p[j] = p[j] - hh * u[j];  // q
+    __syncthreads();
+    // rank-2 update of the leading (l+1)^2 block, both triangles
+    const int m1 = l + 1;
+    for (int j = warp; j <= l; j += kWarps) {
+      const T uj = u[j], qj = p[j];
+      for (int k = lane; k < m1; k += 32) A(j, k) -= (uj * p[k] + qj * u[k]);
+    }
+    if (tid == 0) d[i] = h;
+    __syncthreads();
+  }
+  if (tid == 0) { d[0] = T(0); e[0] = T(0); }
+  __syncthreads();
+  // ---------------- 2. accumulate Q
+  for (int i = 0; i < n; ++i) {
+    const int l = i - 1;
+    const bool apply = (d[i] != T(0));
+    __syncthreads();
+    if (apply) {
+      // g_j = sum_k u_k Q(k, j); p holds g
+      for (int j = tid; j <= l; j += kThreads) {
+        T g = T(0);
+        for (int k = 0; k <= l; ++k) g += A(i, k) * A(k, j);
+        p[j] = g;
+      }
+      __syncthreads();
+      for (int k = warp; k <= l; k += kWarps) {
+        const T uk = A(k, i);
+        for (int j = lane; j <= l; j += 32) A(k, j) -= p[j] * uk;
+      }
+      __syncthreads();
+    }
+    if (tid == 0) {
+      d[i] = A(i, i);
+      A(i, i) = T(1);
+    }
+    for (int j = tid; j <= l; j += kThreads) {
+      A(j, i) = T(0);
+      A(i, j) = T(0);
+    }
+    __syncthreads();
+  }
+  // ---------------- 3. implicit QL on (d, e)
+  if (tid == 0) {
+    for (int i = 1; i < n; ++i) e[i - 1] = e[i];
+    e[n - 1] = T(0);
+    ctl->err = 0;
+  }
+  __syncthreads();
+  T *cs = u, *sn = p;
+  for (int l = 0; l < n; ++l) {
+    int iter = 0;
+    for (;;) {
+      if (tid == 0) {
+        int m;
+        for (m = l; m < n - 1; ++m) {
+          T dd = tabs(d[m]) + tabs(d[m + 1]);
+          if (tabs(e[m]) + dd == dd) break;
+        }
+        ctl->m = m;
+        ctl->done = (m == l);
+        if (m != l) {
+          if (iter++ >= kMaxQlIter) {
+            ctl->err = 1;
+            ctl->done = 1;
+          } else {
+            T g = (d[l + 1] - d[l]) / (T(2) * e[l]);
+            T r = thypot(g, T(1));
+            g = d[m] - d[l] + e[l] / (g + (g >= T(0) ? tabs(r) : -tabs(r)));
+            T s = T(1), c = T(1), pp = T(0);
+            int i;
+            for (i = m - 1; i >= l; --i) {
+              T f = s * e[i];
+              T b = c * e[i];
+              e[i + 1] = (r = thypot(f, g));
+              if (r == T(0)) {
+                d[i + 1] -= pp;
+                e[m] = T(0);
+                break;
+              }
+              s = f / r;
+              c = g / r;
+              g = d[i + 1] - pp;
+              r = (d[i] - g) * s + T(2) * c * b;
+              d[i + 1] = g + (pp = s * r);
+              g = c * r - b;
+              cs[i] = c;
+              sn[i] = s;
+            }
+            ctl->istop = i;
+            if (!(r == T(0) && i >= l)) {
+              d[l] -= pp;
+              e[l] = g;
+              e[m] = T(0);
+            }
+          }
+        }
+      }
+      __syncthreads();
+      const int done = ctl->done, m = ctl->m, istop = ctl->istop;
+      __syncthreads();  // everyone has read ctl before thread 0 rewrites it
+      if (done) break;
+      // apply rotations i = m-1 .. istop+1 to every row of Q
+      for (int k = tid; k < n; k += kThreads) {
+        T f = A(k, m);
+        for (int i = m - 1; i > istop; --i) {
+          const T zi = A(k, i);
+          A(k, i + 1) = sn[i] * zi + cs[i] * f;
+          f = cs[i] * zi - sn[i] * f;
+        }
+        A(k, istop + 1) = f;
+      }
+      __syncthreads();
+    }
+    if (ctl->err) break;
+  }
+#undef A
+}
+
+// Rank eigenvalues (stable ascending) and write E and U (columns permuted).
+template <typename T>
+__device__ void write_sorted(const T *a, int lda, int n, const T *d, int *rank, double *E, double *U,
+                             int ldu) {
+  for (int i = threadIdx.x; i < n; i += kThreads) {
+    const T x = d[i];
+    int r = 0;
+    for (int j = 0; j < n; ++j) {
+      const T y = d[j];
+      r += (y < x) || (y == x && j < i);
+    }
+    rank[i] = r;
+    E[r] = double(x);
+  }
+  __syncthreads();
+  for (int64_t idx = threadIdx.x; idx < int64_t(n) * n; idx += kThreads) {
+    const int row = int(idx / n), col = int(idx - int64_t(row) * n);
+    U[int64_t(row) * ldu + rank[col]] = double(a[int64_t(row) * lda + col]);
+  }
+}
+
+template <typename T>
+__device__ void carve(char *smem, int n, bool matrix_in_smem, T *&amat, T *&d, T *&e, T *&u, T *&p,
+                      T *&red, int *&rank, Ctl *&ctl) {
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    char *q = smem + off;
+    off += (bytes + 15) & ~size_t(15);
+    return q;
+  };
+  ctl = reinterpret_cast<Ctl *>(take(sizeof(Ctl)));
+  red = reinterpret_cast<T *>(take(sizeof(T) * (kWarps + 1)));
+  d = reinterpret_cast<T *>(take(sizeof(T) * n));
+  e = reinterpret_cast<T *>(take(sizeof(T) * n));
+  u = reinterpret_cast<T *>(take(sizeof(T) * n));
+  p = reinterpret_cast<T *>(take(sizeof(T) * n));
+  rank = reinterpret_cast<int *>(u);  // reused after the solve
+  amat = matrix_in_smem ? reinterpret_cast<T *>(take(sizeof(T) * size_t(n) * (n + 1))) : nullptr;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads, 1)
+k_eig(const EigBlock *__restrict__ blocks, int max_n_smem, int *status) {
+  extern __shared__ __align__(16) char smem[];
+  const EigBlock B = blocks[blockIdx.x];
+  const int n = B.n;
+  if (n == 0) return;
+  const bool in_smem = (n <= max_n_smem);
+  T *amat, *d, *e, *u, *p, *red;
+  int *rank;
+  Ctl *ctl;
+  carve<T>(smem, n, in_smem, amat, d, e, u, p, red, rank, ctl);
+  T *a;
+  int lda;
+  if (in_smem) {
+    a = amat;
+    lda = n + 1;
+  } else if (sizeof(T) == sizeof(double)) {
+    a = reinterpret_cast<T *>(B.H);
+    lda = B.ld;
+  } else {
+    a = reinterpret_cast<T *>(B.W);
+    lda = B.ld;
+  }
+  if (in_smem || sizeof(T) != sizeof(double)) {
+    for (int64_t idx = threadIdx.x; idx < int64_t(n) * n; idx += kThreads) {
+      const int r = int(idx / n), c = int(idx - int64_t(r) * n);
+      a[int64_t(r) * lda + c] = T(B.H[int64_t(r) * B.ld + c]);
+    }
+  }
+  __syncthreads();
+  solve_block<T>(a, lda, n, d, e, u, p, red, ctl);
+  __syncthreads();
+  if (ctl->err) {
+    if (threadIdx.x == 0) status[blockIdx.x] = 1;
+    return;
+  }
+  write_sorted<T>(a, lda, n, d, rank, B.E, B.U, B.ldu);
+}
+
+template <typename T> size_t smem_bytes(int n, bool in_smem) {
+  size_t b = 16 + 16 * ((sizeof(T) * (kWarps + 1) + 15) / 16) + 4 * ((sizeof(T) * n + 15) & ~15);
+  if (in_smem) b += (sizeof(T) * size_t(n) * (n + 1) + 15) & ~size_t(15);
+  return b + 64;
+}
+
+template <typename T> int smem_limit() {
+  int n = 8;
+  while (smem_bytes<T>(n + 1, true) <= size_t(kSmemBytes)) ++n;
+  return n;
+}
+
+template <typename T>
+void launch(const EigBlock *blocks, int nblocks, int max_n, int max_n_smem, int *status,
+            cudaStream_t s) {
+  if (nblocks == 0) return;
+  static bool configured = false;
+  if (!configured) {
+    cudaFuncSetAttribute(k_eig<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
+    configured = true;
+  }
+  // enough shared memory for the largest block of this launch
+  size_t bytes = smem_bytes<T>(max_n, max_n <= max_n_smem);
+  if (max_n > max_n_smem) bytes = std::max(bytes, smem_bytes<T>(max_n_smem, true));
+  if (bytes > size_t(kSmemBytes)) bytes = kSmemBytes;
+  k_eig<T><<<nblocks, kThreads, bytes, s>>>(blocks, max_n_smem, status);
+}
+
+}  // namespace
+
+int eig_smem_limit_f64() { return smem_limit<double>(); }
+int eig_smem_limit_f32() { return smem_limit<float>(); }
+
+void launch_eig_f64(const EigBlock *blocks, int nblocks, int max_n, int max_n_smem, int *status,
+                    cudaStream_t s) {
+  launch<double>(blocks, nblocks, max_n, max_n_smem, status, s);
+}
+void launch_eig_f32(const EigBlock *blocks, int nblocks, int max_n, int max_n_smem, int *status,
+                    cudaStream_t s) {
+  launch<float>(blocks, nblocks, max_n, max_n_smem, status, s);
+}
+
+}  // namespace nrg

@@ -1,0 +1,176 @@
+// Backward-pass kernels: FDM spectral binning, reduced density matrix trace,
+// log-Gaussian broadening and the thermodynamic sums.
+#include "nrg_internal.h"
+
+namespace nrg {
+namespace {
+
+constexpr double kFdmMinEnergy = 1e-10;      // fdmSpectrum.hpp:353
+constexpr double kFdmWeightErrorbar = 1e-20;  // fdmSpectrum.hpp:343
+
+// Spectral weights of one (op, i, j) pair (fdmSpectrum::rhoDotOperators,
+// fdmSpectrum.hpp:207-277):
+//   A = B^T with the kept x kept part zeroed
+//   w+ = |(B rho_j)(v,v') A(v',v)|,  w- = |(rho_i B)(v,v') A(v',v)|
+//   bin = int(ln(1 + |s (E_i[v] - E_j[v'])| / 1e-10) * delE)
+// Weights above 1e-20 in bins [0, npts) are added to the op's histograms.
+__global__ void k_fdm_bin(const FdmPair *__restrict__ pairs, int npairs, double scale, double delE,
+                          double *__restrict__ pos, double *__restrict__ neg, int npts) {
+  const int64_t chunk = blockIdx.x;
+  int lo = 0, hi = npairs - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (pairs[mid].chunk0 <= chunk) lo = mid; else hi = mid - 1;
+  }
+  const FdmPair P = pairs[lo];
+  const int64_t nel = int64_t(P.ni) * P.nj;
+  const int64_t e = (chunk - P.chunk0) * blockDim.x + threadIdx.x;
+  if (e >= nel) return;
+  const int iv = int(e / P.nj), ivp = int(e - int64_t(iv) * P.nj);
+  if (iv < P.kci && ivp < P.kcj) return;  // kept-kept part of A is zero
+  const double a = P.B[e];
+  const double aa = P.rhoA[e] * a;
+  const double bv = P.ARho[e] * a;
+  const int bin = int(log(1 + (fabs(scale * (P.Ei[iv] - P.Ej[ivp])) / kFdmMinEnergy)) * delE);
+  if (bin < npts && bin >= 0) {
+    if (fabs(aa) > kFdmWeightErrorbar) atomicAdd(pos + int64_t(P.op) * npts + bin, fabs(aa));
+    if (fabs(bv) > kFdmWeightErrorbar) atomicAdd(neg + int64_t(P.op) * npts + bin, fabs(bv));
+  }
+}
+
+// reducedRho[ii](it,it') = sum over the sub-blocks (ii, bb) of every block
+// (in the reference's sector order) and the bath index il of
+// rho(off + it + k il, off + it' + k il)
+// (fdmSpectrum::setReduceDensityMatrix, fdmSpectrum.hpp:87-113).
+// One CTA row (blockIdx.y) per output matrix; each element sums its inputs
+// in list order and is written once.
+__global__ void k_partial_trace(const TraceTask *__restrict__ tasks, const TraceIn *__restrict__ ins) {
+  const TraceTask T = tasks[blockIdx.y];
+  const int k = T.k;
+  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < k * k; idx += gridDim.x * blockDim.x) {
+    const int it = idx / k, itp = idx - it * k;
+    double acc = 0.0;
+    for (int j = T.in0; j < T.in1; ++j) {
+      const TraceIn I = ins[j];
+      double s = 0.0;
+      for (int il = 0; il < I.d; ++il)
+        s += I.rho[int64_t(I.off + it + k * il) * I.ld + (I.off + itp + k * il)];
+      acc += s;
+    }
+    T.out[idx] = acc;
+  }
+}
+
+// Log-Gaussian broadening of the binned weights (spec.py:27-44).
+__global__ void k_broaden(const double *__restrict__ e, const double *__restrict__ w, int64_t nbins,
+                          const double *__restrict__ omegas, double b, double *__restrict__ out) {
+  __shared__ double red[32];
+  const double x = omegas[blockIdx.x];
+  const double lx = log(x);
+  double s = 0.0;
+  for (int64_t i = threadIdx.x; i < nbins; i += blockDim.x) {
+    const double z = -b * 0.25 + (lx - log(e[i])) / b;
+    s += w[i] * exp(-z * z);
+  }
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int i = 0; i < int(blockDim.x >> 5); ++i) t += red[i];
+    out[blockIdx.x] = (1.0 / x) * t / (b * sqrt(3.14159265358979323846));
+  }
+}
+
+__device__ __forceinline__ double regulate_exp(double x) {  // fdmThermodynamics.hpp:240-249
+  if (x > 100) return exp(100.0);
+  if (x < -100) return exp(-100.0);
+  return exp(x);
+}
+
+__device__ double cta_sum(double v, double *red) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double t = 0.0;
+  for (int i = 0; i < int(blockDim.x >> 5); ++i) t += red[i];
+  __syncthreads();
+  return t;
+}
+
+// One CTA per temperature: partition function, entropy and specific heat from
+// the discarded energies of every shell (fdmThermodynamics::saveFinalData,
+// fdmThermodynamics.hpp:154-226).  disc holds per shell the discarded
+// energies already shifted by the shell minimum; gs the corrected shell
+// ground energies.
+__global__ void k_thermo(const double *__restrict__ disc, const int64_t *__restrict__ disc_off,
+                         const double *__restrict__ gs, int nshell, const double *__restrict__ temps,
+                         double bathdim, double *__restrict__ wm_buf, double *__restrict__ entropy,
+                         double *__restrict__ cv) {
+  __shared__ double red[32];
+  const double kbt = temps[blockIdx.x];
+  double *wm = wm_buf + int64_t(blockIdx.x) * 2 * nshell;
+  double *zp = wm + nshell;
+  for (int i = 0; i < nshell; ++i) {
+    double z = 0.0;
+    for (int64_t a = disc_off[i] + threadIdx.x; a < disc_off[i + 1]; a += blockDim.x)
+      z += regulate_exp((gs[i] - disc[a]) / kbt);
+    z = cta_sum(z, red);
+    if (threadIdx.x == 0) {
+      wm[i] = z * pow(bathdim, double(i));
+      zp[i] = z;
+    }
+  }
+  __syncthreads();
+  double lpart = 0.0;
+  for (int i = 0; i < nshell; ++i) lpart += wm[i];
+  double eav = 0.0, esq = 0.0;
+  for (int i = 0; i < nshell; ++i) {
+    const double wi = wm[i] / lpart;
+    double s1 = 0.0, s2 = 0.0;
+    for (int64_t a = disc_off[i] + threadIdx.x; a < disc_off[i + 1]; a += blockDim.x) {
+      const double blm = regulate_exp((gs[i] - disc[a]) / kbt) / zp[i];
+      const double x = disc[a] - gs[i];
+      s1 += x * wi * blm;
+      s2 += x * x * wi * blm;
+    }
+    eav += cta_sum(s1, red);
+    esq += cta_sum(s2, red);
+  }
+  if (threadIdx.x == 0) {
+    entropy[blockIdx.x] = log(lpart) + (eav / kbt);
+    cv[blockIdx.x] = (esq - eav * eav) / (kbt * kbt);
+  }
+}
+
+}  // namespace
+
+void launch_fdm_bin(const FdmPair *pairs, int npairs, int64_t nchunks, double scale, double delE,
+                    double *pos, double *neg, int npts, cudaStream_t s) {
+  if (npairs == 0 || nchunks == 0) return;
+  k_fdm_bin<<<unsigned(nchunks), 256, 0, s>>>(pairs, npairs, scale, delE, pos, neg, npts);
+}
+
+void launch_partial_trace(const TraceTask *tasks, int ntask, const TraceIn *ins, int maxk,
+                          cudaStream_t s) {
+  if (ntask == 0 || maxk == 0) return;
+  int gx = (maxk * maxk + 255) / 256;
+  if (gx > 64) gx = 64;
+  k_partial_trace<<<dim3(gx, ntask), 256, 0, s>>>(tasks, ins);
+}
+
+void launch_broaden(const double *e, const double *w, int64_t nbins, const double *omegas,
+                    int64_t nomega, double b, double *out, cudaStream_t s) {
+  if (nomega == 0) return;
+  k_broaden<<<unsigned(nomega), 256, 0, s>>>(e, w, nbins, omegas, b, out);
+}
+
+void launch_thermo(const double *disc, const int64_t *disc_off, const double *gs, int nshell,
+                   const double *temps, int nt, double bathdim, double *wm_buf, double *entropy,
+                   double *cv, cudaStream_t s) {
+  if (nt == 0) return;
+  k_thermo<<<nt, 256, 0, s>>>(disc, disc_off, gs, nshell, temps, bathdim, wm_buf, entropy, cv);
+}
+
+}  // namespace nrg

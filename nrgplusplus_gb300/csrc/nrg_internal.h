@@ -1,0 +1,133 @@
+// Internal descriptors shared by the host engine (engine.cpp) and the CUDA
+// kernels.  All device pointers are absolute so one launch can cover the
+// blocks of many independent runs.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace nrg {
+
+// ---------------------------------------------------------------- assembly
+// One device block = one non-empty (Q,Sz) sector of one run.
+struct AsmBlock {
+  double *H;          // output, row-major n x n with leading dimension ld
+  int n, ld;
+  int sub0, nsub;     // sub-blocks [sub0, sub0 + nsub) of the AsmSub table
+  int pair0;          // nsub*nsub entries of the pair table (int2 term ranges)
+  int pad;
+  int64_t chunk0;     // first 1024-element chunk of this block (flattened grid)
+  double rescale;     // sqrt(Lambda) factor of this run
+  double shift;       // ground-state shift of the previous site (0 if none)
+};
+
+// Sub-block (ii, bb): previous sector ii (kept prefix k) times bath sector bb
+// (d states).  Rows off + it + il*k, it < k, il < d (nrgcore.hpp:179-185).
+struct AsmSub {
+  int off, k, d, pad;
+  const double *eprev;  // previous eigenvalues of sector ii (unshifted)
+  const double *ebath;  // bath energies of sector bb
+};
+
+// One hopping term between sub-blocks a (rows) and b (columns) for operator
+// ip: H[a(it,il), b(it',il')] += F[it,it'] * fb[il',il] * chi * t, plus the
+// transpose (nrgcore.hpp:186-224).
+struct AsmTerm {
+  const double *F;      // previous f-dagger kept block, k_a x k_b, row-major
+  const double *fb;     // bath f-dagger block (bb', bb), d_b x d_a, row-major
+  int ldf, pad;
+  double chi, t;
+};
+
+void launch_assemble(const AsmBlock *blocks, int nblocks, int64_t nchunks, const AsmSub *subs,
+                     const int2 *pairs, const AsmTerm *terms, cudaStream_t s);
+
+// ------------------------------------------------------------- eigensolve
+struct EigBlock {
+  double *H;          // input (destroyed when the block is solved in place)
+  double *U;          // output eigenvectors as columns, row-major n x ldu
+  double *E;          // output eigenvalues, ascending
+  float *W;           // FP32 workspace (n x ld) for the FP32 solver, or null
+  int n, ld, ldu, pad;
+};
+// FP64 Householder tridiagonalisation + implicit QL, one CTA per block.
+// status[b] != 0 if block b hit the QL iteration cap.
+// max_n: largest block of the launch; blocks with n <= max_n_smem are solved
+// in shared memory, larger ones in their own global buffer.
+void launch_eig_f64(const EigBlock *blocks, int nblocks, int max_n, int max_n_smem, int *status,
+                    cudaStream_t s);
+// Same algorithm in FP32 (mixed path first stage); writes U and E in FP64.
+void launch_eig_f32(const EigBlock *blocks, int nblocks, int max_n, int max_n_smem, int *status,
+                    cudaStream_t s);
+int eig_smem_limit_f64();
+int eig_smem_limit_f32();
+
+// ----------------------------------------------------------- grouped GEMM
+// C (M x N) = [C if accumulate] + sum_c alpha_c op(A_c) op(B_c)
+struct GemmGroup {
+  double *C;
+  int ldc, M, N, accumulate;
+  int c0, c1;           // contributions [c0, c1)
+};
+struct GemmContrib {
+  const double *A, *B;
+  int lda, ldb, K, trans;  // trans bit0: A stored K x M; bit1: B stored N x K
+  double alpha;
+};
+struct GemmTile {
+  int group, tm, tn, pad;
+};
+void launch_gemm_f64(const GemmTile *tiles, int ntiles, const GemmGroup *groups,
+                     const GemmContrib *contribs, cudaStream_t s);
+constexpr int GEMM_TILE = 64;
+
+// ------------------------------------------------------------- truncation
+struct TruncRun {
+  int b0, b1;           // device blocks [b0, b1) of this run
+  int e0, e1;           // eigenvalues [e0, e1) in the concatenated index space
+  int64_t nkeep;
+  double *sorted;       // all_eigenvalue output (e1 - e0)
+};
+struct TruncBlock {
+  const double *E;      // ascending eigenvalues of the block
+  int n, e0;            // size and first global element index
+};
+struct TruncResult {    // per run
+  double emin, thr;
+  int64_t kept_total, total;
+  int truncated, pad;
+};
+void launch_truncate(const TruncRun *runs, int nruns, const TruncBlock *blocks, int nblocks,
+                     const int *elem_block, int nelem, int *kept, TruncResult *res,
+                     cudaStream_t s);
+
+// ------------------------------------------------------------- FDM / misc
+struct FdmPair {          // one (op, i, j) spectral contribution
+  const double *rhoA;     // B rho_j   (n_i x n_j, ld nj)
+  const double *ARho;     // rho_i B   (n_i x n_j, ld nj)
+  const double *B;        // operator block (n_i x n_j, ld nj)
+  const double *Ei, *Ej;  // eigenvalues of blocks i and j
+  int ni, nj, kci, kcj;   // sizes and current kept counts
+  int op, pad;
+  int64_t chunk0;
+};
+// chunks of 256 elements; chunk0 of each pair is increasing
+void launch_fdm_bin(const FdmPair *pairs, int npairs, int64_t nchunks, double scale, double delE,
+                    double *pos, double *neg, int npts, cudaStream_t s);
+struct TraceTask {        // one reduced-density-matrix output (k x k)
+  double *out;
+  int k, in0, in1, pad;
+};
+struct TraceIn {          // one sub-block (ii, bb) of a rotated rho block
+  const double *rho;
+  int ld, off, d, pad;
+};
+void launch_partial_trace(const TraceTask *tasks, int ntask, const TraceIn *ins, int maxk,
+                          cudaStream_t s);
+void launch_broaden(const double *e, const double *w, int64_t nbins, const double *omegas,
+                    int64_t nomega, double b, double *out, cudaStream_t s);
+// wm_buf: 2 * nshell * nt doubles of scratch
+void launch_thermo(const double *disc, const int64_t *disc_off, const double *gs, int nshell,
+                   const double *temps, int nt, double bathdim, double *wm_buf, double *entropy,
+                   double *cv, cudaStream_t s);
+
+}  // namespace nrg

@@ -1,0 +1,100 @@
+"""Workload drivers: the reference's example mains re-expressed over the GPU
+API (forward RG flow, operator tracking, FDM backward pass, thermodynamics).
+
+  SIAM RG flow        examples/rgflowSIAM/main.cpp:11-46
+  Kondo               examples/rgflowKondo/main.cpp:12-43, entropyKondo/main.cpp:35-119
+  two-channel SIAM    examples/twoChannelSiam/main.cpp:13-66
+  FDM spectrum        examples/fdmSpectrumSiam/main.cpp:15-141 (2 hoppings for
+                      the single-channel spinhalf bath, as rgflowSIAM uses)
+  thermodynamics      examples/entropySIAM/main.cpp:13-97
+"""
+import math
+
+import numpy as np
+
+from . import api
+from . import models as M
+
+
+def temperature_grid(points=200, tmin=1e-10, tmax=2.0):
+    """examples/entropySIAM/main.cpp:68-76."""
+    d = (points - 1.0) / math.log(tmax / tmin)
+    return tmin * np.exp(np.arange(points) / d)
+
+
+def build_models(kind, eps=-0.25, U=0.5, J=0.25):
+    if kind == "siam":
+        return M.spinhalf(eps, U), M.spinhalf(0.0, 0.0)
+    if kind == "kondo":
+        return M.spinhalf_kondo(J, 0.5), M.spinhalf(0.0, 0.0)
+    if kind == "zero":
+        return M.spinhalf(0.0, 0.0), M.spinhalf(0.0, 0.0)
+    if kind == "twochannel":
+        return M.duplicate_ops(M.spinhalf(eps, U), 2), M.two_channel()
+    raise ValueError(kind)
+
+
+def run_nrg(engine, kind, nkeep, nsites, lam, V=None, eps=-0.25, U=0.5, J=0.25, fdm=False,
+            thermo=False, keep_eigs=True):
+    """One NRG run through the public API.  Kondo-type impurities ('kondo',
+    'zero') have no V site and rescale by sqrt(Lambda) from the first site."""
+    imp, bath = build_models(kind, eps, U, J)
+    kondo = kind in ("kondo", "zero")
+    nops = len(imp.fdag)
+    run = api.NrgCore(engine, imp, bath, nkeep)
+    data = api.NrgData(run)
+    ops = None
+    out = {"eig": [], "kept": [], "run": run}
+    if not kondo:
+        run.add_bath_site([V] * nops, 1.0)
+        if fdm:
+            ops = api.OperatorSet(run, M.d_dag_chi())
+            api.update_system_operator(run, ops)
+        run.update_internal_state()
+    min_it = 0
+    for it in range(nsites):
+        r = math.sqrt(lam) if (kondo or it > 0) else 1.0
+        run.add_bath_site([M.hopping(it, lam)] * nops, r)
+        if fdm:
+            if ops is None:
+                ops = api.OperatorSet(run, M.d_dag_chi())
+            api.update_system_operator(run, ops)
+        if fdm or thermo:
+            if run.checkHigherEnergyDiscarded():
+                data.saveCurrentData(ops)
+            else:
+                min_it += 1
+        run.update_internal_state()
+        if keep_eigs:
+            out["eig"].append(run.all_eigenvalue)
+            out["kept"].append(run.kept_counts)
+    out["min_it"] = min_it
+    out["nsites"] = nsites
+    if fdm:
+        f = api.FdmSpectrum(run, ops.nops)
+        cnt = run.nrg_iterations_cnt
+        for it in range(nsites, min_it, -1):
+            cnt -= 1
+            data.loadCurrentData(cnt)
+            f.calcSpectrum(lam ** (-(it - 1.0) / 2.0))
+        out.update(f.saveFinalData())
+        f.close()
+    if thermo:
+        th = api.FdmThermodynamics(run, temperature_grid())
+        cnt = run.nrg_iterations_cnt
+        lo = min_it + (1 if kondo else 0)
+        for it in range(nsites, lo, -1):
+            cnt -= 1
+            data.loadCurrentData(cnt)
+            th.calcThermodynamics(lam ** (-(1.0 * it - 1.0) / 2.0))
+        out.update(th.saveFinalData())
+        th.close()
+    return out
+
+
+def spectral_function(engine, energies, pos, neg, b=0.6, decades=(-8, 0), per_decade=100):
+    """Log-Gaussian broadened A(w) on 100 points per decade over |w| in
+    [1e-8, 1] (spec.py:27-44 form, without the pi*Gamma display factor)."""
+    n = (decades[1] - decades[0]) * per_decade + 1
+    om = np.logspace(decades[0], decades[1], n)
+    return om, engine.broaden(energies, pos, om, b), engine.broaden(energies, neg, om, b)

@@ -1,0 +1,132 @@
+"""Regenerate the golden fixtures under tests/golden/.
+
+Two sources, both the reference's own numbers:
+
+1. Datasets the reference shipped in examples/entropyKondo/resultsJ0.250000.h5
+   and resultsZero.h5 (written by examples/entropyKondo/main.cpp), read with
+   the minimal HDF5 walker in h5mini.py.
+2. Outputs of the reference engine compiled here by oracle/build_ref.sh
+   (oracle/_ref/ref_nrg), for the workloads named in each case below.
+
+Run from the repository root after ``oracle/build_ref.sh``:
+    python tests/golden/make_golden.py
+Needs the reference tree (default /root/reference or $NRG_REF_ROOT); the
+fixtures it writes are committed so nothing else needs the tree.
+"""
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, HERE)
+
+from h5mini import H5Mini  # noqa: E402
+from oracle.refio import read_named_arrays  # noqa: E402
+
+REF = os.environ.get("NRG_REF_ROOT", "/root/reference")
+BIN = os.path.join(ROOT, "oracle", "_ref", "ref_nrg")
+HEAD = 256  # lowest eigenvalues kept per iteration in the fixtures
+
+
+def shipped_h5():
+    for tag, fn in (("kondo_J0.25", "resultsJ0.250000.h5"), ("kondo_zero", "resultsZero.h5")):
+        h = H5Mini(os.path.join(REF, "examples", "entropyKondo", fn))
+        out = {}
+        n = 0
+        while "Eigenvalues%d" % n in h.datasets:
+            e = h.read("Eigenvalues%d" % n)
+            out["eig_head%d" % n] = e[:HEAD]
+            out["eig_count%d" % n] = np.array([e.size])
+            out["eig_sum%d" % n] = np.array([np.sum(e)])
+            n += 1
+        out["niter"] = np.array([n])
+        for k in ("temperatureArray", "entropy", "specificHeat"):
+            out[k] = h.read(k)
+        np.savez_compressed(os.path.join(HERE, "shipped_%s.npz" % tag), **out)
+        print("shipped", tag, n, "iterations")
+
+
+def run_ref(model, name, **kw):
+    path = os.path.join(ROOT, "_work", "golden_tmp_%s.bin" % name)
+    os.makedirs(os.path.dirname(path), exist_ok=True)
+    args = [BIN, model, path] + ["%s=%r" % (k, v) for k, v in kw.items()]
+    env = dict(os.environ, OMP_NUM_THREADS="8", OPENBLAS_NUM_THREADS="8")
+    subprocess.run(args, check=True, stdout=subprocess.DEVNULL, env=env)
+    d = read_named_arrays(path)
+    os.remove(path)
+    return d
+
+
+def pack_run(d, with_ops=False, with_fdm=False, with_thermo=False):
+    out = {}
+    iters = sorted(int(k[len("Eigenvalues"):]) for k in d
+                   if k.startswith("Eigenvalues") and k[len("Eigenvalues"):].isdigit())
+    out["niter"] = np.array([len(iters)])
+    for i in iters:
+        e = d["Eigenvalues%d" % i]
+        out["eig_head%d" % i] = e[:HEAD]
+        out["eig_count%d" % i] = np.array([e.size])
+        out["eig_sum%d" % i] = np.array([np.sum(e)])
+        out["kept%d" % i] = d["kept%d" % i].astype(np.int64)
+        out["dims%d" % i] = d["dims%d" % i].astype(np.int64)
+    if "EigenvaluesV" in d:
+        out["eig_V"] = d["EigenvaluesV"]
+    out["relgs"] = d["relativeGroundStateEnergy"]
+    out["min_it"] = d["minIterations"]
+    if with_ops:
+        for k, v in d.items():
+            if k.startswith(("F", "D", "EQ")) and "_op" in k or k.startswith("EQ"):
+                out[k] = v
+    if with_fdm:
+        for k, v in d.items():
+            if k.startswith("GreenFnPositiveWeight") or k.startswith("GreenFnNegativeWeight"):
+                nz = np.nonzero(v)[0]
+                out[k + "_idx"] = nz.astype(np.int64)
+                out[k + "_val"] = v[nz]
+    if with_thermo:
+        for k in ("temperatureArray", "entropy", "specificHeat"):
+            out[k] = d[k]
+    return out
+
+
+CASES = [
+    # (fixture name, model, parameters, what to keep)
+    ("ref_c1_siam_nk512", "siam",
+     dict(eps=-0.25, U=0.5, V=0.1, **{"lambda": 2.0}, nkeep=512, nsites=40), {}),
+    ("ref_siam_small_ops", "siam",
+     dict(eps=-0.25, U=0.5, V=0.1, **{"lambda": 2.0}, nkeep=64, nsites=6, fdm=1, dumpops=6),
+     {"with_ops": True, "with_fdm": True}),
+    ("ref_c2_siam_fdm_nk256", "siam",
+     dict(eps=-0.4, U=0.8, V=0.15, **{"lambda": 2.0}, nkeep=256, nsites=30, fdm=1),
+     {"with_fdm": True}),
+    ("ref_c2_siam_fdm_nk1024", "siam",
+     dict(eps=-0.4, U=0.8, V=0.15, **{"lambda": 2.0}, nkeep=1024, nsites=50, fdm=1),
+     {"with_fdm": True}),
+    ("ref_c2_siam_thermo_nk1024", "siam",
+     dict(eps=-0.4, U=0.8, V=0.15, **{"lambda": 2.0}, nkeep=1024, nsites=50, thermo=1),
+     {"with_thermo": True}),
+    ("ref_kondo_thermo_nk512", "kondo",
+     dict(J=0.25, **{"lambda": 2.0}, nkeep=512, nsites=30, thermo=1), {"with_thermo": True}),
+    ("ref_twochannel_nk256", "twochannel",
+     dict(eps=-0.3, U=0.6, V=0.12, **{"lambda": 4.0}, nkeep=256, nsites=8), {}),
+]
+
+
+def main(which=None):
+    shipped_h5()
+    for name, model, params, opts in CASES:
+        if which and name not in which:
+            continue
+        d = run_ref(model, name, **params)
+        out = pack_run(d, **opts)
+        out["params"] = np.array([repr((model, params))])
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+        print("wrote", name)
+
+
+if __name__ == "__main__":
+    main(sys.argv[1:] or None)

@@ -443,6 +443,9 @@ static void batch_add_site(nrg_run *const *runs, int nruns, const double *t, int
   count_launch(e);
   post_launch("assemble");
   check_cuda(cudaEventRecord(e->ev[1], s), "event");
+  if (max_n > eig_max_n_f64())
+    fail(NRG_E_ARG, "block dimension " + std::to_string(max_n) + " exceeds the solver limit " +
+                        std::to_string(eig_max_n_f64()));
   if (e->precision == NRG_PREC_FP64) {
     launch_eig_f64(at<EigBlock>(d, o_eblk), int(eblk_sorted.size()), max_n, e->eig_smem_f64,
                    at<int>(d, o_stat), s);

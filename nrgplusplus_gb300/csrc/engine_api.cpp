@@ -264,6 +264,7 @@ static void fdm_calc(nrg_fdm *f, double scale) {
   int64_t po = 0, chunk = 0;
   for (auto &kv : S.ops) {
     const int ip = std::get<0>(kv.first), i = std::get<1>(kv.first), j = std::get<2>(kv.first);
+    if (ip < 0 || ip >= f->nops) fail(NRG_E_ARG, "snapshot operator index exceeds the FDM operator count");
     if (sd.sectors[i].dev < 0 || sd.sectors[j].dev < 0) continue;
     const int bi = sd.sectors[i].dev, bj = sd.sectors[j].dev;
     const DevBlock &Bi = sd.blocks[bi], &Bj = sd.blocks[bj];

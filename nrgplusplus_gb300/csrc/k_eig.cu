@@ -346,6 +346,16 @@ void launch(const EigBlock *blocks, int nblocks, int max_n, int max_n_smem, int 
 int eig_smem_limit_f64() { return smem_limit<double>(); }
 int eig_smem_limit_f32() { return smem_limit<float>(); }
 
+// Largest block the solver accepts: its d, e, u, p vectors must fit in shared
+// memory even when the matrix itself stays in global memory.
+template <typename T> static int max_block() {
+  int n = 1024;
+  while (smem_bytes<T>(n + 1, false) <= size_t(kSmemBytes)) ++n;
+  return n;
+}
+int eig_max_n_f64() { return max_block<double>(); }
+int eig_max_n_f32() { return max_block<float>(); }
+
 void launch_eig_f64(const EigBlock *blocks, int nblocks, int max_n, int max_n_smem, int *status,
                     cudaStream_t s) {
   launch<double>(blocks, nblocks, max_n, max_n_smem, status, s);

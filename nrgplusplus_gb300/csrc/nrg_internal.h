@@ -60,6 +60,8 @@ void launch_eig_f32(const EigBlock *blocks, int nblocks, int max_n, int max_n_sm
                     cudaStream_t s);
 int eig_smem_limit_f64();
 int eig_smem_limit_f32();
+int eig_max_n_f64();
+int eig_max_n_f32();
 
 // ----------------------------------------------------------- grouped GEMM
 // C (M x N) = [C if accumulate] + sum_c alpha_c op(A_c) op(B_c)

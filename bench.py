@@ -1,0 +1,308 @@
+"""Benchmark: complete SIAM FDM runs per second on one GB300.
+
+One step = one full run of the spectral workload (eps_d=-0.4, U=0.8, V=0.15,
+Lambda=2, Nkeep=1024, 50 Wilson sites): forward NRG with the d-dagger-chi
+operators tracked and device-resident snapshots, the T=0 FDM backward pass
+(binning into 1e5 log bins), log-Gaussian broadening (b=0.6, 100 points per
+decade over |w| in [1e-8, 1]) and entropy / specific heat on the 200-point
+temperature grid.  The reference publishes no number for this metric.
+
+  value : runs/s through the engine, results left on the device
+  e2e   : runs/s through the public C-ABI calls a user makes, with the
+          per-site all_eigenvalue and the final spectra / thermodynamics
+          copied to host buffers inside the timed region
+  --impl reference : the reference's CPU algorithm (the numpy port of the
+          oracle) timed on this host's cores on the same workload
+
+usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORK = dict(kind="siam", nkeep=1024, nsites=50, lam=2.0, eps=-0.4, U=0.8, V=0.15)
+CONFIG = {"workload": "siam_fdm_spectral_c2", "impurity": "spinhalf(eps_d=-0.4,U=0.8)",
+          "V": 0.15, "Lambda": 2.0, "Nkeep": 1024, "sites": 50, "T": 1e-6,
+          "spectral": "T=0 FDM, b=0.6, 801 points |w| in [1e-8,1]",
+          "thermo": "entropy + C on 200-point T grid",
+          "l2": "flushed (256 MiB write) between steps", "precision_path": "plain FP64"}
+METRIC = "SIAM runs/s (full FDM spectral run, Nkeep=1024, 50 sites)"
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    return ws, rank
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle sampling during the timed region."""
+
+    def __init__(self, path):
+        self.path = path
+        self.p = None
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.f = open(self.path, "w")
+            self.p = subprocess.Popen(["nvidia-smi", "--query-gpu=" + q, "--format=csv,noheader,nounits",
+                                       "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+        return self
+
+    def __exit__(self, *a):
+        if self.p:
+            self.p.terminate()
+            self.p.wait()
+            self.f.close()
+
+    def summary(self):
+        sm, mx, reasons = [], 0.0, set()
+        try:
+            for line in open(self.path):
+                f = [x.strip() for x in line.split(",")]
+                if len(f) < 9:
+                    continue
+                try:
+                    sm.append(float(f[1]))
+                    mx = max(mx, float(f[2]))
+                except ValueError:
+                    continue
+                for name, v in zip(("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
+                                    "sw_power_cap"), f[5:9]):
+                    if v.lower().startswith("active"):
+                        reasons.add(name)
+        except OSError:
+            pass
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx or None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def one_run(engine, e2e):
+    """One complete spectral run.  With e2e the caller-visible results are
+    copied to host buffers as a user of the API would read them."""
+    from nrgplusplus_gb300 import api, workloads
+    from nrgplusplus_gb300 import models as M
+    w = WORK
+    imp, bath = M.spinhalf(w["eps"], w["U"]), M.spinhalf(0.0, 0.0)
+    run = api.NrgCore(engine, imp, bath, w["nkeep"])
+    data = api.NrgData(run)
+    run.add_bath_site([w["V"]] * 2, 1.0)
+    ops = api.OperatorSet(run, M.d_dag_chi())
+    api.update_system_operator(run, ops)
+    run.update_internal_state()
+    d2h = 0
+    min_it = 0
+    lam = w["lam"]
+    for it in range(w["nsites"]):
+        run.add_bath_site([M.hopping(it, lam)] * 2, math.sqrt(lam) if it > 0 else 1.0)
+        api.update_system_operator(run, ops)
+        if run.checkHigherEnergyDiscarded():
+            data.saveCurrentData(ops)
+        else:
+            min_it += 1
+        run.update_internal_state()
+        if e2e:
+            d2h += run.all_eigenvalue.nbytes
+    f = api.FdmSpectrum(run, 2)
+    th = api.FdmThermodynamics(run, workloads.temperature_grid())
+    cnt = run.nrg_iterations_cnt
+    for it in range(w["nsites"], min_it, -1):
+        cnt -= 1
+        data.loadCurrentData(cnt)
+        f.calcSpectrum(lam ** (-(it - 1.0) / 2.0))
+        th.calcThermodynamics(lam ** (-(1.0 * it - 1.0) / 2.0))
+    spec = f.saveFinalData()
+    om = __import__("numpy").logspace(-8, 0, 801)
+    Ap = [engine.broaden(spec["GreenFnEnergyPoints"], spec["GreenFnPositiveWeight"][ip], om, 0.6)
+          for ip in range(2)]
+    An = [engine.broaden(spec["GreenFnEnergyPoints"], spec["GreenFnNegativeWeight"][ip], om, 0.6)
+          for ip in range(2)]
+    tdat = th.saveFinalData()
+    d2h += spec["GreenFnPositiveWeight"].nbytes * 2 + sum(a.nbytes for a in Ap + An)
+    d2h += tdat["entropy"].nbytes * 2
+    f.close()
+    th.close()
+    ops.close()
+    run.close()
+    return d2h
+
+
+def time_oracle_run(max_sites):
+    """The oracle port on this host's cores: the same workload, forward sites
+    capped at max_sites (bounded sample)."""
+    from oracle.nrg_oracle import siam_run
+    from nrgplusplus_gb300 import models as M
+    w = WORK
+    t0 = time.perf_counter()
+    siam_run(M.spinhalf(w["eps"], w["U"]), M.spinhalf(0, 0), w["nkeep"], max_sites, w["lam"],
+             V=w["V"], track_ops=M.d_dag_chi(), fdm=True, thermo=False, full_fdag=True)
+    return time.perf_counter() - t0
+
+
+def cpu_cores():
+    try:
+        return len(os.sched_getaffinity(0))
+    except Exception:
+        return os.cpu_count() or 1
+
+
+def reference_arm(args):
+    ws, rank = _dist()
+    if rank != 0:
+        return 0
+    times = []
+    sites = WORK["nsites"]
+    for _ in range(args.warmup if args.warmup < 1 else 1):
+        time_oracle_run(4)
+    for _ in range(args.steps):
+        times.append(time_oracle_run(sites))
+    t = sum(times) / len(times)
+    v = 1.0 / t
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "runs/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (model parameters only)", "config": CONFIG,
+            "cpu_baseline": {"value": v, "unit": "runs/s", "cores": cpu_cores(), "kind": "port",
+                             "sample": "full workload per step (numpy restatement of the reference, "
+                                       "LAPACK syevd + BLAS dgemm, all host threads)"},
+            "e2e": {"value": v, "unit": "runs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours")
+    ap.add_argument("--cpu-sites", type=int, default=12,
+                    help="forward sites of the bounded CPU-baseline sample")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return reference_arm(args)
+    import numpy as np
+    import torch
+    from nrgplusplus_gb300 import api
+    from nrgplusplus_gb300.build import build
+    ws, rank = _dist()
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    build(verbose=False)
+    engine = api.Engine(api.PREC_FP64, device=local)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+
+    def barrier():
+        if ws > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        one_run(engine, e2e=False)
+    # device-side phase profile of one run (CUDA events inside the engine)
+    ev_s, ev_e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    times, d2h = [], 0
+    l0 = engine.launch_count()
+    os.makedirs(os.path.join(ROOT, "gpurun_out"), exist_ok=True)
+    with ClockSampler(os.path.join(ROOT, "gpurun_out", "bench_clocks.csv")) as clk:
+        for _ in range(args.steps):
+            flush.zero_()
+            barrier()
+            t0 = time.perf_counter()
+            one_run(engine, e2e=False)
+            engine.sync()
+            barrier()
+            times.append(time.perf_counter() - t0)
+        launches = engine.launch_count() - l0
+        e2e_times = []
+        for _ in range(args.steps):
+            flush.zero_()
+            barrier()
+            t0 = time.perf_counter()
+            d2h = one_run(engine, e2e=True)
+            engine.sync()
+            barrier()
+            e2e_times.append(time.perf_counter() - t0)
+    t = max(times) if ws == 1 else max(times)
+    if ws > 1:
+        tt = torch.tensor([sum(times)], device="cuda")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        tsum = tt.item()
+    else:
+        tsum = sum(times)
+    per = tsum / args.steps
+    value = ws / per
+    e2e_v = ws / (sum(e2e_times) / args.steps)
+    # roofline of the dominant kernel: eigensolver phase of one site step,
+    # measured with the engine's events on its own stream
+    rf = roofline(engine)
+    cpu = None
+    if rank == 0 and ws == 1:
+        sites = max(1, min(args.cpu_sites, WORK["nsites"]))
+        tc = time_oracle_run(sites)
+        cpu = {"value": 1.0 / tc, "unit": "runs/s (of the sample)", "cores": cpu_cores(), "kind": "port",
+               "sample": "numpy oracle, same model, forward %d of 50 sites + FDM backward "
+                         "(%.1f s); runs/s of that truncated run" % (sites, tc)}
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": "runs/s", "n_gpus": ws, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": per * 1e3, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic (model parameters of the workload; no dataset)",
+                "config": CONFIG, "gpu_launches": launches,
+                "e2e": {"value": e2e_v, "unit": "runs/s", "h2d_bytes_per_step": 4096,
+                        "d2h_bytes_per_step": int(d2h)},
+                "roofline": rf, "cpu_baseline": cpu, "clocks": clk.summary()}
+        print(json.dumps(line))
+    engine.close()
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def roofline(engine):
+    """Eigensolver (dominant kernel) rate for one site of the workload:
+    algorithmic flops = sum over blocks of (10/3) n^3 (tridiagonal reduction +
+    back-transformation), divided by the kernel's event-timed duration."""
+    import math as _m
+    from nrgplusplus_gb300 import api
+    from nrgplusplus_gb300 import models as M
+    w = WORK
+    run = api.NrgCore(engine, M.spinhalf(w["eps"], w["U"]), M.spinhalf(0, 0), w["nkeep"])
+    run.add_bath_site([w["V"]] * 2, 1.0)
+    run.update_internal_state()
+    flops, secs = 0.0, 0.0
+    for it in range(30):
+        run.add_bath_site([M.hopping(it, w["lam"])] * 2, _m.sqrt(w["lam"]) if it else 1.0)
+        if it >= 20:  # steady-state sites (blocks at full size)
+            ph = engine.phase_times()
+            dims = [len(e) for e in run.eigenvaluesQ]
+            flops += sum(10.0 / 3.0 * n ** 3 for n in dims)
+            secs += ph[1] * 1e-3
+        run.update_internal_state()
+    run.close()
+    achieved = flops / secs / 1e12
+    peak = 1.25  # nominal GB300 FP64 (no FP64 figure in MEASURED_PEAKS.json)
+    return {"bound": "fp64", "kernel": "k_eig<double>", "achieved": achieved, "peak": peak,
+            "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
+            "peak_source": "nominal GB300 FP64 1.25 TFLOP/s (not in MEASURED_PEAKS.json)",
+            "per_launch": "sum_blocks (10/3) n^3 over one site's blocks, sites 20-29"}
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -11,6 +11,7 @@ no CPU fallback: without the library or a CUDA device every call raises.
 """
 import ctypes as C
 import os
+import weakref
 
 import numpy as np
 
@@ -126,12 +127,22 @@ class Engine:
 
     def __init__(self, precision=PREC_FP64, device=0, hbm_budget_bytes=0):
         self.h = C.c_void_p()
+        self._children = weakref.WeakSet()
         opts = _EngineOpts(device, precision, hbm_budget_bytes, 0)
         _call(lib().nrg_engine_create, C.byref(opts), C.byref(self.h))
         self.precision = precision
 
+    def _adopt(self, obj):
+        self._children.add(obj)
+
     def close(self):
+        """Release every object still open on this engine, then the engine."""
         if self.h:
+            for ch in list(self._children):
+                if not isinstance(ch, NrgCore):
+                    ch.close()
+            for ch in list(self._children):
+                ch.close()
             lib().nrg_engine_destroy(self.h)
             self.h = C.c_void_p()
 
@@ -176,6 +187,7 @@ class NrgCore:
         self.h = C.c_void_p()
         _call(lib().nrg_run_create, engine.h, C.byref(self._imp.desc), C.byref(self._bath.desc),
               C.c_uint64(nkeep), C.byref(self.h))
+        engine._adopt(self)
 
     def close(self):
         if self.h:
@@ -340,6 +352,7 @@ class OperatorSet:
         desc = _OpDesc(self.nops, len(opi), *[_ip(a) for a in arrs], _dp(self._keep[-1]))
         self.h = C.c_void_p()
         _call(lib().nrg_opset_create, run.h, C.byref(desc), C.byref(self.h))
+        run.engine._adopt(self)
 
     def block(self, ip, i, j):
         r, c = C.c_int64(), C.c_int64()
@@ -392,6 +405,7 @@ class FdmSpectrum:
         self.nops = nops
         self.h = C.c_void_p()
         _call(lib().nrg_fdm_create, run.h, nops, C.byref(self.h))
+        run.engine._adopt(self)
 
     def calcSpectrum(self, energy_scale):
         _call(lib().nrg_fdm_calc, self.h, C.c_double(energy_scale))
@@ -423,6 +437,7 @@ class FdmThermodynamics:
         self.temps = np.ascontiguousarray(temps, float)
         self.h = C.c_void_p()
         _call(lib().nrg_thermo_create, run.h, _dp(self.temps), len(self.temps), C.byref(self.h))
+        run.engine._adopt(self)
 
     def calcThermodynamics(self, energy_scale):
         _call(lib().nrg_thermo_calc, self.h, C.c_double(energy_scale))

@@ -266,6 +266,182 @@ static void build_basis(RunStep &st) {
 
 static int round_up(int x, int m) { return (x + m - 1) / m * m; }
 
+// One grouped-GEMM launch (k_gemm.cu) for a list of outputs.
+struct GemmList {
+  std::vector<GemmGroup> groups;
+  std::vector<GemmContrib> contribs;
+  std::vector<GemmTile> tiles;
+  void out(double *C, int ldc, int M, int N, bool acc, std::initializer_list<GemmContrib> cs) {
+    GemmGroup g{};
+    g.C = C;
+    g.ldc = ldc;
+    g.M = M;
+    g.N = N;
+    g.accumulate = acc ? 1 : 0;
+    g.c0 = int(contribs.size());
+    contribs.insert(contribs.end(), cs.begin(), cs.end());
+    g.c1 = int(contribs.size());
+    const int gi = int(groups.size());
+    groups.push_back(g);
+    for (int tm = 0; tm < (M + GEMM_TILE - 1) / GEMM_TILE; ++tm)
+      for (int tn = 0; tn < (N + GEMM_TILE - 1) / GEMM_TILE; ++tn) tiles.push_back({gi, tm, tn, 0});
+  }
+  void launch(nrg_engine *e, std::vector<DevPtr> &hold) {
+    if (tiles.empty()) return;
+    Arena a;
+    size_t ot = a.add(tiles), og = a.add(groups), oc = a.add(contribs);
+    DevPtr d;
+    char *p = a.push(e, d);
+    hold.push_back(d);
+    launch_gemm_f64(at<GemmTile>(p, ot), int(tiles.size()), at<GemmGroup>(p, og),
+                    at<GemmContrib>(p, oc), e->stream);
+    count_launch(e);
+    post_launch("grouped gemm");
+  }
+};
+
+static GemmContrib contrib(const double *A, int lda, const double *B, int ldb, int K, int trans) {
+  GemmContrib c{};
+  c.A = A;
+  c.lda = lda;
+  c.B = B;
+  c.ldb = ldb;
+  c.K = K;
+  c.trans = trans;
+  c.alpha = 1.0;
+  return c;
+}
+
+constexpr int kRefineSteps = 3;
+constexpr double kClusterTau = 1e-4;  // relative gap below which levels form a cluster
+
+// Mixed-precision eigensolve of every block of the batch: FP32 Householder +
+// QL (k_eig<float>), then kRefineSteps Ogita-Aishima Newton steps with
+// FP64-accurate grouped GEMMs and a final Rayleigh-Ritz pass with FP64
+// Jacobi on near-degenerate clusters (k_refine.cu).  Writes U and E of every
+// block; blocks whose cluster exceeds the in-kernel limit are re-solved with
+// the FP64 solver.  H is left intact.
+static void mixed_eigensolve(nrg_engine *e, std::vector<DevBlock *> &blks, int max_n,
+                             std::vector<DevPtr> &hold) {
+  cudaStream_t s = e->stream;
+  const size_t nb = blks.size();
+  if (nb == 0) return;
+  int64_t sz = 0, wsz = 0, esz = 0;
+  std::vector<int64_t> off(nb), woff(nb, -1), eoff(nb);
+  for (size_t b = 0; b < nb; ++b) {
+    off[b] = sz;
+    sz += int64_t(blks[b]->n) * blks[b]->ld;
+    eoff[b] = esz;
+    esz += blks[b]->n;
+    if (blks[b]->n > e->eig_smem_f32) {
+      woff[b] = wsz;
+      wsz += int64_t(blks[b]->n) * blks[b]->ld;
+    }
+  }
+  DevPtr mx0 = dalloc(e, sz * 8), mx1 = dalloc(e, sz * 8), my = dalloc(e, sz * 8),
+         ms = dalloc(e, sz * 8), mg = dalloc(e, sz * 8), me2 = dalloc(e, sz * 8),
+         mw = dalloc(e, wsz * 4 + 16), mlam = dalloc(e, esz * 8 + 8);
+  hold.insert(hold.end(), {mx0, mx1, my, ms, mg, me2, mw, mlam});
+  auto P = [](DevPtr &m, int64_t o) { return static_cast<double *>(m->ptr) + o; };
+  double *X[2] = {P(mx0, 0), P(mx1, 0)};
+  // FP32 solve: eigenvectors (as FP64) into X0
+  std::vector<EigBlock> eb(nb);
+  for (size_t b = 0; b < nb; ++b) {
+    eb[b].H = blks[b]->H;
+    eb[b].U = X[0] + off[b];
+    eb[b].E = P(mlam, eoff[b]);
+    eb[b].W = woff[b] >= 0 ? static_cast<float *>(mw->ptr) + woff[b] : nullptr;
+    eb[b].n = blks[b]->n;
+    eb[b].ld = blks[b]->ld;
+    eb[b].ldu = blks[b]->ld;
+  }
+  std::vector<int> stat(nb + 1, 0);
+  std::vector<RefineBlock> rb(nb);
+  Arena a;
+  size_t oeb = a.add(eb), ost = a.add(stat);
+  const size_t orb = a.add(rb);  // filled per step below (host copy re-uploaded)
+  DevPtr dd;
+  char *dp = a.push(e, dd);
+  hold.push_back(dd);
+  launch_eig_f32(at<EigBlock>(dp, oeb), int(nb), max_n, e->eig_smem_f32, at<int>(dp, ost), s);
+  count_launch(e);
+  post_launch("eigensolve f32");
+  int cur = 0;
+  for (int step = 0; step <= kRefineSteps; ++step) {
+    const bool final = (step == kRefineSteps);
+    GemmList g1, g2;
+    for (size_t b = 0; b < nb; ++b) {
+      const int n = blks[b]->n, ld = blks[b]->ld;
+      double *x = X[cur] + off[b];
+      g1.out(P(my, off[b]), ld, n, n, false, {contrib(blks[b]->H, ld, x, ld, n, 0)});       // Y = H X
+      g2.out(P(ms, off[b]), ld, n, n, false, {contrib(x, ld, P(my, off[b]), ld, n, 1)});    // S = X^T Y
+      g2.out(P(mg, off[b]), ld, n, n, false, {contrib(x, ld, x, ld, n, 1)});                // G = X^T X
+      rb[b].S = P(ms, off[b]);
+      rb[b].G = P(mg, off[b]);
+      rb[b].E2 = P(me2, off[b]);
+      rb[b].X = x;
+      rb[b].U = blks[b]->U;
+      rb[b].Eout = blks[b]->E;
+      rb[b].n = n;
+      rb[b].ld = ld;
+      rb[b].ldu = blks[b]->ld;
+    }
+    g1.launch(e, hold);
+    g2.launch(e, hold);
+    check_cuda(cudaMemcpyAsync(dp + orb, rb.data(), nb * sizeof(RefineBlock), cudaMemcpyHostToDevice, s),
+               "refine descriptors");
+    if (final) {
+      launch_oa_final(at<RefineBlock>(dp, orb), int(nb), max_n, kClusterTau, at<int>(dp, ost), s);
+      count_launch(e);
+      post_launch("refine final");
+      break;
+    }
+    launch_oa_update(at<RefineBlock>(dp, orb), int(nb), max_n, kClusterTau, s);
+    count_launch(e);
+    post_launch("refine update");
+    // X' = X + X E
+    check_cuda(cudaMemcpyAsync(X[1 - cur], X[cur], sz * 8, cudaMemcpyDeviceToDevice, s), "X copy");
+    GemmList g3;
+    for (size_t b = 0; b < nb; ++b) {
+      const int n = blks[b]->n, ld = blks[b]->ld;
+      g3.out(X[1 - cur] + off[b], ld, n, n, true, {contrib(X[cur] + off[b], ld, P(me2, off[b]), ld, n, 0)});
+    }
+    g3.launch(e, hold);
+    cur = 1 - cur;
+  }
+  check_cuda(cudaMemcpyAsync(stat.data(), dp + ost, nb * sizeof(int), cudaMemcpyDeviceToHost, s),
+             "refine status");
+  check_cuda(cudaStreamSynchronize(s), "refine");
+  std::vector<EigBlock> redo;
+  for (size_t b = 0; b < nb; ++b) {
+    if (stat[b] == 1) fail(NRG_E_EIG, "FP32 block eigensolver did not converge");
+    if (stat[b] == 2) {
+      EigBlock x{};
+      x.H = blks[b]->H;
+      x.U = blks[b]->U;
+      x.E = blks[b]->E;
+      x.n = blks[b]->n;
+      x.ld = blks[b]->ld;
+      x.ldu = blks[b]->ld;
+      redo.push_back(x);
+    }
+  }
+  if (!redo.empty()) {  // large near-degenerate cluster: FP64 solve of that block
+    Arena r;
+    std::vector<int> st2(redo.size() + 1, 0);
+    size_t o1 = r.add(redo), o2 = r.add(st2);
+    DevPtr rd;
+    char *rp = r.push(e, rd);
+    hold.push_back(rd);
+    int mn = 0;
+    for (auto &x : redo) mn = std::max(mn, x.n);
+    launch_eig_f64(at<EigBlock>(rp, o1), int(redo.size()), mn, e->eig_smem_f64, at<int>(rp, o2), s);
+    count_launch(e);
+    post_launch("eigensolve f64 (cluster fallback)");
+    e->fallback_blocks += redo.size();
+  }
+}
+
 static void batch_add_site(nrg_run *const *runs, int nruns, const double *t, int nt,
                            const double *rescale) {
   if (nruns <= 0) return;
@@ -449,11 +625,17 @@ static void batch_add_site(nrg_run *const *runs, int nruns, const double *t, int
   if (e->precision == NRG_PREC_FP64) {
     launch_eig_f64(at<EigBlock>(d, o_eblk), int(eblk_sorted.size()), max_n, e->eig_smem_f64,
                    at<int>(d, o_stat), s);
+    count_launch(e);
+    post_launch("eigensolve");
   } else {
-    fail(NRG_E_ARG, "mixed precision path not available in this build");
+    if (max_n > refine_max_n())
+      fail(NRG_E_ARG, "block dimension " + std::to_string(max_n) + " exceeds the refinement limit");
+    std::vector<DevBlock *> blks;
+    for (auto &st : steps)
+      for (auto &db : st.site->blocks) blks.push_back(&db);
+    std::stable_sort(blks.begin(), blks.end(), [](DevBlock *a, DevBlock *b) { return a->n > b->n; });
+    mixed_eigensolve(e, blks, max_n, hold);
   }
-  count_launch(e);
-  post_launch("eigensolve");
   check_cuda(cudaEventRecord(e->ev[2], s), "event");
   launch_truncate(at<TruncRun>(d, o_trun), nruns, at<TruncBlock>(d, o_tblk), nblk_total,
                   at<int>(d, o_elem), nelem_total, at<int>(d, o_kept), at<TruncResult>(d, o_tres), s);

@@ -108,6 +108,7 @@ struct nrg_engine {
   int eig_smem_f64 = 0, eig_smem_f32 = 0;
   int *d_status = nullptr;
   size_t status_cap = 0;
+  uint64_t fallback_blocks = 0;  // mixed path: blocks re-solved in FP64
 };
 
 struct nrg_run {

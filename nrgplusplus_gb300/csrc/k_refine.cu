@@ -1,0 +1,234 @@
+// FP64-accurate refinement of FP32 eigenpairs (mixed-precision path).
+//
+// The FP32 block solver (k_eig<float>) gives eigenvectors X good to ~1e-6.
+// Each refinement step is the Newton-type update of Ogita & Aishima
+// ("Iterative refinement for symmetric eigenvalue decomposition", Japan J.
+// Indust. Appl. Math. 35 (2018)):
+//     S = X^T A X,  G = X^T X  (FP64-accurate GEMMs, all SMs)
+//     l_i  = s_ii / g_ii
+//     e_ii = (1 - g_ii) / 2
+//     e_ij = (s_ij - l_j g_ij) / (l_j - l_i)   if |l_i - l_j| > tau
+//          = -g_ij / 2                         otherwise (near-degenerate pair:
+//                                               orthonormalise only)
+//     X <- X + X E
+// which converges quadratically for separated eigenvalues.  The final pass
+// takes the Rayleigh quotients l_i and, for every run of sorted l with gaps
+// <= tau (a near-degenerate cluster), diagonalises the cluster's block of S
+// with a cyclic FP64 Jacobi iteration and rotates the cluster's columns.
+// Only these O(n^2) element-wise steps and the tiny cluster problems run on
+// the FP64 pipe per block; the O(n^3) work is in the grouped GEMMs.
+#include "nrg_internal.h"
+
+namespace nrg {
+namespace {
+
+constexpr int kThreads = 512;
+constexpr int kWarps = kThreads / 32;
+constexpr int kMaxCluster = 64;
+constexpr int kMaxJacobiSweeps = 30;
+
+__device__ double block_max(double v, double *red) {
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double m = red[0];
+  for (int w = 1; w < kWarps; ++w) m = fmax(m, red[w]);
+  __syncthreads();
+  return m;
+}
+
+__global__ void __launch_bounds__(kThreads)
+k_oa_update(const RefineBlock *__restrict__ blocks, double tau_rel) {
+  extern __shared__ __align__(16) double sm[];
+  __shared__ double red[kWarps];
+  const RefineBlock B = blocks[blockIdx.x];
+  const int n = B.n;
+  double *lam = sm;
+  double local = 0.0;
+  for (int i = threadIdx.x; i < n; i += kThreads) {
+    const double l = B.S[int64_t(i) * B.ld + i] / B.G[int64_t(i) * B.ld + i];
+    lam[i] = l;
+    local = fmax(local, fabs(l));
+  }
+  const double tau = tau_rel * fmax(1.0, block_max(local, red));
+  for (int64_t idx = threadIdx.x; idx < int64_t(n) * n; idx += kThreads) {
+    const int i = int(idx / n), j = int(idx - int64_t(i) * n);
+    const double g = B.G[int64_t(i) * B.ld + j];
+    double e;
+    if (i == j) {
+      e = 0.5 * (1.0 - g);
+    } else {
+      const double d = lam[j] - lam[i];
+      e = (fabs(d) > tau) ? (B.S[int64_t(i) * B.ld + j] - lam[j] * g) / d : -0.5 * g;
+    }
+    B.E2[int64_t(i) * B.ld + j] = e;
+  }
+}
+
+// Final Rayleigh-Ritz pass: eigenvalues, cluster diagonalisation, sorted
+// output (E ascending, U columns in the same order).  status[b] = 2 when a
+// cluster exceeds kMaxCluster (the host then re-solves the block in FP64).
+__global__ void __launch_bounds__(kThreads)
+k_oa_final(const RefineBlock *__restrict__ blocks, double tau_rel, int *status) {
+  extern __shared__ __align__(16) double sm[];
+  __shared__ double red[kWarps];
+  __shared__ int ncl, jac_flag;
+  const RefineBlock B = blocks[blockIdx.x];
+  const int n = B.n;
+  double *lam = sm;                                   // n
+  double *lams = lam + n;                             // n (sorted)
+  double *Sc = lams + n;                              // kMaxCluster^2
+  double *Qc = Sc + kMaxCluster * kMaxCluster;        // kMaxCluster^2
+  int *perm = reinterpret_cast<int *>(Qc + kMaxCluster * kMaxCluster);  // n
+  int *cl = perm + n;                                 // up to n/2 + 1 cluster starts/ends
+  int *order = cl + n + 2;                            // kMaxCluster
+  double local = 0.0;
+  for (int i = threadIdx.x; i < n; i += kThreads) {
+    const double l = B.S[int64_t(i) * B.ld + i] / B.G[int64_t(i) * B.ld + i];
+    lam[i] = l;
+    local = fmax(local, fabs(l));
+  }
+  const double tau = tau_rel * fmax(1.0, block_max(local, red));
+  for (int i = threadIdx.x; i < n; i += kThreads) {
+    const double x = lam[i];
+    int r = 0;
+    for (int j = 0; j < n; ++j) {
+      const double y = lam[j];
+      r += (y < x) || (y == x && j < i);
+    }
+    perm[r] = i;
+    lams[r] = x;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int c = 0, k = 0;
+    while (k < n) {
+      int e = k + 1;
+      while (e < n && lams[e] - lams[e - 1] <= tau) ++e;
+      if (e - k > 1) {
+        cl[2 * c] = k;
+        cl[2 * c + 1] = e;
+        ++c;
+      }
+      k = e;
+    }
+    ncl = c;
+  }
+  __syncthreads();
+  // plain columns: U[:, k] = X[:, perm[k]], E[k] = lams[k]
+  for (int k = threadIdx.x; k < n; k += kThreads) B.Eout[k] = lams[k];
+  for (int64_t idx = threadIdx.x; idx < int64_t(n) * n; idx += kThreads) {
+    const int r = int(idx / n), k = int(idx - int64_t(r) * n);
+    B.U[int64_t(r) * B.ldu + k] = B.X[int64_t(r) * B.ld + perm[k]];
+  }
+  __syncthreads();
+  for (int q = 0; q < ncl; ++q) {
+    const int a = cl[2 * q], c = cl[2 * q + 1] - a;
+    if (c > kMaxCluster) {
+      if (threadIdx.x == 0) status[blockIdx.x] = 2;
+      return;
+    }
+    for (int idx = threadIdx.x; idx < c * c; idx += kThreads) {
+      const int p = idx / c, s = idx - p * c;
+      Sc[idx] = B.S[int64_t(perm[a + p]) * B.ld + perm[a + s]];
+      Qc[idx] = (p == s) ? 1.0 : 0.0;
+    }
+    __syncthreads();
+    // cyclic Jacobi on the c x c cluster block (symmetrised on the fly)
+    for (int sweep = 0; sweep < kMaxJacobiSweeps; ++sweep) {
+      if (threadIdx.x == 0) jac_flag = 0;
+      __syncthreads();
+      for (int p = 0; p < c - 1; ++p)
+        for (int s = p + 1; s < c; ++s) {
+          const double apq = 0.5 * (Sc[p * c + s] + Sc[s * c + p]);
+          const double app = Sc[p * c + p], aqq = Sc[s * c + s];
+          if (fabs(apq) <= 1e-300 || fabs(apq) <= 1e-17 * (fabs(app) + fabs(aqq))) continue;
+          const double th = (aqq - app) / (2.0 * apq);
+          const double t = (th >= 0 ? 1.0 : -1.0) / (fabs(th) + sqrt(th * th + 1.0));
+          const double cs = 1.0 / sqrt(t * t + 1.0), sn = t * cs;
+          __syncthreads();
+          // rows p, s then columns p, s of Sc; columns p, s of Qc
+          for (int k = threadIdx.x; k < c; k += kThreads) {
+            const double xp = Sc[p * c + k], xs = Sc[s * c + k];
+            Sc[p * c + k] = cs * xp - sn * xs;
+            Sc[s * c + k] = sn * xp + cs * xs;
+          }
+          __syncthreads();
+          for (int k = threadIdx.x; k < c; k += kThreads) {
+            const double xp = Sc[k * c + p], xs = Sc[k * c + s];
+            Sc[k * c + p] = cs * xp - sn * xs;
+            Sc[k * c + s] = sn * xp + cs * xs;
+            const double qp = Qc[k * c + p], qs = Qc[k * c + s];
+            Qc[k * c + p] = cs * qp - sn * qs;
+            Qc[k * c + s] = sn * qp + cs * qs;
+          }
+          if (threadIdx.x == 0) jac_flag = 1;
+          __syncthreads();
+        }
+      __syncthreads();
+      const int more = jac_flag;
+      __syncthreads();
+      if (!more) break;
+    }
+    // order the cluster's eigenvalues ascending
+    if (threadIdx.x == 0) {
+      for (int t = 0; t < c; ++t) order[t] = t;
+      for (int t = 1; t < c; ++t) {
+        int v = order[t], u = t - 1;
+        while (u >= 0 && Sc[order[u] * c + order[u]] > Sc[v * c + v]) {
+          order[u + 1] = order[u];
+          --u;
+        }
+        order[u + 1] = v;
+      }
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < c; t += kThreads) B.Eout[a + t] = Sc[order[t] * c + order[t]];
+    for (int64_t idx = threadIdx.x; idx < int64_t(n) * c; idx += kThreads) {
+      const int r = int(idx / c), t = int(idx - int64_t(r) * c);
+      const int col = order[t];
+      double v = 0.0;
+      for (int p = 0; p < c; ++p) v += B.X[int64_t(r) * B.ld + perm[a + p]] * Qc[p * c + col];
+      B.U[int64_t(r) * B.ldu + a + t] = v;
+    }
+    __syncthreads();
+  }
+}
+
+size_t final_smem(int n) {
+  return sizeof(double) * (2 * size_t(n) + 2 * kMaxCluster * kMaxCluster) +
+         sizeof(int) * (2 * size_t(n) + 2 + kMaxCluster) + 64;
+}
+
+}  // namespace
+
+int refine_max_n() {
+  int n = 64;
+  while (final_smem(n + 1) <= 225 * 1024) ++n;
+  return n;
+}
+
+void launch_oa_update(const RefineBlock *blocks, int nblocks, int max_n, double tau_rel,
+                      cudaStream_t s) {
+  if (nblocks == 0) return;
+  static bool cfg = false;
+  if (!cfg) {
+    cudaFuncSetAttribute(k_oa_update, cudaFuncAttributeMaxDynamicSharedMemorySize, 225 * 1024);
+    cfg = true;
+  }
+  k_oa_update<<<nblocks, kThreads, sizeof(double) * size_t(max_n) + 16, s>>>(blocks, tau_rel);
+}
+
+void launch_oa_final(const RefineBlock *blocks, int nblocks, int max_n, double tau_rel, int *status,
+                     cudaStream_t s) {
+  if (nblocks == 0) return;
+  static bool cfg = false;
+  if (!cfg) {
+    cudaFuncSetAttribute(k_oa_final, cudaFuncAttributeMaxDynamicSharedMemorySize, 225 * 1024);
+    cfg = true;
+  }
+  k_oa_final<<<nblocks, kThreads, final_smem(max_n), s>>>(blocks, tau_rel, status);
+}
+
+}  // namespace nrg

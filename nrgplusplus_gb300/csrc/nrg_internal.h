@@ -63,6 +63,23 @@ int eig_smem_limit_f32();
 int eig_max_n_f64();
 int eig_max_n_f32();
 
+// ------------------------------------------- mixed-precision refinement
+struct RefineBlock {
+  const double *S, *G;  // X^T A X and X^T X (n x n, leading dimension ld)
+  double *E2;           // Newton correction E (ld)
+  const double *X;      // current eigenvector estimate (ld)
+  double *U;            // final eigenvectors, columns ascending (ldu)
+  double *Eout;         // final eigenvalues, ascending
+  int n, ld, ldu, pad;
+};
+void launch_oa_update(const RefineBlock *blocks, int nblocks, int max_n, double tau_rel,
+                      cudaStream_t s);
+// status[b] = 2: a near-degenerate cluster is too large for the in-kernel
+// Jacobi; the host re-solves that block with the FP64 solver.
+void launch_oa_final(const RefineBlock *blocks, int nblocks, int max_n, double tau_rel, int *status,
+                     cudaStream_t s);
+int refine_max_n();
+
 // ----------------------------------------------------------- grouped GEMM
 // C (M x N) = [C if accumulate] + sum_c alpha_c op(A_c) op(B_c)
 struct GemmGroup {

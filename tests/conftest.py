@@ -26,3 +26,13 @@ def gpu_engine():
     eng = api.Engine(api.PREC_FP64)
     yield eng
     eng.close()
+
+
+@pytest.fixture(scope="session")
+def mixed_engine():
+    from nrgplusplus_gb300 import api
+    from nrgplusplus_gb300.build import build
+    build(verbose=False)
+    eng = api.Engine(api.PREC_MIXED)
+    yield eng
+    eng.close()

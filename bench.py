@@ -33,7 +33,7 @@ CONFIG = {"workload": "siam_fdm_spectral_c2", "impurity": "spinhalf(eps_d=-0.4,U
           "V": 0.15, "Lambda": 2.0, "Nkeep": 1024, "sites": 50, "T": 1e-6,
           "spectral": "T=0 FDM, b=0.6, 801 points |w| in [1e-8,1]",
           "thermo": "entropy + C on 200-point T grid",
-          "l2": "flushed (256 MiB write) between steps", "precision_path": "plain FP64"}
+          "l2": "flushed (256 MiB write) between steps"}
 METRIC = "SIAM runs/s (full FDM spectral run, Nkeep=1024, 50 sites)"
 
 
@@ -183,6 +183,36 @@ def reference_arm(args):
     return 0
 
 
+# nominal per-GPU peaks for the pipes MEASURED_PEAKS.json does not cover
+FP64_PEAK_TFLOPS = 1.25   # GB300 FP64 (vector and tensor) dense
+FP32_PEAK_TFLOPS = 80.5   # 152 SMs x 128 FP32 lanes x 2 flops x 2.07 GHz
+PEAKS = {"k_gemm_f64": ("fp64", FP64_PEAK_TFLOPS), "k_eig_f64": ("fp64", FP64_PEAK_TFLOPS),
+         "k_eig_f32": ("fp32", FP32_PEAK_TFLOPS)}
+
+
+def kernel_profile(engine):
+    """One extra run with per-kernel CUDA events on the engine stream."""
+    engine.set_profiling(True)
+    engine.kernel_times()
+    one_run(engine, e2e=False)
+    kt = engine.kernel_times()
+    engine.set_profiling(False)
+    return kt
+
+
+def roofline_from(kt):
+    top = max(kt.items(), key=lambda kv: kv[1][0])
+    name, (ms, work, n) = top
+    bound, peak = PEAKS.get(name, ("fp64", FP64_PEAK_TFLOPS))
+    achieved = work / (ms * 1e-3) / 1e12 if ms > 0 else 0.0
+    return {"bound": bound, "kernel": name, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+            "frac": achieved / peak if peak else None, "traffic": None,
+            "peak_source": "nominal GB300 %s (MEASURED_PEAKS.json has HBM and bf16 only)" % bound,
+            "launches": n, "ms_total": ms,
+            "per_launch": "algorithmic flops summed over the launch's blocks: 2MNK per GEMM "
+                          "contribution, (10/3) n^3 per eigensolved block"}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -191,10 +221,10 @@ def main():
     ap.add_argument("--impl", default="ours")
     ap.add_argument("--cpu-sites", type=int, default=12,
                     help="forward sites of the bounded CPU-baseline sample")
+    ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 comparator")
     args = ap.parse_args()
     if args.impl == "reference":
         return reference_arm(args)
-    import numpy as np
     import torch
     from nrgplusplus_gb300 import api
     from nrgplusplus_gb300.build import build
@@ -205,7 +235,7 @@ def main():
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     torch.cuda.set_device(local)
     build(verbose=False)
-    engine = api.Engine(api.PREC_FP64, device=local)
+    engine = api.Engine(api.PREC_MIXED, device=local)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
 
     def barrier():
@@ -215,8 +245,6 @@ def main():
 
     for _ in range(args.warmup):
         one_run(engine, e2e=False)
-    # device-side phase profile of one run (CUDA events inside the engine)
-    ev_s, ev_e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     times, d2h = [], 0
     l0 = engine.launch_count()
     os.makedirs(os.path.join(ROOT, "gpurun_out"), exist_ok=True)
@@ -229,7 +257,7 @@ def main():
             engine.sync()
             barrier()
             times.append(time.perf_counter() - t0)
-        launches = engine.launch_count() - l0
+        launches = (engine.launch_count() - l0) // args.steps
         e2e_times = []
         for _ in range(args.steps):
             flush.zero_()
@@ -239,19 +267,31 @@ def main():
             engine.sync()
             barrier()
             e2e_times.append(time.perf_counter() - t0)
-    t = max(times) if ws == 1 else max(times)
     if ws > 1:
-        tt = torch.tensor([sum(times)], device="cuda")
+        tt = torch.tensor([sum(times), sum(e2e_times)], device="cuda")
         torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        tsum = tt.item()
+        tsum, esum = tt[0].item(), tt[1].item()
     else:
-        tsum = sum(times)
+        tsum, esum = sum(times), sum(e2e_times)
     per = tsum / args.steps
     value = ws / per
-    e2e_v = ws / (sum(e2e_times) / args.steps)
-    # roofline of the dominant kernel: eigensolver phase of one site step,
-    # measured with the engine's events on its own stream
-    rf = roofline(engine)
+    e2e_v = ws / (esum / args.steps)
+    kt = kernel_profile(engine)
+    rf = roofline_from(kt)
+    engine.close()
+    plain = None
+    if not args.no_fp64:
+        e64 = api.Engine(api.PREC_FP64, device=local)
+        flush.zero_()
+        barrier()
+        t0 = time.perf_counter()
+        one_run(e64, e2e=False)
+        e64.sync()
+        barrier()
+        t64 = time.perf_counter() - t0
+        e64.close()
+        plain = {"value": ws / t64, "unit": "runs/s", "ms_per_run": t64 * 1e3,
+                 "speedup_mixed_over_fp64": value / (ws / t64)}
     cpu = None
     if rank == 0 and ws == 1:
         sites = max(1, min(args.cpu_sites, WORK["nsites"]))
@@ -262,46 +302,19 @@ def main():
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "runs/s", "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": per * 1e3, "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64 (mixed)",
                 "data": "synthetic (model parameters of the workload; no dataset)",
-                "config": CONFIG, "gpu_launches": launches,
+                "config": dict(CONFIG, precision_path="mixed: FP32 block solve + FP64-accurate refinement"),
+                "gpu_launches": launches,
                 "e2e": {"value": e2e_v, "unit": "runs/s", "h2d_bytes_per_step": 4096,
                         "d2h_bytes_per_step": int(d2h)},
-                "roofline": rf, "cpu_baseline": cpu, "clocks": clk.summary()}
+                "plain_fp64": plain, "roofline": rf,
+                "kernels_ms_per_run": {k: round(v[0], 3) for k, v in kt.items()},
+                "cpu_baseline": cpu, "clocks": clk.summary()}
         print(json.dumps(line))
-    engine.close()
     if ws > 1:
         torch.distributed.destroy_process_group()
     return 0
-
-
-def roofline(engine):
-    """Eigensolver (dominant kernel) rate for one site of the workload:
-    algorithmic flops = sum over blocks of (10/3) n^3 (tridiagonal reduction +
-    back-transformation), divided by the kernel's event-timed duration."""
-    import math as _m
-    from nrgplusplus_gb300 import api
-    from nrgplusplus_gb300 import models as M
-    w = WORK
-    run = api.NrgCore(engine, M.spinhalf(w["eps"], w["U"]), M.spinhalf(0, 0), w["nkeep"])
-    run.add_bath_site([w["V"]] * 2, 1.0)
-    run.update_internal_state()
-    flops, secs = 0.0, 0.0
-    for it in range(30):
-        run.add_bath_site([M.hopping(it, w["lam"])] * 2, _m.sqrt(w["lam"]) if it else 1.0)
-        if it >= 20:  # steady-state sites (blocks at full size)
-            ph = engine.phase_times()
-            dims = [len(e) for e in run.eigenvaluesQ]
-            flops += sum(10.0 / 3.0 * n ** 3 for n in dims)
-            secs += ph[1] * 1e-3
-        run.update_internal_state()
-    run.close()
-    achieved = flops / secs / 1e12
-    peak = 1.25  # nominal GB300 FP64 (no FP64 figure in MEASURED_PEAKS.json)
-    return {"bound": "fp64", "kernel": "k_eig<double>", "achieved": achieved, "peak": peak,
-            "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
-            "peak_source": "nominal GB300 FP64 1.25 TFLOP/s (not in MEASURED_PEAKS.json)",
-            "per_launch": "sum_blocks (10/3) n^3 over one site's blocks, sites 20-29"}
 
 
 if __name__ == "__main__":

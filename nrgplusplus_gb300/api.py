@@ -57,7 +57,8 @@ class RunInfo(C.Structure):
 
 EXPORTS = [
     "nrg_last_error", "nrg_engine_create", "nrg_engine_destroy", "nrg_engine_phase_times",
-    "nrg_engine_launch_count", "nrg_engine_sync", "nrg_run_create", "nrg_run_destroy",
+    "nrg_engine_launch_count", "nrg_engine_set_profiling", "nrg_engine_kernel_times",
+    "nrg_engine_sync", "nrg_run_create", "nrg_run_destroy",
     "nrg_run_set_parameters", "nrg_run_set_bath", "nrg_run_add_site", "nrg_run_update_state",
     "nrg_run_check_discarded", "nrg_run_get_info", "nrg_run_get_all_eigenvalues",
     "nrg_run_get_relgs", "nrg_run_get_sectors", "nrg_run_get_eigenvalues_q", "nrg_run_get_kept",
@@ -165,6 +166,22 @@ class Engine:
 
     def sync(self):
         _call(lib().nrg_engine_sync, self.h)
+
+    def set_profiling(self, on=True):
+        _call(lib().nrg_engine_set_profiling, self.h, 1 if on else 0)
+
+    def kernel_times(self):
+        """{kernel: (ms, algorithmic flops, launches)} recorded since the last call."""
+        cap = 64
+        names = C.create_string_buffer(8192)
+        ms = (C.c_double * cap)()
+        work = (C.c_double * cap)()
+        cnt = (C.c_uint64 * cap)()
+        nk = C.c_int()
+        _call(lib().nrg_engine_kernel_times, self.h, names, C.c_uint64(8192), ms, work, cnt, cap,
+              C.byref(nk))
+        keys = names.value.decode().split("\n")[:nk.value]
+        return {k: (ms[i], work[i], cnt[i]) for i, k in enumerate(keys)}
 
     def broaden(self, energies, weights, omegas, b):
         e = np.ascontiguousarray(energies, float)

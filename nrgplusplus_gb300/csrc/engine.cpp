@@ -266,6 +266,45 @@ static void build_basis(RunStep &st) {
 
 static int round_up(int x, int m) { return (x + m - 1) / m * m; }
 
+static cudaEvent_t take_event(nrg_engine *e) {
+  if (!e->ev_pool.empty()) {
+    cudaEvent_t x = e->ev_pool.back();
+    e->ev_pool.pop_back();
+    return x;
+  }
+  cudaEvent_t x;
+  check_cuda(cudaEventCreate(&x), "event");
+  return x;
+}
+
+Prof::Prof(nrg_engine *eng, const char *nm, double w) : e(eng), name(nm), work(w) {
+  if (e->profile) {
+    a = take_event(e);
+    cudaEventRecord(a, e->stream);
+  }
+}
+Prof::~Prof() {
+  if (a) {
+    cudaEvent_t b = take_event(e);
+    cudaEventRecord(b, e->stream);
+    e->prof.push_back({name, a, b, work});
+  }
+}
+
+// algorithmic flops of a grouped GEMM: 2 M N K per contribution
+double gemm_flops(const std::vector<GemmGroup> &gs, const std::vector<GemmContrib> &cs) {
+  double f = 0;
+  for (auto &g : gs)
+    for (int c = g.c0; c < g.c1; ++c) f += 2.0 * g.M * g.N * double(cs[c].K);
+  return f;
+}
+
+static double eig_flops(const std::vector<EigBlock> &b) {
+  double f = 0;
+  for (auto &x : b) f += 10.0 / 3.0 * double(x.n) * x.n * x.n;
+  return f;
+}
+
 // One grouped-GEMM launch (k_gemm.cu) for a list of outputs.
 struct GemmList {
   std::vector<GemmGroup> groups;
@@ -293,6 +332,7 @@ struct GemmList {
     DevPtr d;
     char *p = a.push(e, d);
     hold.push_back(d);
+    Prof pf(e, "k_gemm_f64", gemm_flops(groups, contribs));
     launch_gemm_f64(at<GemmTile>(p, ot), int(tiles.size()), at<GemmGroup>(p, og),
                     at<GemmContrib>(p, oc), e->stream);
     count_launch(e);
@@ -363,9 +403,12 @@ static void mixed_eigensolve(nrg_engine *e, std::vector<DevBlock *> &blks, int m
   DevPtr dd;
   char *dp = a.push(e, dd);
   hold.push_back(dd);
-  launch_eig_f32(at<EigBlock>(dp, oeb), int(nb), max_n, e->eig_smem_f32, at<int>(dp, ost), s);
-  count_launch(e);
-  post_launch("eigensolve f32");
+  {
+    Prof pf(e, "k_eig_f32", eig_flops(eb));
+    launch_eig_f32(at<EigBlock>(dp, oeb), int(nb), max_n, e->eig_smem_f32, at<int>(dp, ost), s);
+    count_launch(e);
+    post_launch("eigensolve f32");
+  }
   int cur = 0;
   for (int step = 0; step <= kRefineSteps; ++step) {
     const bool final = (step == kRefineSteps);
@@ -391,14 +434,18 @@ static void mixed_eigensolve(nrg_engine *e, std::vector<DevBlock *> &blks, int m
     check_cuda(cudaMemcpyAsync(dp + orb, rb.data(), nb * sizeof(RefineBlock), cudaMemcpyHostToDevice, s),
                "refine descriptors");
     if (final) {
+      Prof pf(e, "k_oa_final");
       launch_oa_final(at<RefineBlock>(dp, orb), int(nb), max_n, kClusterTau, at<int>(dp, ost), s);
       count_launch(e);
       post_launch("refine final");
       break;
     }
-    launch_oa_update(at<RefineBlock>(dp, orb), int(nb), max_n, kClusterTau, s);
-    count_launch(e);
-    post_launch("refine update");
+    {
+      Prof pf(e, "k_oa_update");
+      launch_oa_update(at<RefineBlock>(dp, orb), int(nb), max_n, kClusterTau, s);
+      count_launch(e);
+      post_launch("refine update");
+    }
     // X' = X + X E
     check_cuda(cudaMemcpyAsync(X[1 - cur], X[cur], sz * 8, cudaMemcpyDeviceToDevice, s), "X copy");
     GemmList g3;
@@ -614,15 +661,19 @@ static void batch_add_site(nrg_run *const *runs, int nruns, const double *t, int
   hold.push_back(desc);
 
   check_cuda(cudaEventRecord(e->ev[0], s), "event");
-  launch_assemble(at<AsmBlock>(d, o_ablk), int(ablk.size()), chunks, at<AsmSub>(d, o_asub),
-                  at<int2>(d, o_apair), at<AsmTerm>(d, o_aterm), s);
-  count_launch(e);
-  post_launch("assemble");
+  {
+    Prof pf(e, "k_assemble");
+    launch_assemble(at<AsmBlock>(d, o_ablk), int(ablk.size()), chunks, at<AsmSub>(d, o_asub),
+                    at<int2>(d, o_apair), at<AsmTerm>(d, o_aterm), s);
+    count_launch(e);
+    post_launch("assemble");
+  }
   check_cuda(cudaEventRecord(e->ev[1], s), "event");
   if (max_n > eig_max_n_f64())
     fail(NRG_E_ARG, "block dimension " + std::to_string(max_n) + " exceeds the solver limit " +
                         std::to_string(eig_max_n_f64()));
   if (e->precision == NRG_PREC_FP64) {
+    Prof pf(e, "k_eig_f64", eig_flops(eblk_sorted));
     launch_eig_f64(at<EigBlock>(d, o_eblk), int(eblk_sorted.size()), max_n, e->eig_smem_f64,
                    at<int>(d, o_stat), s);
     count_launch(e);
@@ -637,10 +688,13 @@ static void batch_add_site(nrg_run *const *runs, int nruns, const double *t, int
     mixed_eigensolve(e, blks, max_n, hold);
   }
   check_cuda(cudaEventRecord(e->ev[2], s), "event");
-  launch_truncate(at<TruncRun>(d, o_trun), nruns, at<TruncBlock>(d, o_tblk), nblk_total,
-                  at<int>(d, o_elem), nelem_total, at<int>(d, o_kept), at<TruncResult>(d, o_tres), s);
-  count_launch(e, 2);
-  post_launch("truncate");
+  {
+    Prof pf(e, "k_truncate");
+    launch_truncate(at<TruncRun>(d, o_trun), nruns, at<TruncBlock>(d, o_tblk), nblk_total,
+                    at<int>(d, o_elem), nelem_total, at<int>(d, o_kept), at<TruncResult>(d, o_tres), s);
+    count_launch(e, 2);
+    post_launch("truncate");
+  }
   check_cuda(cudaEventRecord(e->ev[3], s), "event");
   // results back to the host: kept per block, run results, solver status,
   // sorted eigenvalues and per-block eigenvalues
@@ -756,6 +810,7 @@ static void batch_add_site(nrg_run *const *runs, int nruns, const double *t, int
     char *gp = ag.push(e, gd);
     hold.push_back(gd);
     check_cuda(cudaEventRecord(e->ev[4], s), "event");
+    Prof pf(e, "k_gemm_f64", gemm_flops(groups, contribs));
     launch_gemm_f64(at<GemmTile>(gp, o_t), int(tiles.size()), at<GemmGroup>(gp, o_g),
                     at<GemmContrib>(gp, o_c), s);
     count_launch(e);

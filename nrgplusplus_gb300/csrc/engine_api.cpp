@@ -17,6 +17,7 @@ void engine_batch_add_site(nrg_run *const *runs, int nruns, const double *t, int
                            const double *rescale);
 void engine_update_state(nrg_run *r);
 void engine_count_launch(nrg_engine *e, int n);
+double gemm_flops(const std::vector<GemmGroup> &gs, const std::vector<GemmContrib> &cs);
 
 constexpr int kFdmPts = 100000;                  // fdmSpectrum.hpp:351
 constexpr double kFdmMin = 1e-10, kFdmMax = 10;  // fdmSpectrum.hpp:352-353
@@ -81,6 +82,7 @@ struct GemmBatch {
     size_t ot = st.add(tiles), og = st.add(groups), oc = st.add(contribs);
     DevPtr hold;
     char *d = st.push(e, hold);
+    Prof pf(e, "k_gemm_f64", gemm_flops(groups, contribs));
     launch_gemm_f64(at<GemmTile>(d, ot), int(tiles.size()), at<GemmGroup>(d, og),
                     at<GemmContrib>(d, oc), e->stream);
     engine_count_launch(e, 1);
@@ -298,6 +300,7 @@ static void fdm_calc(nrg_fdm *f, double scale) {
     DevPtr hold;
     char *d = st.push(e, hold);
     double *hist = static_cast<double *>(f->hist->ptr);
+    Prof pf(e, "k_fdm_bin");
     launch_fdm_bin(at<FdmPair>(d, op), int(pairs.size()), chunk, scale, fdm_delE(), hist,
                    hist + int64_t(f->nops) * kFdmPts, kFdmPts, s);
     engine_count_launch(e, 1);
@@ -421,6 +424,49 @@ int nrg_engine_phase_times(nrg_engine *e, double *out, int cap, int *n) {
     int m = std::min(cap, 4);
     for (int i = 0; i < m; ++i) out[i] = ms[i];
     if (n) *n = m;
+  });
+}
+
+int nrg_engine_set_profiling(nrg_engine *e, int on) {
+  return guard([&] {
+    if (!e) fail(NRG_E_ARG, "null engine");
+    e->profile = on != 0;
+  });
+}
+
+int nrg_engine_kernel_times(nrg_engine *e, char *names, uint64_t names_cap, double *ms, double *work,
+                            uint64_t *count, int cap, int *nk) {
+  return guard([&] {
+    if (!e || !names || !ms || !work || !count || !nk) fail(NRG_E_ARG, "null argument");
+    check_cuda(cudaStreamSynchronize(e->stream), "profile sync");
+    std::vector<std::string> order;
+    std::map<std::string, std::tuple<double, double, uint64_t>> acc;
+    for (auto &p : e->prof) {
+      float t = 0;
+      cudaEventElapsedTime(&t, p.a, p.b);
+      if (!acc.count(p.name)) order.push_back(p.name);
+      auto &a = acc[p.name];
+      std::get<0>(a) += t;
+      std::get<1>(a) += p.work;
+      std::get<2>(a) += 1;
+      e->ev_pool.push_back(p.a);
+      e->ev_pool.push_back(p.b);
+    }
+    e->prof.clear();
+    std::string joined;
+    int k = 0;
+    for (auto &nm : order) {
+      if (k >= cap) break;
+      auto &a = acc[nm];
+      ms[k] = std::get<0>(a);
+      work[k] = std::get<1>(a);
+      count[k] = std::get<2>(a);
+      joined += nm + "\n";
+      ++k;
+    }
+    if (joined.size() + 1 > names_cap) fail(NRG_E_ARG, "names buffer too small");
+    std::memcpy(names, joined.c_str(), joined.size() + 1);
+    *nk = k;
   });
 }
 

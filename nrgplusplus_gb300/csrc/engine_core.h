@@ -109,7 +109,29 @@ struct nrg_engine {
   int *d_status = nullptr;
   size_t status_cap = 0;
   uint64_t fallback_blocks = 0;  // mixed path: blocks re-solved in FP64
+  // optional per-kernel event timing (nrg_engine_set_profiling)
+  bool profile = false;
+  struct ProfRec {
+    std::string name;
+    cudaEvent_t a, b;
+    double work;  // algorithmic flops of the launch
+  };
+  std::vector<ProfRec> prof;
+  std::vector<cudaEvent_t> ev_pool;
 };
+
+namespace nrg {
+// Records CUDA events around one kernel launch on the engine stream when
+// profiling is on; `work` is the launch's algorithmic flop count.
+struct Prof {
+  nrg_engine *e;
+  const char *name;
+  double work;
+  cudaEvent_t a = nullptr;
+  Prof(nrg_engine *eng, const char *nm, double w = 0.0);
+  ~Prof();
+};
+}  // namespace nrg
 
 struct nrg_run {
   nrg_engine *eng = nullptr;

@@ -190,6 +190,14 @@ int nrg_thermo_destroy(nrg_thermo *t);
 int nrg_thermo_calc(nrg_thermo *t, double energy_scale);        /* calcThermodynamics :42-89 */
 int nrg_thermo_final(nrg_thermo *t, double *entropy, double *specific_heat); /* :101-236 */
 
+/* ---- standalone batched symmetric eigensolver --------------------------- */
+/* The block solver behind qmatrix::diag (qmatrix.hpp:375-404, LAPACKE_dsyevd
+ * 'V','U'): nblk dense symmetric row-major blocks H (concatenated), dims[b]
+ * each; eigenvalues ascending into E (concatenated) and eigenvectors as
+ * columns into U (row-major, concatenated).  Uses the engine's precision mode. */
+int nrg_eigh_batched(nrg_engine *eng, int nblk, const int *dims, const double *H, double *E,
+                     double *U);
+
 /* ---- batched stepping of independent runs (one launch per phase) ------- */
 int nrg_batch_add_site(nrg_run *const *runs, int nruns, const double *t, int nt,
                        const double *rescale);

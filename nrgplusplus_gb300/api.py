@@ -67,6 +67,7 @@ EXPORTS = [
     "nrg_run_snapshot", "nrg_run_load_snapshot", "nrg_fdm_create", "nrg_fdm_destroy",
     "nrg_fdm_calc", "nrg_fdm_get", "nrg_broaden", "nrg_thermo_create", "nrg_thermo_destroy",
     "nrg_thermo_calc", "nrg_thermo_final", "nrg_batch_add_site", "nrg_batch_update_state",
+    "nrg_eigh_batched",
 ]
 
 
@@ -182,6 +183,22 @@ class Engine:
               C.byref(nk))
         keys = names.value.decode().split("\n")[:nk.value]
         return {k: (ms[i], work[i], cnt[i]) for i, k in enumerate(keys)}
+
+    def eigh_batched(self, mats):
+        """Eigen-decompose a list of dense symmetric blocks on the GPU
+        (qmatrix::diag semantics): [(eigenvalues ascending, eigenvectors as columns)]."""
+        dims = np.array([m.shape[0] for m in mats], dtype=np.int32)
+        H = np.ascontiguousarray(np.concatenate([np.ascontiguousarray(m, float).ravel() for m in mats]))
+        E = np.zeros(int(dims.sum()))
+        U = np.zeros(H.size)
+        _call(lib().nrg_eigh_batched, self.h, len(mats), _ip(dims), _dp(H), _dp(E), _dp(U))
+        out, eo, uo = [], 0, 0
+        for n in dims:
+            n = int(n)
+            out.append((E[eo:eo + n].copy(), U[uo:uo + n * n].reshape(n, n).copy()))
+            eo += n
+            uo += n * n
+        return out
 
     def broaden(self, energies, weights, omegas, b):
         e = np.ascontiguousarray(energies, float)

@@ -871,3 +871,87 @@ void engine_batch_add_site(nrg_run *const *runs, int nruns, const double *t, int
 void engine_update_state(nrg_run *r) { update_state(r); }
 void engine_count_launch(nrg_engine *e, int n) { count_launch(e, n); }
 }  // namespace nrg
+
+// ------------------------------------------------ standalone batched eigh
+extern "C" int nrg_eigh_batched(nrg_engine *e, int nblk, const int *dims, const double *H, double *E,
+                                double *U) {
+  using namespace nrg;
+  try {
+    if (!e || nblk < 0 || (nblk > 0 && (!dims || !H || !E || !U))) fail(NRG_E_ARG, "null argument");
+    cudaStream_t s = e->stream;
+    int64_t hsz = 0, esz = 0, hin = 0;
+    int max_n = 0;
+    std::vector<DevBlock> blocks(nblk);
+    for (int b = 0; b < nblk; ++b) {
+      if (dims[b] <= 0) fail(NRG_E_ARG, "block dimension must be positive");
+      blocks[b].n = dims[b];
+      blocks[b].ld = round_up(dims[b], 2);
+      hsz += int64_t(blocks[b].n) * blocks[b].ld;
+      hin += int64_t(dims[b]) * dims[b];
+      esz += dims[b];
+      max_n = std::max(max_n, dims[b]);
+    }
+    if (nblk == 0) return NRG_OK;
+    if (max_n > eig_max_n_f64()) fail(NRG_E_ARG, "block dimension exceeds the solver limit");
+    std::vector<DevPtr> hold;
+    DevPtr mh = dalloc(e, hsz * 8), mu = dalloc(e, hsz * 8), me = dalloc(e, esz * 8 + 8);
+    int64_t ho = 0, eo = 0, io = 0;
+    for (auto &b : blocks) {
+      b.H = static_cast<double *>(mh->ptr) + ho;
+      b.U = static_cast<double *>(mu->ptr) + ho;
+      b.E = static_cast<double *>(me->ptr) + eo;
+      check_cuda(cudaMemcpy2DAsync(b.H, b.ld * 8, H + io, b.n * 8, b.n * 8, b.n, cudaMemcpyHostToDevice, s),
+                 "H upload");
+      ho += int64_t(b.n) * b.ld;
+      eo += b.n;
+      io += int64_t(b.n) * b.n;
+    }
+    if (e->precision == NRG_PREC_FP64) {
+      std::vector<EigBlock> eb(nblk);
+      for (int b = 0; b < nblk; ++b) {
+        eb[b] = EigBlock{};
+        eb[b].H = blocks[b].H;
+        eb[b].U = blocks[b].U;
+        eb[b].E = blocks[b].E;
+        eb[b].n = blocks[b].n;
+        eb[b].ld = blocks[b].ld;
+        eb[b].ldu = blocks[b].ld;
+      }
+      std::vector<int> st(nblk + 1, 0);
+      Arena a;
+      size_t o1 = a.add(eb), o2 = a.add(st);
+      DevPtr dd;
+      char *dp = a.push(e, dd);
+      {
+        Prof pf(e, "k_eig_f64", eig_flops(eb));
+        launch_eig_f64(at<EigBlock>(dp, o1), nblk, max_n, e->eig_smem_f64, at<int>(dp, o2), s);
+        count_launch(e);
+        post_launch("eigh f64");
+      }
+      check_cuda(cudaMemcpyAsync(st.data(), dp + o2, nblk * sizeof(int), cudaMemcpyDeviceToHost, s), "status");
+      check_cuda(cudaStreamSynchronize(s), "eigh");
+      for (int b = 0; b < nblk; ++b)
+        if (st[b]) fail(NRG_E_EIG, "block eigensolver did not converge");
+    } else {
+      if (max_n > refine_max_n()) fail(NRG_E_ARG, "block dimension exceeds the refinement limit");
+      std::vector<DevBlock *> ptrs;
+      for (auto &b : blocks) ptrs.push_back(&b);
+      std::stable_sort(ptrs.begin(), ptrs.end(), [](DevBlock *x, DevBlock *y) { return x->n > y->n; });
+      mixed_eigensolve(e, ptrs, max_n, hold);
+    }
+    eo = 0;
+    io = 0;
+    for (auto &b : blocks) {
+      check_cuda(cudaMemcpy2DAsync(U + io, b.n * 8, b.U, b.ld * 8, b.n * 8, b.n, cudaMemcpyDeviceToHost, s),
+                 "U download");
+      check_cuda(cudaMemcpyAsync(E + eo, b.E, b.n * 8, cudaMemcpyDeviceToHost, s), "E download");
+      eo += b.n;
+      io += int64_t(b.n) * b.n;
+    }
+    check_cuda(cudaStreamSynchronize(s), "eigh");
+    return NRG_OK;
+  } catch (const Error &x) {
+    g_err = x.msg;
+    return x.code;
+  }
+}

@@ -35,6 +35,26 @@ __device__ __forceinline__ float thypot(float a, float b) { return hypotf(a, b);
 __device__ __forceinline__ double tsqrt(double a) { return sqrt(a); }
 __device__ __forceinline__ float tsqrt(float a) { return sqrtf(a); }
 
+// Givens pair of the QL chain: r = hypot(f, g), s = f / r, c = g / r.
+// FP64 keeps IEEE hypot and division; the FP32 first stage of the mixed path
+// uses one reciprocal square root (its result is refined in FP64 anyway).
+__device__ __forceinline__ double givens(double f, double g, double &s, double &c) {
+  const double r = hypot(f, g);
+  if (r != 0.0) {
+    s = f / r;
+    c = g / r;
+  }
+  return r;
+}
+__device__ __forceinline__ float givens(float f, float g, float &s, float &c) {
+  const float r2 = fmaf(f, f, g * g);
+  if (r2 == 0.f) return 0.f;
+  const float ri = rsqrtf(r2);
+  s = f * ri;
+  c = g * ri;
+  return r2 * ri;
+}
+
 template <typename T> __device__ __forceinline__ T warp_sum(T v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -157,6 +177,17 @@ __device__ void solve_block(T *a, int lda, int n, T *d, T *e, T *u, T *p, T *red
     __syncthreads();
   }
   // ---------------- 3. implicit QL on (d, e)
+  // Q is transposed in place first, so that the Givens rotations of the QL
+  // sweeps act on contiguous rows (coalesced / bank-conflict free); the
+  // eigenvectors end up as rows of the working matrix.
+  for (int64_t idx = tid; idx < int64_t(n) * n; idx += kThreads) {
+    const int r = int(idx / n), c = int(idx - int64_t(r) * n);
+    if (r < c) {
+      const T x = A(r, c);
+      A(r, c) = A(c, r);
+      A(c, r) = x;
+    }
+  }
   if (tid == 0) {
     for (int i = 1; i < n; ++i) e[i - 1] = e[i];
     e[n - 1] = T(0);
@@ -188,14 +219,16 @@ __device__ void solve_block(T *a, int lda, int n, T *d, T *e, T *u, T *p, T *red
             for (i = m - 1; i >= l; --i) {
               T f = s * e[i];
               T b = c * e[i];
-              e[i + 1] = (r = thypot(f, g));
+              T sn_new, cs_new;
+              r = givens(f, g, sn_new, cs_new);
+              e[i + 1] = r;
               if (r == T(0)) {
                 d[i + 1] -= pp;
                 e[m] = T(0);
                 break;
               }
-              s = f / r;
-              c = g / r;
+              s = sn_new;
+              c = cs_new;
               g = d[i + 1] - pp;
               r = (d[i] - g) * s + T(2) * c * b;
               d[i + 1] = g + (pp = s * r);
@@ -216,15 +249,16 @@ __device__ void solve_block(T *a, int lda, int n, T *d, T *e, T *u, T *p, T *red
       const int done = ctl->done, m = ctl->m, istop = ctl->istop;
       __syncthreads();  // everyone has read ctl before thread 0 rewrites it
       if (done) break;
-      // apply rotations i = m-1 .. istop+1 to every row of Q
+      // apply rotations i = m-1 .. istop+1 to rows i, i+1 of Q^T; thread k
+      // owns column k and carries the running row value in a register
       for (int k = tid; k < n; k += kThreads) {
-        T f = A(k, m);
+        T f = A(m, k);
         for (int i = m - 1; i > istop; --i) {
-          const T zi = A(k, i);
-          A(k, i + 1) = sn[i] * zi + cs[i] * f;
+          const T zi = A(i, k);
+          A(i + 1, k) = sn[i] * zi + cs[i] * f;
           f = cs[i] * zi - sn[i] * f;
         }
-        A(k, istop + 1) = f;
+        A(istop + 1, k) = f;
       }
       __syncthreads();
     }
@@ -248,9 +282,10 @@ __device__ void write_sorted(const T *a, int lda, int n, const T *d, int *rank, 
     E[r] = double(x);
   }
   __syncthreads();
+  // eigenvector `vec` is row `vec` of the working matrix
   for (int64_t idx = threadIdx.x; idx < int64_t(n) * n; idx += kThreads) {
-    const int row = int(idx / n), col = int(idx - int64_t(row) * n);
-    U[int64_t(row) * ldu + rank[col]] = double(a[int64_t(row) * lda + col]);
+    const int vec = int(idx / n), row = int(idx - int64_t(vec) * n);
+    U[int64_t(row) * ldu + rank[vec]] = double(a[int64_t(vec) * lda + row]);
   }
 }
 

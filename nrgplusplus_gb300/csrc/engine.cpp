@@ -366,48 +366,60 @@ static void mixed_eigensolve(nrg_engine *e, std::vector<DevBlock *> &blks, int m
   cudaStream_t s = e->stream;
   const size_t nb = blks.size();
   if (nb == 0) return;
-  int64_t sz = 0, wsz = 0, esz = 0;
-  std::vector<int64_t> off(nb), woff(nb, -1), eoff(nb);
+  int64_t sz = 0, esz = 0;
+  std::vector<int64_t> off(nb), eoff(nb);
   for (size_t b = 0; b < nb; ++b) {
     off[b] = sz;
     sz += int64_t(blks[b]->n) * blks[b]->ld;
     eoff[b] = esz;
     esz += blks[b]->n;
-    if (blks[b]->n > e->eig_smem_f32) {
-      woff[b] = wsz;
-      wsz += int64_t(blks[b]->n) * blks[b]->ld;
-    }
   }
   DevPtr mx0 = dalloc(e, sz * 8), mx1 = dalloc(e, sz * 8), my = dalloc(e, sz * 8),
          ms = dalloc(e, sz * 8), mg = dalloc(e, sz * 8), me2 = dalloc(e, sz * 8),
-         mw = dalloc(e, wsz * 4 + 16), mlam = dalloc(e, esz * 8 + 8);
+         mw = dalloc(e, 3 * sz * 4 + 16), mlam = dalloc(e, esz * 8 + 8);
   hold.insert(hold.end(), {mx0, mx1, my, ms, mg, me2, mw, mlam});
   auto P = [](DevPtr &m, int64_t o) { return static_cast<double *>(m->ptr) + o; };
   double *X[2] = {P(mx0, 0), P(mx1, 0)};
+  float *wbase = static_cast<float *>(mw->ptr);
   // FP32 solve: eigenvectors (as FP64) into X0
   std::vector<EigBlock> eb(nb);
+  std::vector<int4> bt_tiles;
   for (size_t b = 0; b < nb; ++b) {
+    eb[b] = EigBlock{};
     eb[b].H = blks[b]->H;
     eb[b].U = X[0] + off[b];
     eb[b].E = P(mlam, eoff[b]);
-    eb[b].W = woff[b] >= 0 ? static_cast<float *>(mw->ptr) + woff[b] : nullptr;
+    eb[b].W = wbase + off[b];
+    eb[b].V = wbase + sz + off[b];
+    eb[b].Bt = wbase + 2 * sz + off[b];
     eb[b].n = blks[b]->n;
     eb[b].ld = blks[b]->ld;
     eb[b].ldu = blks[b]->ld;
+    const int nt = (blks[b]->n + 63) / 64;
+    for (int tm = 0; tm < nt; ++tm)
+      for (int tn = 0; tn < nt; ++tn) bt_tiles.push_back(make_int4(int(b), tm, tn, 0));
   }
   std::vector<int> stat(nb + 1, 0);
   std::vector<RefineBlock> rb(nb);
   Arena a;
-  size_t oeb = a.add(eb), ost = a.add(stat);
+  size_t oeb = a.add(eb), ost = a.add(stat), obt = a.add(bt_tiles);
   const size_t orb = a.add(rb);  // filled per step below (host copy re-uploaded)
   DevPtr dd;
   char *dp = a.push(e, dd);
   hold.push_back(dd);
   {
-    Prof pf(e, "k_eig_f32", eig_flops(eb));
-    launch_eig_f32(at<EigBlock>(dp, oeb), int(nb), max_n, e->eig_smem_f32, at<int>(dp, ost), s);
+    Prof pf(e, "k_eig_bi_f32", eig_flops(eb) * 0.4);  // tridiagonal reduction + Q: 4/3 n^3
+    launch_eig_bisect_f32(at<EigBlock>(dp, oeb), int(nb), max_n, e->eig_smem_f32, s);
     count_launch(e);
     post_launch("eigensolve f32");
+  }
+  {
+    double f = 0;
+    for (auto &x : eb) f += 2.0 * double(x.n) * x.n * x.n;
+    Prof pf(e, "k_backtransform", f);
+    launch_backtransform(at<EigBlock>(dp, oeb), at<int4>(dp, obt), int(bt_tiles.size()), s);
+    count_launch(e);
+    post_launch("backtransform");
   }
   int cur = 0;
   for (int step = 0; step <= kRefineSteps; ++step) {

@@ -81,10 +81,12 @@ struct Ctl {
   int m, istop, done, err;
 };
 
-// Core solver on matrix a (n x n, leading dimension lda, either memory space).
-// d, e, u, p: shared arrays of n; cs/sn alias u/p during the QL stage.
+// Householder reduction of a (n x n, leading dimension lda, either memory
+// space) to tridiagonal form and accumulation of the orthogonal transform:
+// on return a = Q, d = diagonal, e[i] = coupling of i-1 and i (e[0] = 0).
+// d, e, u, p: shared arrays of n.
 template <typename T>
-__device__ void solve_block(T *a, int lda, int n, T *d, T *e, T *u, T *p, T *red, Ctl *ctl) {
+__device__ void tred2_acc(T *a, int lda, int n, T *d, T *e, T *u, T *p, T *red) {
   const int tid = threadIdx.x;
   const int warp = tid >> 5, lane = tid & 31;
 #define A(i, j) a[int64_t(i) * lda + (j)]
@@ -176,6 +178,15 @@ __device__ void solve_block(T *a, int lda, int n, T *d, T *e, T *u, T *p, T *red
     }
     __syncthreads();
   }
+#undef A
+}
+
+// Implicit QL with Wilkinson shifts on (d, e) with the eigenvectors
+// accumulated into a (= Q on entry); cs/sn alias u/p.
+template <typename T>
+__device__ void ql_vectors(T *a, int lda, int n, T *d, T *e, T *u, T *p, Ctl *ctl) {
+  const int tid = threadIdx.x;
+#define A(i, j) a[int64_t(i) * lda + (j)]
   // ---------------- 3. implicit QL on (d, e)
   // Q is transposed in place first, so that the Givens rotations of the QL
   // sweeps act on contiguous rows (coalesced / bank-conflict free); the
@@ -339,13 +350,250 @@ k_eig(const EigBlock *__restrict__ blocks, int max_n_smem, int *status) {
     }
   }
   __syncthreads();
-  solve_block<T>(a, lda, n, d, e, u, p, red, ctl);
+  tred2_acc<T>(a, lda, n, d, e, u, p, red);
+  ql_vectors<T>(a, lda, n, d, e, u, p, ctl);
   __syncthreads();
   if (ctl->err) {
     if (threadIdx.x == 0) status[blockIdx.x] = 1;
     return;
   }
   write_sorted<T>(a, lda, n, d, rank, B.E, B.U, B.ldu);
+}
+
+// ------------------------------------------------------------------------
+// FP32 first stage of the mixed path: Householder (tred2_acc) as above, then
+// the tridiagonal problem without the sequential QL chain:
+//   * Sturm-sequence bisection, one thread per eigenvalue (all in parallel);
+//   * inverse iteration, one thread per eigenvector (tridiagonal LU solve,
+//     vectors stored column-wise so every step is a coalesced row access);
+//   * near-degenerate clusters (gaps <= 1e-3 |T|) redone one warp per
+//     cluster, re-orthogonalising each new iterate against the cluster's
+//     earlier vectors (the classic inverse-iteration/Gram-Schmidt scheme);
+//   * the back-transform X = Q V is a separate tiled kernel (k_backtransform).
+// Accuracy is FP32 (~1e-6); the FP64-accurate refinement follows.
+
+constexpr float kClusterGap = 1e-3f;
+constexpr int kInvIter = 3;
+
+__device__ __forceinline__ float block_minf(float v, float *red) {
+  for (int o = 16; o > 0; o >>= 1) v = fminf(v, __shfl_xor_sync(0xffffffffu, v, o));
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  float m = red[0];
+  for (int w = 1; w < kWarps; ++w) m = fminf(m, red[w]);
+  __syncthreads();
+  return m;
+}
+
+// number of eigenvalues of the tridiagonal (d, e) below x
+__device__ __forceinline__ int sturm_count(const float *d, const float *e, int n, float x) {
+  float q = d[0] - x;
+  int cnt = q < 0.f;
+  for (int i = 1; i < n; ++i) {
+    if (fabsf(q) < 1e-30f) q = -1e-30f;
+    q = (d[i] - x) - e[i] * e[i] / q;
+    cnt += q < 0.f;
+  }
+  return cnt;
+}
+
+// One inverse-iteration solve (T - lam I) x = s * v for column j of V (in
+// place), with the LU pivots in column j of Bt.  Pivots smaller than pivmin
+// are replaced by +-pivmin; growth beyond 1e15 is rescaled on the fly (the
+// vector's scale is irrelevant).  Returns 1 / ||x||.
+__device__ float inv_solve(const float *d, const float *e, int n, float lam, float pivmin, float s,
+                           float *V, float *Bt, int ld, int j) {
+  float beta = d[0] - lam;
+  if (fabsf(beta) < pivmin) beta = copysignf(pivmin, beta);
+  float fb = s;  // scale applied to the remaining right-hand side entries
+  float y = V[j] * fb;
+  Bt[j] = beta;
+  V[j] = y;
+  for (int i = 1; i < n; ++i) {
+    const float m = e[i] / beta;
+    beta = (d[i] - lam) - m * e[i];
+    if (fabsf(beta) < pivmin) beta = copysignf(pivmin, beta);
+    y = V[int64_t(i) * ld + j] * fb - m * y;
+    if (fabsf(y) > 1e15f) {
+      for (int k = 0; k < i; ++k) V[int64_t(k) * ld + j] *= 1e-15f;
+      y *= 1e-15f;
+      fb *= 1e-15f;
+    }
+    Bt[int64_t(i) * ld + j] = beta;
+    V[int64_t(i) * ld + j] = y;
+  }
+  float x = y / beta;
+  V[int64_t(n - 1) * ld + j] = x;
+  float nrm = x * x;
+  for (int i = n - 2; i >= 0; --i) {
+    float xi = (V[int64_t(i) * ld + j] - e[i + 1] * x) / Bt[int64_t(i) * ld + j];
+    if (fabsf(xi) > 1e15f) {
+      for (int k = i + 1; k < n; ++k) V[int64_t(k) * ld + j] *= 1e-15f;
+      xi *= 1e-15f;
+      nrm *= 1e-30f;
+    }
+    V[int64_t(i) * ld + j] = xi;
+    nrm += xi * xi;
+    x = xi;
+  }
+  return rsqrtf(fmaxf(nrm, 1e-37f));
+}
+
+__global__ void __launch_bounds__(kThreads, 1)
+k_eig_bi(const EigBlock *__restrict__ blocks, int max_n_smem) {
+  extern __shared__ __align__(16) char smem[];
+  const EigBlock B = blocks[blockIdx.x];
+  const int n = B.n;
+  if (n == 0) return;
+  const bool in_smem = (n <= max_n_smem);
+  float *amat, *d, *e, *u, *p, *red;
+  int *rank;
+  Ctl *ctl;
+  carve<float>(smem, n, in_smem, amat, d, e, u, p, red, rank, ctl);
+  float *a = in_smem ? amat : B.W;
+  const int lda = in_smem ? n + 1 : B.ld;
+  for (int64_t idx = threadIdx.x; idx < int64_t(n) * n; idx += kThreads) {
+    const int r = int(idx / n), c = int(idx - int64_t(r) * n);
+    a[int64_t(r) * lda + c] = float(B.H[int64_t(r) * B.ld + c]);
+  }
+  __syncthreads();
+  tred2_acc<float>(a, lda, n, d, e, u, p, red);
+  if (in_smem) {  // Q out to its global buffer for the back-transform
+    for (int64_t idx = threadIdx.x; idx < int64_t(n) * n; idx += kThreads) {
+      const int r = int(idx / n), c = int(idx - int64_t(r) * n);
+      B.W[int64_t(r) * B.ld + c] = a[int64_t(r) * lda + c];
+    }
+  }
+  // Gershgorin interval and the norm used for pivots and cluster gaps
+  float lo = 3e38f, hi = -3e38f, tn = 0.f;
+  for (int i = threadIdx.x; i < n; i += kThreads) {
+    const float r = fabsf(e[i]) + (i + 1 < n ? fabsf(e[i + 1]) : 0.f);
+    lo = fminf(lo, d[i] - r);
+    hi = fmaxf(hi, d[i] + r);
+    tn = fmaxf(tn, fabsf(d[i]) + r);
+  }
+  lo = block_minf(lo, red);
+  hi = -block_minf(-hi, red);
+  tn = -block_minf(-tn, red);
+  const float span = fmaxf(hi - lo, 1e-30f);
+  lo -= 1e-6f * span;
+  hi += 1e-6f * span;
+  float *lam = u;                           // eigenvalues, ascending
+  int *cl = reinterpret_cast<int *>(p);     // cluster [start, end) pairs
+  for (int j = threadIdx.x; j < n; j += kThreads) {
+    float a0 = lo, b0 = hi;
+    for (int it = 0; it < 80; ++it) {
+      const float mid = 0.5f * (a0 + b0);
+      if (mid <= a0 || mid >= b0) break;
+      if (sturm_count(d, e, n, mid) > j) b0 = mid; else a0 = mid;
+    }
+    lam[j] = 0.5f * (a0 + b0);
+  }
+  __syncthreads();
+  const float pivmin = fmaxf(tn, 1e-30f) * 1.2e-7f;
+  // inverse iteration for every eigenvalue in parallel
+  for (int j = threadIdx.x; j < n; j += kThreads) {
+    for (int i = 0; i < n; ++i)
+      B.V[int64_t(i) * B.ld + j] = 1.0f + 0.25f * float((i * 7919 + j * 104729) % 97) / 97.f;
+    float s = 1.f;
+    for (int it = 0; it < kInvIter; ++it) s = inv_solve(d, e, n, lam[j], pivmin, s, B.V, B.Bt, B.ld, j);
+    for (int i = 0; i < n; ++i) B.V[int64_t(i) * B.ld + j] *= s;
+  }
+  // clusters of near-degenerate eigenvalues
+  if (threadIdx.x == 0) {
+    int c = 0, k = 0;
+    const float gap = kClusterGap * fmaxf(tn, 1e-30f);
+    while (k < n) {
+      int q = k + 1;
+      while (q < n && lam[q] - lam[q - 1] <= gap) ++q;
+      if (q - k > 1) {
+        cl[2 * c] = k;
+        cl[2 * c + 1] = q;
+        ++c;
+      }
+      k = q;
+    }
+    ctl->m = c;
+  }
+  __syncthreads();
+  const int ncl = ctl->m;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int q = warp; q < ncl; q += kWarps) {
+    const int c0 = cl[2 * q], c1 = cl[2 * q + 1];
+    for (int j = c0; j < c1; ++j) {
+      for (int rep = 0; rep < 2; ++rep) {
+        if (lane == 0) inv_solve(d, e, n, lam[j], pivmin, 1.f, B.V, B.Bt, B.ld, j);
+        __syncwarp();
+        for (int k = c0; k < j; ++k) {
+          float dot = 0.f;
+          for (int i = lane; i < n; i += 32) dot += B.V[int64_t(i) * B.ld + k] * B.V[int64_t(i) * B.ld + j];
+          dot = warp_sum(dot);
+          for (int i = lane; i < n; i += 32) B.V[int64_t(i) * B.ld + j] -= dot * B.V[int64_t(i) * B.ld + k];
+          __syncwarp();
+        }
+        float nrm = 0.f;
+        for (int i = lane; i < n; i += 32) {
+          const float v = B.V[int64_t(i) * B.ld + j];
+          nrm += v * v;
+        }
+        nrm = warp_sum(nrm);
+        const float sc = rsqrtf(fmaxf(nrm, 1e-37f));
+        for (int i = lane; i < n; i += 32) B.V[int64_t(i) * B.ld + j] *= sc;
+        __syncwarp();
+      }
+    }
+  }
+  for (int j = threadIdx.x; j < n; j += kThreads) B.E[j] = double(lam[j]);
+}
+
+// X = Q V for every block (FP32 SIMT, 64 x 64 tiles, 4 x 4 per thread);
+// the result is written in FP64 as the first eigenvector estimate.
+__global__ void __launch_bounds__(256)
+k_backtransform(const EigBlock *__restrict__ blocks, const int4 *__restrict__ tiles) {
+  __shared__ float As[16][65];
+  __shared__ float Bs[16][65];
+  const int4 t = tiles[blockIdx.x];
+  const EigBlock B = blocks[t.x];
+  const int n = B.n, m0 = t.y * 64, n0 = t.z * 64;
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  float acc[4][4] = {};
+  for (int k0 = 0; k0 < n; k0 += 16) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int idx = threadIdx.x + q * 256;
+      const int kk = idx & 15, mm = idx >> 4;  // Q tile 64 x 16, k fastest
+      const int gm = m0 + mm, gk = k0 + kk;
+      As[kk][mm] = (gm < n && gk < n) ? B.W[int64_t(gm) * B.ld + gk] : 0.f;
+      const int nn = idx & 63, k2 = idx >> 6;  // V tile 16 x 64, n fastest
+      const int gn = n0 + nn, gk2 = k0 + k2;
+      Bs[k2][nn] = (gn < n && gk2 < n) ? B.V[int64_t(gk2) * B.ld + gn] : 0.f;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < 16; ++kk) {
+      float av[4], bv[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) av[i] = As[kk][ty + 16 * i];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) bv[j] = Bs[kk][tx + 16 * j];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(av[i], bv[j], acc[i][j]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int gm = m0 + ty + 16 * i;
+    if (gm >= n) continue;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int gn = n0 + tx + 16 * j;
+      if (gn < n) B.U[int64_t(gm) * B.ldu + gn] = double(acc[i][j]);
+    }
+  }
 }
 
 template <typename T> size_t smem_bytes(int n, bool in_smem) {
@@ -394,6 +642,25 @@ int eig_max_n_f32() { return max_block<float>(); }
 void launch_eig_f64(const EigBlock *blocks, int nblocks, int max_n, int max_n_smem, int *status,
                     cudaStream_t s) {
   launch<double>(blocks, nblocks, max_n, max_n_smem, status, s);
+}
+
+void launch_eig_bisect_f32(const EigBlock *blocks, int nblocks, int max_n, int max_n_smem,
+                           cudaStream_t s) {
+  if (nblocks == 0) return;
+  static bool configured = false;
+  if (!configured) {
+    cudaFuncSetAttribute(k_eig_bi, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
+    configured = true;
+  }
+  size_t bytes = smem_bytes<float>(max_n, max_n <= max_n_smem);
+  if (max_n > max_n_smem) bytes = std::max(bytes, smem_bytes<float>(max_n_smem, true));
+  if (bytes > size_t(kSmemBytes)) bytes = kSmemBytes;
+  k_eig_bi<<<nblocks, kThreads, bytes, s>>>(blocks, max_n_smem);
+}
+
+void launch_backtransform(const EigBlock *blocks, const int4 *tiles, int ntiles, cudaStream_t s) {
+  if (ntiles == 0) return;
+  k_backtransform<<<ntiles, 256, 0, s>>>(blocks, tiles);
 }
 void launch_eig_f32(const EigBlock *blocks, int nblocks, int max_n, int max_n_smem, int *status,
                     cudaStream_t s) {

@@ -46,9 +46,17 @@ struct EigBlock {
   double *H;          // input (destroyed when the block is solved in place)
   double *U;          // output eigenvectors as columns, row-major n x ldu
   double *E;          // output eigenvalues, ascending
-  float *W;           // FP32 workspace (n x ld) for the FP32 solver, or null
+  float *W;           // FP32 workspace (n x ld): working matrix, then Q
+  float *V, *Bt;      // FP32 tridiagonal eigenvectors and LU pivots (n x ld)
   int n, ld, ldu, pad;
 };
+// FP32 bisection + inverse-iteration solver (mixed path first stage): writes
+// E (FP64) and Q into W, tridiagonal eigenvectors into V; then
+// launch_backtransform writes U = Q V (FP64).  tiles: (block, tile row,
+// tile col, 0) of 64 x 64 output tiles.
+void launch_eig_bisect_f32(const EigBlock *blocks, int nblocks, int max_n, int max_n_smem,
+                           cudaStream_t s);
+void launch_backtransform(const EigBlock *blocks, const int4 *tiles, int ntiles, cudaStream_t s);
 // FP64 Householder tridiagonalisation + implicit QL, one CTA per block.
 // status[b] != 0 if block b hit the QL iteration cap.
 // max_n: largest block of the launch; blocks with n <= max_n_smem are solved

@@ -282,12 +282,15 @@ __device__ void ql_vectors(T *a, int lda, int n, T *d, T *e, T *u, T *p, Ctl *ct
 template <typename T>
 __device__ void write_sorted(const T *a, int lda, int n, const T *d, int *rank, double *E, double *U,
                              int ldu) {
+  // total order (NaN sorts last, ties by index) so rank is a permutation
   for (int i = threadIdx.x; i < n; i += kThreads) {
     const T x = d[i];
+    const T kx = (x == x) ? x : T(INFINITY);
     int r = 0;
     for (int j = 0; j < n; ++j) {
       const T y = d[j];
-      r += (y < x) || (y == x && j < i);
+      const T ky = (y == y) ? y : T(INFINITY);
+      r += (ky < kx) || (ky == kx && j < i);
     }
     rank[i] = r;
     E[r] = double(x);
@@ -415,23 +418,28 @@ __device__ float inv_solve(const float *d, const float *e, int n, float lam, flo
     beta = (d[i] - lam) - m * e[i];
     if (fabsf(beta) < pivmin) beta = copysignf(pivmin, beta);
     y = V[int64_t(i) * ld + j] * fb - m * y;
-    if (fabsf(y) > 1e15f) {
-      for (int k = 0; k < i; ++k) V[int64_t(k) * ld + j] *= 1e-15f;
-      y *= 1e-15f;
-      fb *= 1e-15f;
+    if (fabsf(y) > 1e15f) {  // rescale the entries computed so far to ~1
+      const float sc = 1.f / fabsf(y);
+      for (int k = 0; k < i; ++k) V[int64_t(k) * ld + j] *= sc;
+      y *= sc;
+      fb *= sc;
     }
     Bt[int64_t(i) * ld + j] = beta;
     V[int64_t(i) * ld + j] = y;
   }
+  // pivots are >= pivmin >= 1e-20 and entries <= 1e15, so no quotient
+  // below overflows before it is rescaled
   float x = y / beta;
+  if (!(fabsf(x) <= 1e15f)) x = copysignf(1.f, x);  // first entry: any scale will do
   V[int64_t(n - 1) * ld + j] = x;
   float nrm = x * x;
   for (int i = n - 2; i >= 0; --i) {
     float xi = (V[int64_t(i) * ld + j] - e[i + 1] * x) / Bt[int64_t(i) * ld + j];
     if (fabsf(xi) > 1e15f) {
-      for (int k = i + 1; k < n; ++k) V[int64_t(k) * ld + j] *= 1e-15f;
-      xi *= 1e-15f;
-      nrm *= 1e-30f;
+      const float sc = 1.f / fabsf(xi);
+      for (int k = i + 1; k < n; ++k) V[int64_t(k) * ld + j] *= sc;
+      xi *= sc;
+      nrm *= sc * sc;
     }
     V[int64_t(i) * ld + j] = xi;
     nrm += xi * xi;
@@ -491,7 +499,7 @@ k_eig_bi(const EigBlock *__restrict__ blocks, int max_n_smem) {
     lam[j] = 0.5f * (a0 + b0);
   }
   __syncthreads();
-  const float pivmin = fmaxf(tn, 1e-30f) * 1.2e-7f;
+  const float pivmin = fmaxf(tn * 1.2e-7f, 1e-20f);
   // inverse iteration for every eigenvalue in parallel
   for (int j = threadIdx.x; j < n; j += kThreads) {
     for (int i = 0; i < n; ++i)

@@ -49,7 +49,7 @@ k_oa_update(const RefineBlock *__restrict__ blocks, double tau_rel) {
   for (int i = threadIdx.x; i < n; i += kThreads) {
     const double l = B.S[int64_t(i) * B.ld + i] / B.G[int64_t(i) * B.ld + i];
     lam[i] = l;
-    local = fmax(local, fabs(l));
+    if (isfinite(l)) local = fmax(local, fabs(l));
   }
   const double tau = tau_rel * fmax(1.0, block_max(local, red));
   for (int64_t idx = threadIdx.x; idx < int64_t(n) * n; idx += kThreads) {
@@ -83,13 +83,18 @@ k_oa_final(const RefineBlock *__restrict__ blocks, double tau_rel, int *status) 
   int *perm = reinterpret_cast<int *>(Qc + kMaxCluster * kMaxCluster);  // n
   int *cl = perm + n;                                 // up to n/2 + 1 cluster starts/ends
   int *order = cl + n + 2;                            // kMaxCluster
-  double local = 0.0;
+  double local = 0.0, bad = 0.0;
   for (int i = threadIdx.x; i < n; i += kThreads) {
     const double l = B.S[int64_t(i) * B.ld + i] / B.G[int64_t(i) * B.ld + i];
     lam[i] = l;
     local = fmax(local, fabs(l));
+    if (!isfinite(l)) bad = 1.0;
   }
   const double tau = tau_rel * fmax(1.0, block_max(local, red));
+  if (block_max(bad, red) > 0.0) {  // refinement broke down: re-solve in FP64
+    if (threadIdx.x == 0) status[blockIdx.x] = 2;
+    return;
+  }
   for (int i = threadIdx.x; i < n; i += kThreads) {
     const double x = lam[i];
     int r = 0;

@@ -352,6 +352,113 @@ static GemmContrib contrib(const double *A, int lda, const double *B, int ldb, i
   return c;
 }
 
+// Digit planes (k_ozaki.cu) of one FP64 array of square blocks.
+struct Planes {
+  DevPtr mem, exps;
+  std::vector<int64_t> poff;
+  std::vector<int> ldp;
+  int64_t pstride = 0;
+  OzOperand op(size_t b, int row0 = 0) const {
+    OzOperand o{};
+    o.p = static_cast<const __nv_bfloat16 *>(mem->ptr) + poff[b] + int64_t(row0) * ldp[b];
+    o.pstride = pstride;
+    o.ld = ldp[b];
+    o.exp = static_cast<const int *>(exps->ptr) + b;
+    return o;
+  }
+};
+
+static Planes make_planes(nrg_engine *e, const std::vector<int> &dims, std::vector<DevPtr> &hold) {
+  Planes p;
+  int64_t tot = 0;
+  for (int n : dims) {
+    p.poff.push_back(tot);
+    p.ldp.push_back(round_up(n, 8));
+    tot += int64_t(n) * round_up(n, 8);
+  }
+  p.pstride = tot;
+  p.mem = dalloc(e, tot * 8 * 2 + 16);
+  p.exps = dalloc(e, dims.size() * sizeof(int) + 16);
+  hold.push_back(p.mem);
+  hold.push_back(p.exps);
+  return p;
+}
+
+static void split_planes(nrg_engine *e, Planes &p, const std::vector<const double *> &src,
+                         const std::vector<int> &ld, std::vector<DevPtr> &hold) {
+  std::vector<SplitTask> t(src.size());
+  for (size_t b = 0; b < src.size(); ++b) {
+    t[b] = SplitTask{};
+    t[b].src = src[b];
+    const int64_t plane_elems = (b + 1 < p.poff.size() ? p.poff[b + 1] : p.pstride) - p.poff[b];
+    const int rows = int(plane_elems / p.ldp[b]);
+    t[b].rows = rows;
+    t[b].cols = rows;
+    t[b].ld = ld[b];
+    t[b].ldp = p.ldp[b];
+    t[b].planes = static_cast<__nv_bfloat16 *>(p.mem->ptr) + p.poff[b];
+    t[b].pstride = p.pstride;
+    t[b].exp = static_cast<int *>(p.exps->ptr) + b;
+  }
+  Arena a;
+  size_t o = a.add(t);
+  DevPtr d;
+  char *dp = a.push(e, d);
+  hold.push_back(d);
+  Prof pf(e, "k_split");
+  launch_split(at<SplitTask>(dp, o), int(t.size()), e->stream);
+  count_launch(e);
+  post_launch("split");
+}
+
+// One tensor-core (Ozaki) grouped-GEMM launch.
+struct OzList {
+  std::vector<OzGroup> groups;
+  std::vector<OzContrib> contribs;
+  std::vector<GemmTile> tiles;
+  double flops = 0;
+  void out(double *C, int ldc, int M, int N, bool acc, std::initializer_list<OzContrib> cs) {
+    OzGroup g{};
+    g.C = C;
+    g.ldc = ldc;
+    g.M = M;
+    g.N = N;
+    g.accumulate = acc ? 1 : 0;
+    g.c0 = int(contribs.size());
+    for (auto &c : cs) {
+      contribs.push_back(c);
+      flops += 2.0 * M * N * double(c.K);
+    }
+    g.c1 = int(contribs.size());
+    const int gi = int(groups.size());
+    groups.push_back(g);
+    for (int tm = 0; tm < (M + GEMM_TILE - 1) / GEMM_TILE; ++tm)
+      for (int tn = 0; tn < (N + GEMM_TILE - 1) / GEMM_TILE; ++tn) tiles.push_back({gi, tm, tn, 0});
+  }
+  void launch(nrg_engine *e, std::vector<DevPtr> &hold) {
+    if (tiles.empty()) return;
+    Arena a;
+    size_t ot = a.add(tiles), og = a.add(groups), oc = a.add(contribs);
+    DevPtr d;
+    char *p = a.push(e, d);
+    hold.push_back(d);
+    Prof pf(e, "k_gemm_oz", flops);
+    launch_gemm_oz(at<GemmTile>(p, ot), int(tiles.size()), at<OzGroup>(p, og), at<OzContrib>(p, oc), e->stream);
+    count_launch(e);
+    post_launch("ozaki gemm");
+  }
+};
+
+static OzContrib ozc(const OzOperand &A, const OzOperand &B, int K, int trans, double alpha = 1.0) {
+  OzContrib c{};
+  c.A = A;
+  c.B = B;
+  c.K = K;
+  c.trans = trans;
+  c.alpha = alpha;
+  return c;
+}
+
 constexpr int kRefineSteps = 3;
 constexpr double kClusterTau = 1e-4;  // relative gap below which levels form a cluster
 
@@ -422,15 +529,56 @@ static void mixed_eigensolve(nrg_engine *e, std::vector<DevBlock *> &blks, int m
     post_launch("backtransform");
   }
   int cur = 0;
+  // digit planes for the tensor-core GEMMs (H once, X / Y / E per step)
+  const bool oz = e->ozaki;
+  std::vector<int> dims(nb), lds(nb);
+  for (size_t b = 0; b < nb; ++b) {
+    dims[b] = blks[b]->n;
+    lds[b] = blks[b]->ld;
+  }
+  Planes pH, pX, pY, pE;
+  if (oz) {
+    pH = make_planes(e, dims, hold);
+    pX = make_planes(e, dims, hold);
+    pY = make_planes(e, dims, hold);
+    pE = make_planes(e, dims, hold);
+    std::vector<const double *> src(nb);
+    for (size_t b = 0; b < nb; ++b) src[b] = blks[b]->H;
+    split_planes(e, pH, src, lds, hold);
+  }
+  auto splitv = [&](Planes &pl, double *base) {
+    std::vector<const double *> src(nb);
+    for (size_t b = 0; b < nb; ++b) src[b] = base + off[b];
+    split_planes(e, pl, src, lds, hold);
+  };
   for (int step = 0; step <= kRefineSteps; ++step) {
     const bool final = (step == kRefineSteps);
+    if (oz) {
+      splitv(pX, X[cur]);
+      OzList y;
+      for (size_t b = 0; b < nb; ++b) {  // Y = H X
+        const int n = blks[b]->n;
+        y.out(P(my, off[b]), lds[b], n, n, false, {ozc(pH.op(b), pX.op(b), n, 0)});
+      }
+      y.launch(e, hold);
+      splitv(pY, P(my, 0));
+      OzList sg;
+      for (size_t b = 0; b < nb; ++b) {  // S = X^T Y, G = X^T X
+        const int n = blks[b]->n;
+        sg.out(P(ms, off[b]), lds[b], n, n, false, {ozc(pX.op(b), pY.op(b), n, 1)});
+        sg.out(P(mg, off[b]), lds[b], n, n, false, {ozc(pX.op(b), pX.op(b), n, 1)});
+      }
+      sg.launch(e, hold);
+    }
     GemmList g1, g2;
     for (size_t b = 0; b < nb; ++b) {
       const int n = blks[b]->n, ld = blks[b]->ld;
       double *x = X[cur] + off[b];
-      g1.out(P(my, off[b]), ld, n, n, false, {contrib(blks[b]->H, ld, x, ld, n, 0)});       // Y = H X
-      g2.out(P(ms, off[b]), ld, n, n, false, {contrib(x, ld, P(my, off[b]), ld, n, 1)});    // S = X^T Y
-      g2.out(P(mg, off[b]), ld, n, n, false, {contrib(x, ld, x, ld, n, 1)});                // G = X^T X
+      if (!oz) {
+        g1.out(P(my, off[b]), ld, n, n, false, {contrib(blks[b]->H, ld, x, ld, n, 0)});     // Y = H X
+        g2.out(P(ms, off[b]), ld, n, n, false, {contrib(x, ld, P(my, off[b]), ld, n, 1)});  // S = X^T Y
+        g2.out(P(mg, off[b]), ld, n, n, false, {contrib(x, ld, x, ld, n, 1)});              // G = X^T X
+      }
       rb[b].S = P(ms, off[b]);
       rb[b].G = P(mg, off[b]);
       rb[b].E2 = P(me2, off[b]);
@@ -460,12 +608,22 @@ static void mixed_eigensolve(nrg_engine *e, std::vector<DevBlock *> &blks, int m
     }
     // X' = X + X E
     check_cuda(cudaMemcpyAsync(X[1 - cur], X[cur], sz * 8, cudaMemcpyDeviceToDevice, s), "X copy");
-    GemmList g3;
-    for (size_t b = 0; b < nb; ++b) {
-      const int n = blks[b]->n, ld = blks[b]->ld;
-      g3.out(X[1 - cur] + off[b], ld, n, n, true, {contrib(X[cur] + off[b], ld, P(me2, off[b]), ld, n, 0)});
+    if (oz) {
+      splitv(pE, P(me2, 0));
+      OzList g3;
+      for (size_t b = 0; b < nb; ++b) {
+        const int n = blks[b]->n;
+        g3.out(X[1 - cur] + off[b], lds[b], n, n, true, {ozc(pX.op(b), pE.op(b), n, 0)});
+      }
+      g3.launch(e, hold);
+    } else {
+      GemmList g3;
+      for (size_t b = 0; b < nb; ++b) {
+        const int n = blks[b]->n, ld = blks[b]->ld;
+        g3.out(X[1 - cur] + off[b], ld, n, n, true, {contrib(X[cur] + off[b], ld, P(me2, off[b]), ld, n, 0)});
+      }
+      g3.launch(e, hold);
     }
-    g3.launch(e, hold);
     cur = 1 - cur;
   }
   check_cuda(cudaMemcpyAsync(stat.data(), dp + ost, nb * sizeof(int), cudaMemcpyDeviceToHost, s),

@@ -3,6 +3,7 @@
 // the FDM spectral pass (fdmSpectrum) and thermodynamics (fdmThermodynamics).
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <numeric>
 
@@ -398,6 +399,7 @@ int nrg_engine_create(const nrg_engine_opts *opts, nrg_engine **out) {
     for (auto &ev : e->ev) check_cuda(cudaEventCreate(&ev), "event");
     e->eig_smem_f64 = eig_smem_limit_f64();
     e->eig_smem_f32 = eig_smem_limit_f32();
+    if (const char *oz = std::getenv("NRG_OZAKI")) e->ozaki = std::atoi(oz) != 0;
     *out = e;
   });
 }

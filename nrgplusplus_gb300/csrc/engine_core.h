@@ -109,6 +109,7 @@ struct nrg_engine {
   int *d_status = nullptr;
   size_t status_cap = 0;
   uint64_t fallback_blocks = 0;  // mixed path: blocks re-solved in FP64
+  bool ozaki = true;             // mixed path: FP64-accurate GEMMs on tensor cores
   // optional per-kernel event timing (nrg_engine_set_profiling)
   bool profile = false;
   struct ProfRec {

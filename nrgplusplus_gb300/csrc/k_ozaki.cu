@@ -1,0 +1,239 @@
+// FP64-accurate GEMM on the tensor cores (Ozaki-type digit splitting).
+//
+// Every FP64 operand block is split once (k_split) into 8 bf16 "digit planes":
+// with e = ilogb(max|x|) + 1 over the block, X = rint(x * 2^(55-e)) is an
+// integer with |X| <= 2^55, written in balanced base 128 as
+//     X = sum_p a_p 128^(7-p),   a_p integer in [-64, 64]
+// so x = 2^(e-55) sum_p a_p 128^(7-p) to within 2^(e-56).  Each a_p is exact
+// in bf16.  A product then is
+//     A B = 2^(eA+eB-110) sum_{p,q} 128^(14-p-q) (a_p b_q)
+// The digit products are exact in FP32 (|a_p b_q| <= 2^12) and so are their
+// sums while |sum| <= 2^24: grouping the pairs by d = p + q (d <= 7; the
+// dropped groups weigh below 2^-51 of the result scale) and accumulating each
+// group over at most 512 k-terms keeps every partial sum an exact integer.
+// The 8 group sums are combined once per output element and K-chunk in FP64
+// by Horner (h = G_0; h = 128 h + G_d), so the FP64 pipe does 8 FMAs per
+// output element instead of K.  The bf16 products use mma.sync m16n8k16 with
+// FP32 accumulation; the result matches an FP64 GEMM to FP64 round-off.
+#include <cuda_bf16.h>
+
+#include "nrg_internal.h"
+
+namespace nrg {
+namespace {
+
+constexpr int kPlanes = 8;
+constexpr int kChunkK = 512;
+constexpr int BM = 64, BN = 64, BK = 32;
+constexpr int kThreads = 256;
+// shared-memory row pitches (bf16 elements): 80-byte and 144-byte rows make
+// the 8 row addresses of every ldmatrix fall in distinct 16-byte bank groups
+constexpr int kPitchK = BK + 8;   // tiles stored [m or n][k]
+constexpr int kPitchMN = BM + 8;  // tiles stored [k][m or n]
+constexpr int kTileElems = kPlanes * BM * kPitchK;  // >= kPlanes * BK * kPitchMN
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void ldsm_x4(uint32_t addr, uint32_t &r0, uint32_t &r1, uint32_t &r2, uint32_t &r3) {
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+               : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3) : "r"(addr));
+}
+__device__ __forceinline__ void ldsm_x4_t(uint32_t addr, uint32_t &r0, uint32_t &r1, uint32_t &r2, uint32_t &r3) {
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+               : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3) : "r"(addr));
+}
+__device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};\n"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// ---------------------------------------------------------------- split
+__global__ void __launch_bounds__(256) k_split(const SplitTask *__restrict__ tasks) {
+  __shared__ double red[8];
+  const SplitTask T = tasks[blockIdx.x];
+  const int64_t nel = int64_t(T.rows) * T.cols;
+  double m = 0.0;
+  for (int64_t i = threadIdx.x; i < nel; i += blockDim.x) {
+    const int r = int(i / T.cols), c = int(i - int64_t(r) * T.cols);
+    m = fmax(m, fabs(T.src[int64_t(r) * T.ld + c]));
+  }
+  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+  __syncthreads();
+  double mx = red[0];
+  for (int w = 1; w < int(blockDim.x >> 5); ++w) mx = fmax(mx, red[w]);
+  const int e = (mx > 0.0 && isfinite(mx)) ? ilogb(mx) + 1 : 0;
+  if (threadIdx.x == 0) *T.exp = e;
+  for (int64_t i = threadIdx.x; i < int64_t(T.rows) * T.ldp; i += blockDim.x) {
+    const int r = int(i / T.ldp), c = int(i - int64_t(r) * T.ldp);
+    long long X = 0;
+    if (c < T.cols) X = llrint(scalbn(T.src[int64_t(r) * T.ld + c], 55 - e));
+    // balanced base-128 digits, least significant first
+#pragma unroll
+    for (int p = kPlanes - 1; p >= 0; --p) {
+      const long long a = ((X + 64) & 127) - 64;
+      X = (X - a) >> 7;
+      static_cast<__nv_bfloat16 *>(T.planes)[int64_t(p) * T.pstride + i] = __float2bfloat16_rn(float(a));
+    }
+  }
+}
+
+// ----------------------------------------------------------------- GEMM
+struct Frag {
+  uint32_t a[kPlanes][4];
+};
+
+__global__ void __launch_bounds__(kThreads, 1)
+k_gemm_oz(const GemmTile *__restrict__ tiles, const OzGroup *__restrict__ groups,
+          const OzContrib *__restrict__ contribs) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __nv_bfloat16 *As = reinterpret_cast<__nv_bfloat16 *>(smem_raw);
+  __nv_bfloat16 *Bs = As + kTileElems;
+  double *Ct = reinterpret_cast<double *>(Bs + kTileElems);  // BM x BN FP64 totals
+  const GemmTile t = tiles[blockIdx.x];
+  const OzGroup g = groups[t.group];
+  const int m0 = t.tm * BM, n0 = t.tn * BN;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int wm = (warp & 3) * 16, wn = (warp >> 2) * 32;
+  for (int i = tid; i < BM * BN; i += kThreads) Ct[i] = 0.0;
+
+  for (int c = g.c0; c < g.c1; ++c) {
+    const OzContrib q = contribs[c];
+    const bool ta = q.trans & 1, tb = (q.trans >> 1) & 1;
+    const double scale = q.alpha * scalbn(1.0, *q.A.exp + *q.B.exp - 61);
+    for (int kc = 0; kc < q.K; kc += kChunkK) {
+      const int kend = min(q.K, kc + kChunkK);
+      float acc[kPlanes][4][4];
+#pragma unroll
+      for (int d = 0; d < kPlanes; ++d)
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+#pragma unroll
+          for (int v = 0; v < 4; ++v) acc[d][j][v] = 0.f;
+      for (int k0 = kc; k0 < kend; k0 += BK) {
+        __syncthreads();
+        // stage A: op(A)[m0..m0+63][k0..k0+31] for every plane
+        for (int idx = tid; idx < kPlanes * BM * BK; idx += kThreads) {
+          const int p = idx / (BM * BK), rem = idx - p * (BM * BK);
+          int mm, kk;
+          if (ta) { mm = rem & 63; kk = rem >> 6; } else { kk = rem & 31; mm = rem >> 5; }
+          const int gm = m0 + mm, gk = k0 + kk;
+          __nv_bfloat16 v = __float2bfloat16_rn(0.f);
+          if (gm < g.M && gk < kend)
+            v = ta ? q.A.p[int64_t(p) * q.A.pstride + int64_t(gk) * q.A.ld + gm]
+                   : q.A.p[int64_t(p) * q.A.pstride + int64_t(gm) * q.A.ld + gk];
+          if (ta) As[p * (BK * kPitchMN) + kk * kPitchMN + mm] = v;
+          else    As[p * (BM * kPitchK) + mm * kPitchK + kk] = v;
+        }
+        // stage B: op(B)[k0..k0+31][n0..n0+63]
+        for (int idx = tid; idx < kPlanes * BN * BK; idx += kThreads) {
+          const int p = idx / (BN * BK), rem = idx - p * (BN * BK);
+          int nn, kk;
+          if (tb) { kk = rem & 31; nn = rem >> 5; } else { nn = rem & 63; kk = rem >> 6; }
+          const int gn = n0 + nn, gk = k0 + kk;
+          __nv_bfloat16 v = __float2bfloat16_rn(0.f);
+          if (gn < g.N && gk < kend)
+            v = tb ? q.B.p[int64_t(p) * q.B.pstride + int64_t(gn) * q.B.ld + gk]
+                   : q.B.p[int64_t(p) * q.B.pstride + int64_t(gk) * q.B.ld + gn];
+          if (tb) Bs[p * (BN * kPitchK) + nn * kPitchK + kk] = v;
+          else    Bs[p * (BK * kPitchMN) + kk * kPitchMN + nn] = v;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int ks = 0; ks < BK; ks += 16) {
+          Frag fa;
+#pragma unroll
+          for (int p = 0; p < kPlanes; ++p) {
+            if (!ta) {
+              // As[m][k]: rows wm + (lane % 16), k ks + (lane / 16) * 8
+              const __nv_bfloat16 *ptr = As + p * (BM * kPitchK) + (wm + (lane & 15)) * kPitchK + ks + (lane >> 4) * 8;
+              ldsm_x4(smem_u32(ptr), fa.a[p][0], fa.a[p][1], fa.a[p][2], fa.a[p][3]);
+            } else {
+              // As[k][m]: matrix mi = lane / 8 covers k ks + (mi/2)*8, m wm + (mi%2)*8
+              const int mi = lane >> 3;
+              const __nv_bfloat16 *ptr = As + p * (BK * kPitchMN) + (ks + (mi >> 1) * 8 + (lane & 7)) * kPitchMN + wm + (mi & 1) * 8;
+              ldsm_x4_t(smem_u32(ptr), fa.a[p][0], fa.a[p][1], fa.a[p][2], fa.a[p][3]);
+            }
+          }
+#pragma unroll
+          for (int qd = 0; qd < kPlanes; ++qd) {
+            // B fragments of plane qd for the warp's 4 n8 tiles
+            uint32_t b[4][2];
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+              // two n8 tiles per ldmatrix.x4: matrices (n-tile 2h, k 0-7), (2h, k 8-15), (2h+1, 0-7), (2h+1, 8-15)
+              const int mi = lane >> 3;
+              const int ntile = 2 * h + (mi >> 1), khalf = mi & 1;
+              uint32_t r0, r1, r2, r3;
+              if (tb) {  // Bs[n][k]
+                const __nv_bfloat16 *ptr = Bs + qd * (BN * kPitchK) + (wn + ntile * 8 + (lane & 7)) * kPitchK + ks + khalf * 8;
+                ldsm_x4(smem_u32(ptr), r0, r1, r2, r3);
+              } else {   // Bs[k][n]
+                const __nv_bfloat16 *ptr = Bs + qd * (BK * kPitchMN) + (ks + khalf * 8 + (lane & 7)) * kPitchMN + wn + ntile * 8;
+                ldsm_x4_t(smem_u32(ptr), r0, r1, r2, r3);
+              }
+              b[2 * h][0] = r0;
+              b[2 * h][1] = r1;
+              b[2 * h + 1][0] = r2;
+              b[2 * h + 1][1] = r3;
+            }
+#pragma unroll
+            for (int p = 0; p < kPlanes; ++p) {
+              if (p + qd >= kPlanes) continue;
+#pragma unroll
+              for (int j = 0; j < 4; ++j) mma_bf16(acc[p + qd][j], fa.a[p], b[j][0], b[j][1]);
+            }
+          }
+        }
+      }
+      // exact group sums -> FP64 (Horner over the groups), into the tile totals
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+          double h = acc[0][j][v];
+#pragma unroll
+          for (int d = 1; d < kPlanes; ++d) h = fma(h, 128.0, double(acc[d][j][v]));
+          const int r = wm + (lane >> 2) + (v >> 1) * 8;
+          const int col = wn + j * 8 + (lane & 3) * 2 + (v & 1);
+          Ct[r * BN + col] += scale * h;
+        }
+    }
+  }
+  __syncthreads();
+  for (int i = tid; i < BM * BN; i += kThreads) {
+    const int r = i / BN, col = i - r * BN;
+    const int gm = m0 + r, gn = n0 + col;
+    if (gm < g.M && gn < g.N) {
+      double *cp = g.C + int64_t(gm) * g.ldc + gn;
+      *cp = g.accumulate ? (*cp + Ct[i]) : Ct[i];
+    }
+  }
+}
+
+constexpr size_t kGemmSmem = 2 * size_t(kTileElems) * sizeof(__nv_bfloat16) + BM * BN * sizeof(double);
+
+}  // namespace
+
+void launch_split(const SplitTask *tasks, int ntasks, cudaStream_t s) {
+  if (ntasks == 0) return;
+  k_split<<<ntasks, 256, 0, s>>>(tasks);
+}
+
+void launch_gemm_oz(const GemmTile *tiles, int ntiles, const OzGroup *groups, const OzContrib *contribs,
+                    cudaStream_t s) {
+  if (ntiles == 0) return;
+  static bool cfg = false;
+  if (!cfg) {
+    cudaFuncSetAttribute(k_gemm_oz, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kGemmSmem));
+    cfg = true;
+  }
+  k_gemm_oz<<<ntiles, kThreads, kGemmSmem, s>>>(tiles, groups, contribs);
+}
+
+}  // namespace nrg

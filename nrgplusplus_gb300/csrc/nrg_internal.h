@@ -3,6 +3,7 @@
 // blocks of many independent runs.
 #pragma once
 #include <cstdint>
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 namespace nrg {
@@ -106,6 +107,37 @@ struct GemmTile {
 void launch_gemm_f64(const GemmTile *tiles, int ntiles, const GemmGroup *groups,
                      const GemmContrib *contribs, cudaStream_t s);
 constexpr int GEMM_TILE = 64;
+
+// ------------------------------------- FP64-accurate tensor-core GEMM
+// Digit planes of one FP64 block (k_ozaki.cu): 8 bf16 planes, plane p at
+// planes + p * pstride, row r at + r * ldp; value = 2^(exp-55) *
+// sum_p plane_p * 128^(7-p).
+struct SplitTask {
+  const double *src;
+  int rows, cols, ld, ldp;
+  void *planes;        // __nv_bfloat16
+  int64_t pstride;
+  int *exp;            // written: block exponent
+};
+struct OzOperand {
+  const __nv_bfloat16 *p;  // plane 0 (already offset to the first row used)
+  int64_t pstride;
+  int ld, pad;
+  const int *exp;
+};
+struct OzContrib {
+  OzOperand A, B;
+  int K, trans;            // trans bit0: A stored K x M; bit1: B stored N x K
+  double alpha;
+};
+struct OzGroup {
+  double *C;
+  int ldc, M, N, accumulate;
+  int c0, c1;
+};
+void launch_split(const SplitTask *tasks, int ntasks, cudaStream_t s);
+void launch_gemm_oz(const GemmTile *tiles, int ntiles, const OzGroup *groups, const OzContrib *contribs,
+                    cudaStream_t s);
 
 // ------------------------------------------------------------- truncation
 struct TruncRun {

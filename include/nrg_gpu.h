@@ -198,6 +198,15 @@ int nrg_thermo_final(nrg_thermo *t, double *entropy, double *specific_heat); /* 
 int nrg_eigh_batched(nrg_engine *eng, int nblk, const int *dims, const double *H, double *E,
                      double *U);
 
+/* ---- FP64-accurate GEMM on the tensor cores ------------------------------ */
+/* C = alpha op(A) op(B) (+ C when beta == 1; beta must be 0 or 1), row-major
+ * host buffers; op(X) = X^T when trans is set.  The engine's building block
+ * behind the operator rotations of qmatrix::dot (qmatrix.hpp:351-374,
+ * cblas_dgemm): digit-split bf16 products with exact FP32 sums, combined in
+ * FP64, accurate to FP64 round-off. */
+int nrg_dgemm_tc(nrg_engine *eng, int transA, int transB, int M, int N, int K, double alpha,
+                 const double *A, int lda, const double *B, int ldb, double beta, double *C, int ldc);
+
 /* ---- batched stepping of independent runs (one launch per phase) ------- */
 int nrg_batch_add_site(nrg_run *const *runs, int nruns, const double *t, int nt,
                        const double *rescale);

@@ -67,7 +67,7 @@ EXPORTS = [
     "nrg_run_snapshot", "nrg_run_load_snapshot", "nrg_fdm_create", "nrg_fdm_destroy",
     "nrg_fdm_calc", "nrg_fdm_get", "nrg_broaden", "nrg_thermo_create", "nrg_thermo_destroy",
     "nrg_thermo_calc", "nrg_thermo_final", "nrg_batch_add_site", "nrg_batch_update_state",
-    "nrg_eigh_batched",
+    "nrg_eigh_batched", "nrg_dgemm_tc",
 ]
 
 
@@ -199,6 +199,18 @@ class Engine:
             eo += n
             uo += n * n
         return out
+
+    def dgemm_tc(self, A, B, transA=False, transB=False, alpha=1.0):
+        """FP64-accurate op(A) op(B) on the tensor cores."""
+        A = np.ascontiguousarray(A, float)
+        B = np.ascontiguousarray(B, float)
+        M = A.shape[1] if transA else A.shape[0]
+        K = A.shape[0] if transA else A.shape[1]
+        N = B.shape[0] if transB else B.shape[1]
+        C = np.zeros((M, N))
+        _call(lib().nrg_dgemm_tc, self.h, int(transA), int(transB), M, N, K, C.dtype.type(alpha),
+              _dp(A), A.shape[1], _dp(B), B.shape[1], C.dtype.type(0.0), _dp(C), N)
+        return C
 
     def broaden(self, energies, weights, omegas, b):
         e = np.ascontiguousarray(energies, float)

@@ -1125,3 +1125,55 @@ extern "C" int nrg_eigh_batched(nrg_engine *e, int nblk, const int *dims, const 
     return x.code;
   }
 }
+
+// ------------------------------------- FP64-accurate tensor-core GEMM ABI
+extern "C" int nrg_dgemm_tc(nrg_engine *e, int transA, int transB, int M, int N, int K, double alpha,
+                            const double *A, int lda, const double *B, int ldb, double beta, double *C,
+                            int ldc) {
+  using namespace nrg;
+  try {
+    if (!e || M < 0 || N < 0 || K < 0 || !A || !B || !C) fail(NRG_E_ARG, "bad argument");
+    if (M == 0 || N == 0) return NRG_OK;
+    if (beta != 0.0 && beta != 1.0) fail(NRG_E_ARG, "beta must be 0 or 1");
+    cudaStream_t s = e->stream;
+    std::vector<DevPtr> hold;
+    // stored shapes: A is (transA ? K x M : M x K), B is (transB ? N x K : K x N)
+    const int ar = transA ? K : M, ac = transA ? M : K, br = transB ? N : K, bc = transB ? K : N;
+    if (lda < ac || ldb < bc || ldc < N) fail(NRG_E_ARG, "leading dimension too small");
+    DevPtr da = dalloc(e, int64_t(ar) * ac * 8 + 8), db = dalloc(e, int64_t(br) * bc * 8 + 8),
+           dc = dalloc(e, int64_t(M) * N * 8 + 8);
+    check_cuda(cudaMemcpy2DAsync(da->ptr, ac * 8, A, lda * 8, ac * 8, ar, cudaMemcpyHostToDevice, s), "A");
+    check_cuda(cudaMemcpy2DAsync(db->ptr, bc * 8, B, ldb * 8, bc * 8, br, cudaMemcpyHostToDevice, s), "B");
+    if (beta != 0.0)
+      check_cuda(cudaMemcpy2DAsync(dc->ptr, N * 8, C, ldc * 8, N * 8, M, cudaMemcpyHostToDevice, s), "C");
+    const int lpa = round_up(ac, 8), lpb = round_up(bc, 8);
+    DevPtr pa = dalloc(e, int64_t(ar) * lpa * 8 * 2 + 16), pb = dalloc(e, int64_t(br) * lpb * 8 * 2 + 16),
+           ex = dalloc(e, 64);
+    std::vector<SplitTask> t(2);
+    t[0] = SplitTask{static_cast<double *>(da->ptr), ar, ac, ac, lpa, pa->ptr, int64_t(ar) * lpa,
+                     static_cast<int *>(ex->ptr)};
+    t[1] = SplitTask{static_cast<double *>(db->ptr), br, bc, bc, lpb, pb->ptr, int64_t(br) * lpb,
+                     static_cast<int *>(ex->ptr) + 1};
+    Arena a;
+    size_t o = a.add(t);
+    DevPtr dd;
+    char *dp = a.push(e, dd);
+    launch_split(at<SplitTask>(dp, o), 2, s);
+    count_launch(e);
+    post_launch("split");
+    OzOperand oa{static_cast<const __nv_bfloat16 *>(pa->ptr), int64_t(ar) * lpa, lpa, 0,
+                 static_cast<const int *>(ex->ptr)};
+    OzOperand ob{static_cast<const __nv_bfloat16 *>(pb->ptr), int64_t(br) * lpb, lpb, 0,
+                 static_cast<const int *>(ex->ptr) + 1};
+    OzList l;
+    l.out(static_cast<double *>(dc->ptr), N, M, N, beta != 0.0,
+          {ozc(oa, ob, K, (transA ? 1 : 0) | (transB ? 2 : 0), alpha)});
+    l.launch(e, hold);
+    check_cuda(cudaMemcpy2DAsync(C, ldc * 8, dc->ptr, N * 8, N * 8, M, cudaMemcpyDeviceToHost, s), "C");
+    check_cuda(cudaStreamSynchronize(s), "dgemm_tc");
+    return NRG_OK;
+  } catch (const Error &x) {
+    g_err = x.msg;
+    return x.code;
+  }
+}

@@ -73,13 +73,17 @@ __global__ void __launch_bounds__(256) k_split(const SplitTask *__restrict__ tas
     const int r = int(i / T.ldp), c = int(i - int64_t(r) * T.ldp);
     long long X = 0;
     if (c < T.cols) X = llrint(scalbn(T.src[int64_t(r) * T.ld + c], 55 - e));
-    // balanced base-128 digits, least significant first
+    // balanced base-128 digits, least significant first; the most
+    // significant digit is the remainder itself, which lies in [-64, 64]
+    // (|X| <= 2^55 and the lower digits sum to less than 0.504 * 128^7)
+    __nv_bfloat16 *pl = static_cast<__nv_bfloat16 *>(T.planes);
 #pragma unroll
-    for (int p = kPlanes - 1; p >= 0; --p) {
+    for (int p = kPlanes - 1; p >= 1; --p) {
       const long long a = ((X + 64) & 127) - 64;
       X = (X - a) >> 7;
-      static_cast<__nv_bfloat16 *>(T.planes)[int64_t(p) * T.pstride + i] = __float2bfloat16_rn(float(a));
+      pl[int64_t(p) * T.pstride + i] = __float2bfloat16_rn(float(a));
     }
+    pl[i] = __float2bfloat16_rn(float(X));
   }
 }
 
@@ -88,13 +92,65 @@ struct Frag {
   uint32_t a[kPlanes][4];
 };
 
+__device__ __forceinline__ void cp_async16(void *dst, const void *src, bool valid) {
+  const uint32_t d = smem_u32(dst);
+  const int sz = valid ? 16 : 0;  // 0: no bytes read, 16 zero bytes written
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(d), "l"(src), "r"(sz));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+template <int N> __device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N));
+}
+
+// Stage one 32-deep k-slice of every digit plane of op(A) (64 x 32) and
+// op(B) (32 x 64) into shared memory with 16-byte cp.async copies.  Plane
+// rows are zero-padded to a multiple of 8 elements and row starts are
+// 16-byte aligned, so every 8-element vector is either wholly inside the
+// operand or zero-filled.
+__device__ __forceinline__ void stage_tiles(const OzContrib &q, bool ta, bool tb, int M, int N, int m0,
+                                            int n0, int k0, int kend, __nv_bfloat16 *As,
+                                            __nv_bfloat16 *Bs) {
+  const int tid = threadIdx.x;
+#pragma unroll
+  for (int p = 0; p < kPlanes; ++p) {
+    {  // A: 256 vectors per plane, one per thread
+      const __nv_bfloat16 *base = q.A.p + int64_t(p) * q.A.pstride;
+      if (!ta) {  // [m][k], 64 rows x 4 vectors
+        const int mm = tid >> 2, v = tid & 3;
+        const int gm = m0 + mm, gk = k0 + 8 * v;
+        const bool ok = gm < M && gk < kend;
+        cp_async16(As + (p * BM + mm) * kPitchK + 8 * v, ok ? base + int64_t(gm) * q.A.ld + gk : base, ok);
+      } else {    // [k][m], 32 rows x 8 vectors
+        const int kk = tid >> 3, v = tid & 7;
+        const int gk = k0 + kk, gm = m0 + 8 * v;
+        const bool ok = gk < kend && gm < M;
+        cp_async16(As + (p * BK + kk) * kPitchMN + 8 * v, ok ? base + int64_t(gk) * q.A.ld + gm : base, ok);
+      }
+    }
+    {  // B
+      const __nv_bfloat16 *base = q.B.p + int64_t(p) * q.B.pstride;
+      if (tb) {   // [n][k]
+        const int nn = tid >> 2, v = tid & 3;
+        const int gn = n0 + nn, gk = k0 + 8 * v;
+        const bool ok = gn < N && gk < kend;
+        cp_async16(Bs + (p * BN + nn) * kPitchK + 8 * v, ok ? base + int64_t(gn) * q.B.ld + gk : base, ok);
+      } else {    // [k][n]
+        const int kk = tid >> 3, v = tid & 7;
+        const int gk = k0 + kk, gn = n0 + 8 * v;
+        const bool ok = gk < kend && gn < N;
+        cp_async16(Bs + (p * BK + kk) * kPitchMN + 8 * v, ok ? base + int64_t(gk) * q.B.ld + gn : base, ok);
+      }
+    }
+  }
+}
+
 __global__ void __launch_bounds__(kThreads, 1)
 k_gemm_oz(const GemmTile *__restrict__ tiles, const OzGroup *__restrict__ groups,
           const OzContrib *__restrict__ contribs) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  __nv_bfloat16 *As = reinterpret_cast<__nv_bfloat16 *>(smem_raw);
-  __nv_bfloat16 *Bs = As + kTileElems;
-  double *Ct = reinterpret_cast<double *>(Bs + kTileElems);  // BM x BN FP64 totals
+  __nv_bfloat16 *As0 = reinterpret_cast<__nv_bfloat16 *>(smem_raw);
+  __nv_bfloat16 *Bs0 = As0 + 2 * kTileElems;
+  double *Ct = reinterpret_cast<double *>(Bs0 + 2 * kTileElems);  // BM x BN FP64 totals
   const GemmTile t = tiles[blockIdx.x];
   const OzGroup g = groups[t.group];
   const int m0 = t.tm * BM, n0 = t.tn * BN;
@@ -108,6 +164,7 @@ k_gemm_oz(const GemmTile *__restrict__ tiles, const OzGroup *__restrict__ groups
     const double scale = q.alpha * scalbn(1.0, *q.A.exp + *q.B.exp - 61);
     for (int kc = 0; kc < q.K; kc += kChunkK) {
       const int kend = min(q.K, kc + kChunkK);
+      const int nst = (kend - kc + BK - 1) / BK;
       float acc[kPlanes][4][4];
 #pragma unroll
       for (int d = 0; d < kPlanes; ++d)
@@ -115,35 +172,22 @@ k_gemm_oz(const GemmTile *__restrict__ tiles, const OzGroup *__restrict__ groups
         for (int j = 0; j < 4; ++j)
 #pragma unroll
           for (int v = 0; v < 4; ++v) acc[d][j][v] = 0.f;
-      for (int k0 = kc; k0 < kend; k0 += BK) {
-        __syncthreads();
-        // stage A: op(A)[m0..m0+63][k0..k0+31] for every plane
-        for (int idx = tid; idx < kPlanes * BM * BK; idx += kThreads) {
-          const int p = idx / (BM * BK), rem = idx - p * (BM * BK);
-          int mm, kk;
-          if (ta) { mm = rem & 63; kk = rem >> 6; } else { kk = rem & 31; mm = rem >> 5; }
-          const int gm = m0 + mm, gk = k0 + kk;
-          __nv_bfloat16 v = __float2bfloat16_rn(0.f);
-          if (gm < g.M && gk < kend)
-            v = ta ? q.A.p[int64_t(p) * q.A.pstride + int64_t(gk) * q.A.ld + gm]
-                   : q.A.p[int64_t(p) * q.A.pstride + int64_t(gm) * q.A.ld + gk];
-          if (ta) As[p * (BK * kPitchMN) + kk * kPitchMN + mm] = v;
-          else    As[p * (BM * kPitchK) + mm * kPitchK + kk] = v;
-        }
-        // stage B: op(B)[k0..k0+31][n0..n0+63]
-        for (int idx = tid; idx < kPlanes * BN * BK; idx += kThreads) {
-          const int p = idx / (BN * BK), rem = idx - p * (BN * BK);
-          int nn, kk;
-          if (tb) { kk = rem & 31; nn = rem >> 5; } else { nn = rem & 63; kk = rem >> 6; }
-          const int gn = n0 + nn, gk = k0 + kk;
-          __nv_bfloat16 v = __float2bfloat16_rn(0.f);
-          if (gn < g.N && gk < kend)
-            v = tb ? q.B.p[int64_t(p) * q.B.pstride + int64_t(gn) * q.B.ld + gk]
-                   : q.B.p[int64_t(p) * q.B.pstride + int64_t(gk) * q.B.ld + gn];
-          if (tb) Bs[p * (BN * kPitchK) + nn * kPitchK + kk] = v;
-          else    Bs[p * (BK * kPitchMN) + kk * kPitchMN + nn] = v;
+      __syncthreads();  // previous users of both buffers are done
+      stage_tiles(q, ta, tb, g.M, g.N, m0, n0, kc, kend, As0, Bs0);
+      cp_async_commit();
+      for (int st = 0; st < nst; ++st) {
+        const int buf = st & 1;
+        if (st + 1 < nst) {
+          stage_tiles(q, ta, tb, g.M, g.N, m0, n0, kc + (st + 1) * BK, kend, As0 + (buf ^ 1) * kTileElems,
+                      Bs0 + (buf ^ 1) * kTileElems);
+          cp_async_commit();
+          cp_async_wait<1>();
+        } else {
+          cp_async_wait<0>();
         }
         __syncthreads();
+        const __nv_bfloat16 *As = As0 + buf * kTileElems;
+        const __nv_bfloat16 *Bs = Bs0 + buf * kTileElems;
 #pragma unroll
         for (int ks = 0; ks < BK; ks += 16) {
           Frag fa;
@@ -151,30 +195,29 @@ k_gemm_oz(const GemmTile *__restrict__ tiles, const OzGroup *__restrict__ groups
           for (int p = 0; p < kPlanes; ++p) {
             if (!ta) {
               // As[m][k]: rows wm + (lane % 16), k ks + (lane / 16) * 8
-              const __nv_bfloat16 *ptr = As + p * (BM * kPitchK) + (wm + (lane & 15)) * kPitchK + ks + (lane >> 4) * 8;
+              const __nv_bfloat16 *ptr = As + (p * BM + wm + (lane & 15)) * kPitchK + ks + (lane >> 4) * 8;
               ldsm_x4(smem_u32(ptr), fa.a[p][0], fa.a[p][1], fa.a[p][2], fa.a[p][3]);
             } else {
               // As[k][m]: matrix mi = lane / 8 covers k ks + (mi/2)*8, m wm + (mi%2)*8
               const int mi = lane >> 3;
-              const __nv_bfloat16 *ptr = As + p * (BK * kPitchMN) + (ks + (mi >> 1) * 8 + (lane & 7)) * kPitchMN + wm + (mi & 1) * 8;
+              const __nv_bfloat16 *ptr = As + (p * BK + ks + (mi >> 1) * 8 + (lane & 7)) * kPitchMN + wm + (mi & 1) * 8;
               ldsm_x4_t(smem_u32(ptr), fa.a[p][0], fa.a[p][1], fa.a[p][2], fa.a[p][3]);
             }
           }
 #pragma unroll
           for (int qd = 0; qd < kPlanes; ++qd) {
-            // B fragments of plane qd for the warp's 4 n8 tiles
             uint32_t b[4][2];
 #pragma unroll
             for (int h = 0; h < 2; ++h) {
-              // two n8 tiles per ldmatrix.x4: matrices (n-tile 2h, k 0-7), (2h, k 8-15), (2h+1, 0-7), (2h+1, 8-15)
+              // matrices (n-tile 2h, k 0-7), (2h, k 8-15), (2h+1, k 0-7), (2h+1, k 8-15)
               const int mi = lane >> 3;
               const int ntile = 2 * h + (mi >> 1), khalf = mi & 1;
               uint32_t r0, r1, r2, r3;
               if (tb) {  // Bs[n][k]
-                const __nv_bfloat16 *ptr = Bs + qd * (BN * kPitchK) + (wn + ntile * 8 + (lane & 7)) * kPitchK + ks + khalf * 8;
+                const __nv_bfloat16 *ptr = Bs + (qd * BN + wn + ntile * 8 + (lane & 7)) * kPitchK + ks + khalf * 8;
                 ldsm_x4(smem_u32(ptr), r0, r1, r2, r3);
               } else {   // Bs[k][n]
-                const __nv_bfloat16 *ptr = Bs + qd * (BK * kPitchMN) + (ks + khalf * 8 + (lane & 7)) * kPitchMN + wn + ntile * 8;
+                const __nv_bfloat16 *ptr = Bs + (qd * BK + ks + khalf * 8 + (lane & 7)) * kPitchMN + wn + ntile * 8;
                 ldsm_x4_t(smem_u32(ptr), r0, r1, r2, r3);
               }
               b[2 * h][0] = r0;
@@ -190,6 +233,7 @@ k_gemm_oz(const GemmTile *__restrict__ tiles, const OzGroup *__restrict__ groups
             }
           }
         }
+        __syncthreads();  // this buffer may be refilled by the next stage
       }
       // exact group sums -> FP64 (Horner over the groups), into the tile totals
 #pragma unroll
@@ -216,7 +260,7 @@ k_gemm_oz(const GemmTile *__restrict__ tiles, const OzGroup *__restrict__ groups
   }
 }
 
-constexpr size_t kGemmSmem = 2 * size_t(kTileElems) * sizeof(__nv_bfloat16) + BM * BN * sizeof(double);
+constexpr size_t kGemmSmem = 4 * size_t(kTileElems) * sizeof(__nv_bfloat16) + BM * BN * sizeof(double);
 
 }  // namespace
 

@@ -92,6 +92,9 @@ def _call(fn, *args):
         raise NrgError(rc, lib().nrg_last_error().decode())
 
 
+C_double = C.c_double
+
+
 def _dp(a):
     return a.ctypes.data_as(C.POINTER(C.c_double))
 
@@ -208,8 +211,8 @@ class Engine:
         K = A.shape[0] if transA else A.shape[1]
         N = B.shape[0] if transB else B.shape[1]
         C = np.zeros((M, N))
-        _call(lib().nrg_dgemm_tc, self.h, int(transA), int(transB), M, N, K, C.dtype.type(alpha),
-              _dp(A), A.shape[1], _dp(B), B.shape[1], C.dtype.type(0.0), _dp(C), N)
+        _call(lib().nrg_dgemm_tc, self.h, int(transA), int(transB), M, N, K, C_double(alpha),
+              _dp(A), A.shape[1], _dp(B), B.shape[1], C_double(0.0), _dp(C), N)
         return C
 
     def broaden(self, energies, weights, omegas, b):

@@ -228,7 +228,13 @@ def main():
     ap.add_argument("--cpu-sites", type=int, default=12,
                     help="forward sites of the bounded CPU-baseline sample")
     ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 comparator")
+    ap.add_argument("--sites", type=int, default=50,
+                    help="Wilson sites per run (50 = the workload; fewer only for profiling captures)")
     args = ap.parse_args()
+    if args.sites != WORK["nsites"]:
+        WORK["nsites"] = args.sites
+        CONFIG["sites"] = args.sites
+        CONFIG["workload"] += "_reduced_for_profiling"
     if args.impl == "reference":
         return reference_arm(args)
     import torch

@@ -352,104 +352,105 @@ static GemmContrib contrib(const double *A, int lda, const double *B, int ldb, i
   return c;
 }
 
-// Digit planes (k_ozaki.cu) of one FP64 array of square blocks.
-struct Planes {
-  DevPtr mem, exps;
-  std::vector<int64_t> poff;
-  std::vector<int> ldp;
-  int64_t pstride = 0;
-  OzOperand op(size_t b, int row0 = 0) const {
-    OzOperand o{};
-    o.p = static_cast<const __nv_bfloat16 *>(mem->ptr) + poff[b] + int64_t(row0) * ldp[b];
-    o.pstride = pstride;
-    o.ld = ldp[b];
-    o.exp = static_cast<const int *>(exps->ptr) + b;
-    return o;
-  }
-};
-
-static Planes make_planes(nrg_engine *e, const std::vector<int> &dims, std::vector<DevPtr> &hold) {
-  Planes p;
+// Split a list of FP64 matrix views (rows x cols, leading dimension ld) into
+// bf16 digit planes (k_ozaki.cu) with one grid-wide pass.  All matrices share
+// one allocation; plane p of matrix i starts at p * pstride + poff[i].
+PlaneBuf split_matrices(nrg_engine *e, const std::vector<MatRef> &mats, std::vector<DevPtr> &hold) {
+  PlaneBuf pb;
+  const size_t nm = mats.size();
+  std::vector<int64_t> poff(nm), cmax(nm + 1, 0), cdig(nm + 1, 0);
+  std::vector<int> ldp(nm);
   int64_t tot = 0;
-  for (int n : dims) {
-    p.poff.push_back(tot);
-    p.ldp.push_back(round_up(n, 8));
-    tot += int64_t(n) * round_up(n, 8);
+  for (size_t i = 0; i < nm; ++i) {
+    ldp[i] = round_up(std::max(mats[i].cols, 1), 8);
+    poff[i] = tot;
+    tot += int64_t(mats[i].rows) * ldp[i];
+    cmax[i + 1] = cmax[i] + (int64_t(mats[i].rows) * mats[i].cols + 1023) / 1024;
+    cdig[i + 1] = cdig[i] + (int64_t(mats[i].rows) * ldp[i] + 1023) / 1024;
   }
-  p.pstride = tot;
-  p.mem = dalloc(e, tot * 8 * 2 + 16);
-  p.exps = dalloc(e, dims.size() * sizeof(int) + 16);
-  hold.push_back(p.mem);
-  hold.push_back(p.exps);
-  return p;
-}
-
-static void split_planes(nrg_engine *e, Planes &p, const std::vector<const double *> &src,
-                         const std::vector<int> &ld, std::vector<DevPtr> &hold) {
-  std::vector<SplitTask> t(src.size());
-  for (size_t b = 0; b < src.size(); ++b) {
-    t[b] = SplitTask{};
-    t[b].src = src[b];
-    const int64_t plane_elems = (b + 1 < p.poff.size() ? p.poff[b + 1] : p.pstride) - p.poff[b];
-    const int rows = int(plane_elems / p.ldp[b]);
-    t[b].rows = rows;
-    t[b].cols = rows;
-    t[b].ld = ld[b];
-    t[b].ldp = p.ldp[b];
-    t[b].planes = static_cast<__nv_bfloat16 *>(p.mem->ptr) + p.poff[b];
-    t[b].pstride = p.pstride;
-    t[b].exp = static_cast<int *>(p.exps->ptr) + b;
+  pb.mem = dalloc(e, tot * kDigitPlanes * 2 + 16);
+  pb.exps = dalloc(e, nm * sizeof(int) + 16);
+  hold.push_back(pb.mem);
+  hold.push_back(pb.exps);
+  std::vector<SplitTask> t(nm);
+  pb.ops.resize(nm);
+  for (size_t i = 0; i < nm; ++i) {
+    t[i] = SplitTask{};
+    t[i].src = mats[i].p;
+    t[i].rows = mats[i].rows;
+    t[i].cols = mats[i].cols;
+    t[i].ld = mats[i].ld;
+    t[i].ldp = ldp[i];
+    t[i].planes = static_cast<__nv_bfloat16 *>(pb.mem->ptr) + poff[i];
+    t[i].pstride = tot;
+    t[i].exp = static_cast<int *>(pb.exps->ptr) + i;
+    OzOperand o{};
+    o.p = static_cast<const __nv_bfloat16 *>(pb.mem->ptr) + poff[i];
+    o.pstride = tot;
+    o.ld = ldp[i];
+    o.exp = static_cast<const int *>(pb.exps->ptr) + i;
+    pb.ops[i] = o;
   }
+  if (nm == 0) return pb;
+  const int64_t nchunk_max = cmax[nm], nchunk_dig = cdig[nm];
+  cmax.pop_back();
+  cdig.pop_back();
+  std::vector<unsigned long long> scratch(nm, 0);
   Arena a;
-  size_t o = a.add(t);
+  size_t ot = a.add(t), om = a.add(cmax), od = a.add(cdig), os = a.add(scratch);
   DevPtr d;
   char *dp = a.push(e, d);
   hold.push_back(d);
   Prof pf(e, "k_split");
-  launch_split(at<SplitTask>(dp, o), int(t.size()), e->stream);
-  count_launch(e);
+  launch_split_grid(at<SplitTask>(dp, ot), at<int64_t>(dp, om), at<int64_t>(dp, od), int(nm), nchunk_max,
+                    nchunk_dig, at<unsigned long long>(dp, os), e->stream);
+  count_launch(e, 2);
   post_launch("split");
+  return pb;
 }
 
-// One tensor-core (Ozaki) grouped-GEMM launch.
-struct OzList {
-  std::vector<OzGroup> groups;
-  std::vector<OzContrib> contribs;
-  std::vector<GemmTile> tiles;
-  double flops = 0;
-  void out(double *C, int ldc, int M, int N, bool acc, std::initializer_list<OzContrib> cs) {
-    OzGroup g{};
-    g.C = C;
-    g.ldc = ldc;
-    g.M = M;
-    g.N = N;
-    g.accumulate = acc ? 1 : 0;
-    g.c0 = int(contribs.size());
-    for (auto &c : cs) {
-      contribs.push_back(c);
-      flops += 2.0 * M * N * double(c.K);
-    }
-    g.c1 = int(contribs.size());
-    const int gi = int(groups.size());
-    groups.push_back(g);
-    for (int tm = 0; tm < (M + GEMM_TILE - 1) / GEMM_TILE; ++tm)
-      for (int tn = 0; tn < (N + GEMM_TILE - 1) / GEMM_TILE; ++tn) tiles.push_back({gi, tm, tn, 0});
-  }
-  void launch(nrg_engine *e, std::vector<DevPtr> &hold) {
-    if (tiles.empty()) return;
-    Arena a;
-    size_t ot = a.add(tiles), og = a.add(groups), oc = a.add(contribs);
-    DevPtr d;
-    char *p = a.push(e, d);
-    hold.push_back(d);
-    Prof pf(e, "k_gemm_oz", flops);
-    launch_gemm_oz(at<GemmTile>(p, ot), int(tiles.size()), at<OzGroup>(p, og), at<OzContrib>(p, oc), e->stream);
-    count_launch(e);
-    post_launch("ozaki gemm");
-  }
-};
+// square blocks of one arena (offset off[b], dimension dims[b], ld lds[b])
+static PlaneBuf split_blocks(nrg_engine *e, const double *base, const std::vector<int64_t> &off,
+                             const std::vector<int> &dims, const std::vector<int> &lds,
+                             std::vector<DevPtr> &hold) {
+  std::vector<MatRef> m(dims.size());
+  for (size_t b = 0; b < dims.size(); ++b) m[b] = MatRef{base + off[b], dims[b], dims[b], lds[b]};
+  return split_matrices(e, m, hold);
+}
 
-static OzContrib ozc(const OzOperand &A, const OzOperand &B, int K, int trans, double alpha = 1.0) {
+void OzList::out(double *C, int ldc, int M, int N, bool acc, const std::vector<OzContrib> &cs) {
+  OzGroup g{};
+  g.C = C;
+  g.ldc = ldc;
+  g.M = M;
+  g.N = N;
+  g.accumulate = acc ? 1 : 0;
+  g.c0 = int(contribs.size());
+  for (auto &c : cs) {
+    contribs.push_back(c);
+    flops += 2.0 * M * N * double(c.K);
+  }
+  g.c1 = int(contribs.size());
+  const int gi = int(groups.size());
+  groups.push_back(g);
+  for (int tm = 0; tm < (M + GEMM_TILE - 1) / GEMM_TILE; ++tm)
+    for (int tn = 0; tn < (N + GEMM_TILE - 1) / GEMM_TILE; ++tn) tiles.push_back({gi, tm, tn, 0});
+}
+
+void OzList::launch(nrg_engine *e, std::vector<DevPtr> &hold) {
+  if (tiles.empty()) return;
+  Arena a;
+  size_t ot = a.add(tiles), og = a.add(groups), oc = a.add(contribs);
+  DevPtr d;
+  char *p = a.push(e, d);
+  hold.push_back(d);
+  Prof pf(e, "k_gemm_oz", flops);
+  launch_gemm_oz(at<GemmTile>(p, ot), int(tiles.size()), at<OzGroup>(p, og), at<OzContrib>(p, oc), e->stream);
+  count_launch(e);
+  post_launch("ozaki gemm");
+}
+
+OzContrib ozc(const OzOperand &A, const OzOperand &B, int K, int trans, double alpha) {
   OzContrib c{};
   c.A = A;
   c.B = B;
@@ -536,21 +537,13 @@ static void mixed_eigensolve(nrg_engine *e, std::vector<DevBlock *> &blks, int m
     dims[b] = blks[b]->n;
     lds[b] = blks[b]->ld;
   }
-  Planes pH, pX, pY, pE;
+  PlaneBuf pH, pX, pY, pE;
   if (oz) {
-    pH = make_planes(e, dims, hold);
-    pX = make_planes(e, dims, hold);
-    pY = make_planes(e, dims, hold);
-    pE = make_planes(e, dims, hold);
-    std::vector<const double *> src(nb);
-    for (size_t b = 0; b < nb; ++b) src[b] = blks[b]->H;
-    split_planes(e, pH, src, lds, hold);
+    std::vector<MatRef> hm(nb);
+    for (size_t b = 0; b < nb; ++b) hm[b] = MatRef{blks[b]->H, dims[b], dims[b], lds[b]};
+    pH = split_matrices(e, hm, hold);
   }
-  auto splitv = [&](Planes &pl, double *base) {
-    std::vector<const double *> src(nb);
-    for (size_t b = 0; b < nb; ++b) src[b] = base + off[b];
-    split_planes(e, pl, src, lds, hold);
-  };
+  auto splitv = [&](PlaneBuf &pl, double *base) { pl = split_blocks(e, base, off, dims, lds, hold); };
   for (int step = 0; step <= kRefineSteps; ++step) {
     const bool final = (step == kRefineSteps);
     if (oz) {
@@ -856,6 +849,20 @@ static void batch_add_site(nrg_run *const *runs, int nruns, const double *t, int
       for (auto &db : st.site->blocks) blks.push_back(&db);
     std::stable_sort(blks.begin(), blks.end(), [](DevBlock *a, DevBlock *b) { return a->n > b->n; });
     mixed_eigensolve(e, blks, max_n, hold);
+    if (e->ozaki) {  // digit planes of every new U: operands of all rotations of this site
+      std::vector<MatRef> um;
+      for (auto &st : steps)
+        for (auto &db : st.site->blocks) um.push_back(MatRef{db.U, db.n, db.n, db.ld});
+      std::vector<DevPtr> keep;
+      PlaneBuf pu = split_matrices(e, um, keep);
+      size_t q = 0;
+      for (auto &st : steps) {
+        for (auto &db : st.site->blocks) db.uop = pu.ops[q++];
+        st.site->mem_Uplanes = pu.mem;
+        st.site->mem_Uexps = pu.exps;
+        st.site->has_uplanes = true;
+      }
+    }
   }
   check_cuda(cudaEventRecord(e->ev[2], s), "event");
   {
@@ -895,6 +902,7 @@ static void batch_add_site(nrg_run *const *runs, int nruns, const double *t, int
   std::vector<GemmGroup> groups;
   std::vector<GemmContrib> contribs;
   std::vector<GemmTile> tiles;
+  OzList ozrot;
   for (int i = 0; i < nruns; ++i) {
     RunStep &st = steps[i];
     nrg_run *r = st.run;
@@ -913,6 +921,8 @@ static void batch_add_site(nrg_run *const *runs, int nruns, const double *t, int
     // f-dagger rotation into the new basis, kept x kept part only
     // (nrgcore.hpp:409-476; the next site reads only this part, :199-203)
     std::map<OpKey, std::vector<GemmContrib>> outs;
+    std::map<OpKey, std::vector<OzContrib>> ozouts;
+    const bool use_oz = sd.has_uplanes;
     for (int ip = 0; ip < r->bath.nops; ++ip)
       for (auto &kv : r->bath.op[ip]) {
         const int bb = kv.first.first, bbp = kv.first.second;
@@ -927,10 +937,18 @@ static void batch_add_site(nrg_run *const *runs, int nruns, const double *t, int
           const DevBlock &bi = sd.blocks[sd.sectors[si].dev];
           const DevBlock &bj = sd.blocks[sd.sectors[sj].dev];
           auto &lst = outs[OpKey{ip, si, sj}];
+          auto &olst = ozouts[OpKey{ip, si, sj}];
           for (int il = 0; il < fb.rows; ++il)
             for (int ilp = 0; ilp < fb.cols; ++ilp) {
               const double v = fb.v[int64_t(il) * fb.cols + ilp];
               if (v == 0.0) continue;
+              if (use_oz) {
+                OzOperand a = bi.uop, b = bj.uop;
+                a.p += int64_t(ia->second.second + il * k) * a.ld;
+                b.p += int64_t(ja->second.second + ilp * k) * b.ld;
+                olst.push_back(ozc(a, b, k, 1, v));
+                continue;
+              }
               GemmContrib c{};
               c.A = bi.U + int64_t(ia->second.second + il * k) * bi.ld;
               c.lda = bi.ld;
@@ -958,6 +976,10 @@ static void batch_add_site(nrg_run *const *runs, int nruns, const double *t, int
       FBlock fbk{static_cast<double *>(r->fcur_mem->ptr) + fo, M, N, N};
       fo += int64_t(M) * N;
       r->fcur[kv.first] = fbk;
+      if (use_oz) {
+        ozrot.out(fbk.p, N, M, N, false, ozouts[kv.first]);
+        continue;
+      }
       GemmGroup g{};
       g.C = fbk.p;
       g.ldc = N;
@@ -973,7 +995,11 @@ static void batch_add_site(nrg_run *const *runs, int nruns, const double *t, int
         for (int tn = 0; tn < (N + GEMM_TILE - 1) / GEMM_TILE; ++tn) tiles.push_back({gi, tm, tn, 0});
     }
   }
-  if (!tiles.empty()) {
+  if (!ozrot.tiles.empty()) {
+    check_cuda(cudaEventRecord(e->ev[4], s), "event");
+    ozrot.launch(e, hold);
+    check_cuda(cudaEventRecord(e->ev[5], s), "event");
+  } else if (!tiles.empty()) {
     Arena ag;
     size_t o_t = ag.add(tiles), o_g = ag.add(groups), o_c = ag.add(contribs);
     DevPtr gd;

@@ -148,6 +148,13 @@ static void opset_update(nrg_opset *o) {
   DevPtr ymem = engine_alloc(e, ysz * sizeof(double) + 8);
   int64_t yo = 0;
   std::map<OpKey, std::vector<GemmContrib>> p2c;
+  // tensor-core variant (mixed path): digit planes of the O views and of Y
+  const bool oz = sd.has_uplanes;
+  std::vector<MatRef> omats, ymats;
+  std::map<const double *, size_t> oidx;
+  struct P1 { size_t o; OzOperand u; int kp, k, nj; double *Y; };
+  std::vector<P1> p1oz;
+  std::map<OpKey, std::vector<std::pair<OzOperand, size_t>>> p2oz;  // (U_i rows, Y index)
   for (auto &t : pend) {
     const FBlock *F = std::get<0>(t);
     const int ip = std::get<1>(t), ii = std::get<2>(t), iip = std::get<3>(t), bb = std::get<4>(t),
@@ -159,6 +166,17 @@ static void opset_update(nrg_opset *o) {
     const DevBlock &bj = sd.blocks[sd.sectors[b.first].dev];
     double *Y = static_cast<double *>(ymem->ptr) + yo;
     yo += int64_t(k) * bj.n;
+    if (oz) {
+      auto ins = oidx.emplace(F->p, omats.size());
+      if (ins.second) omats.push_back(MatRef{F->p, k, kp, F->ld});
+      OzOperand uj = bj.uop, ui = bi.uop;
+      uj.p += int64_t(b.second + il * kp) * uj.ld;
+      ui.p += int64_t(a.second + il * k) * ui.ld;
+      p1oz.push_back(P1{ins.first->second, uj, kp, k, bj.n, Y});
+      p2oz[OpKey{ip, a.first, b.first}].push_back({ui, ymats.size()});
+      ymats.push_back(MatRef{Y, k, bj.n, bj.n});
+      continue;
+    }
     // pass 1: Y (k x n_j) = O[:k,:k'] U_j[rows (iip,bb,il), :]
     p1.out(Y, bj.n, k, bj.n, false,
            {gc(F->p, F->ld, bj.U + int64_t(b.second + il * kp) * bj.ld, bj.ld, kp, 0, 1.0)});
@@ -181,11 +199,30 @@ static void opset_update(nrg_opset *o) {
     FBlock fb{static_cast<double *>(omem->ptr) + oo, bi.n, bj.n, bj.n};
     oo += int64_t(bi.n) * bj.n;
     nb_blocks[kv.first] = fb;
+    if (oz) continue;
     auto it = p2c.find(kv.first);
     p2.out(fb.p, fb.ld, bi.n, bj.n, false, it == p2c.end() ? std::vector<GemmContrib>{} : it->second);
   }
-  p1.run(e);
-  p2.run(e);
+  if (oz) {
+    std::vector<DevPtr> hold;
+    PlaneBuf po = split_matrices(e, omats, hold);
+    OzList l1;
+    for (auto &x : p1oz) l1.out(x.Y, x.nj, x.k, x.nj, false, {ozc(po.op(x.o), x.u, x.kp, 0)});
+    l1.launch(e, hold);
+    PlaneBuf py = split_matrices(e, ymats, hold);
+    OzList l2;
+    for (auto &kv : nb_blocks) {
+      std::vector<OzContrib> cs;
+      auto it = p2oz.find(kv.first);
+      if (it != p2oz.end())
+        for (auto &pr : it->second) cs.push_back(ozc(pr.first, py.op(pr.second), ymats[pr.second].rows, 1));
+      l2.out(kv.second.p, kv.second.ld, kv.second.rows, kv.second.cols, false, cs);
+    }
+    l2.launch(e, hold);
+  } else {
+    p1.run(e);
+    p2.run(e);
+  }
   o->blocks = std::move(nb_blocks);
   o->mem = omem;
   o->updated_this_site = true;
@@ -265,6 +302,24 @@ static void fdm_calc(nrg_fdm *f, double scale) {
   }
   DevPtr pm = engine_alloc(e, psz * sizeof(double) + 8);
   int64_t po = 0, chunk = 0;
+  // tensor-core variant (mixed path): digit planes of rho and of the operator blocks
+  const bool oz = sd.has_uplanes;
+  std::vector<DevPtr> ozhold;
+  PlaneBuf prho, pB;
+  std::map<const double *, size_t> bidx;
+  OzList ozg;
+  if (oz) {
+    std::vector<MatRef> rm, bm;
+    for (size_t b = 0; b < sd.blocks.size(); ++b) rm.push_back(MatRef{rp[b], sd.blocks[b].n, sd.blocks[b].n, sd.blocks[b].n});
+    for (auto &kv : S.ops) {
+      const int i = std::get<1>(kv.first), j = std::get<2>(kv.first);
+      if (sd.sectors[i].dev < 0 || sd.sectors[j].dev < 0) continue;
+      bidx[kv.second.p] = bm.size();
+      bm.push_back(MatRef{kv.second.p, kv.second.rows, kv.second.cols, kv.second.ld});
+    }
+    prho = split_matrices(e, rm, ozhold);
+    pB = split_matrices(e, bm, ozhold);
+  }
   for (auto &kv : S.ops) {
     const int ip = std::get<0>(kv.first), i = std::get<1>(kv.first), j = std::get<2>(kv.first);
     if (ip < 0 || ip >= f->nops) fail(NRG_E_ARG, "snapshot operator index exceeds the FDM operator count");
@@ -276,8 +331,14 @@ static void fdm_calc(nrg_fdm *f, double scale) {
     po += int64_t(Bi.n) * Bj.n;
     double *ARho = static_cast<double *>(pm->ptr) + po;
     po += int64_t(Bi.n) * Bj.n;
-    g.out(rhoA, Bj.n, Bi.n, Bj.n, false, {gc(B.p, B.ld, rp[bj], Bj.n, Bj.n, 0, 1.0)});
-    g.out(ARho, Bj.n, Bi.n, Bj.n, false, {gc(rp[bi], Bi.n, B.p, B.ld, Bi.n, 0, 1.0)});
+    if (oz) {
+      const size_t q = bidx.at(B.p);
+      ozg.out(rhoA, Bj.n, Bi.n, Bj.n, false, {ozc(pB.op(q), prho.op(bj), Bj.n, 0)});
+      ozg.out(ARho, Bj.n, Bi.n, Bj.n, false, {ozc(prho.op(bi), pB.op(q), Bi.n, 0)});
+    } else {
+      g.out(rhoA, Bj.n, Bi.n, Bj.n, false, {gc(B.p, B.ld, rp[bj], Bj.n, Bj.n, 0, 1.0)});
+      g.out(ARho, Bj.n, Bi.n, Bj.n, false, {gc(rp[bi], Bi.n, B.p, B.ld, Bi.n, 0, 1.0)});
+    }
     FdmPair fp{};
     fp.rhoA = rhoA;
     fp.ARho = ARho;
@@ -295,6 +356,7 @@ static void fdm_calc(nrg_fdm *f, double scale) {
     if (B.ld != Bj.n) fail(NRG_E_STATE, "operator block layout");
   }
   g.run(e);
+  ozg.launch(e, ozhold);
   if (!pairs.empty()) {
     Staged st;
     size_t op = st.add(pairs);
@@ -310,18 +372,35 @@ static void fdm_calc(nrg_fdm *f, double scale) {
   // setReduceDensityMatrix (:71-114): rho <- U rho U^T, then the partial trace
   DevPtr xm = engine_alloc(e, rsz * sizeof(double) + 8), rm = engine_alloc(e, rsz * sizeof(double) + 8);
   GemmBatch g1, g2;
+  OzList o1, o2;
   std::vector<double *> rot(sd.blocks.size());
+  std::vector<MatRef> xmats;
   int64_t xo = 0;
   for (size_t b = 0; b < sd.blocks.size(); ++b) {
     const DevBlock &db = sd.blocks[b];
     double *X = static_cast<double *>(xm->ptr) + xo;
     rot[b] = static_cast<double *>(rm->ptr) + xo;
     xo += int64_t(db.n) * db.n;
+    if (oz) {
+      o1.out(X, db.n, db.n, db.n, false, {ozc(prho.op(b), db.uop, db.n, 2)});  // rho U^T
+      xmats.push_back(MatRef{X, db.n, db.n, db.n});
+      continue;
+    }
     g1.out(X, db.n, db.n, db.n, false, {gc(rp[b], db.n, db.U, db.ld, db.n, 2, 1.0)});  // rho U^T
     g2.out(rot[b], db.n, db.n, db.n, false, {gc(db.U, db.ld, X, db.n, db.n, 0, 1.0)});  // U X
   }
-  g1.run(e);
-  g2.run(e);
+  if (oz) {
+    o1.launch(e, ozhold);
+    PlaneBuf px = split_matrices(e, xmats, ozhold);
+    for (size_t b = 0; b < sd.blocks.size(); ++b) {
+      const DevBlock &db = sd.blocks[b];
+      o2.out(rot[b], db.n, db.n, db.n, false, {ozc(db.uop, px.op(b), db.n, 0)});  // U X
+    }
+    o2.launch(e, ozhold);
+  } else {
+    g1.run(e);
+    g2.run(e);
+  }
   const int npre = int(sd.pre_q.size());
   std::vector<DevPtr> red_mem(npre);
   std::vector<double *> red(npre, nullptr);
@@ -828,7 +907,7 @@ int nrg_broaden(nrg_engine *e, const double *energies, const double *weights, ui
     std::vector<double> ee, ww;
     for (uint64_t i = 0; i < nbins; ++i)
       if (weights[i] != 0.0) {
-        ee.push_back(energies[i]);
+        ee.push_back(std::log(energies[i]));  // the kernel takes ln(e_i)
         ww.push_back(weights[i]);
       }
     std::vector<double> om(omegas, omegas + nomega);

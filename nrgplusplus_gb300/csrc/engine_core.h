@@ -65,6 +65,7 @@ struct DevBlock {     // non-empty sector on the device
   int sector = 0;
   int n = 0, ld = 0;
   double *H = nullptr, *U = nullptr, *E = nullptr;
+  OzOperand uop{};    // digit planes of U (mixed path), when present
 };
 
 struct FBlock {       // one operator block on the device
@@ -84,7 +85,38 @@ struct SiteData {
   std::vector<int64_t> kept_prev;  // eigenvaluesQ_kept_indices sizes (pre sectors)
   DevPtr mem_U, mem_E;
   std::vector<std::vector<double>> E_host;  // eigenvalues per sector (unshifted)
+  DevPtr mem_Uplanes, mem_Uexps;            // digit planes of every U block (mixed path)
+  bool has_uplanes = false;
 };
+
+// FP64 matrix view and its bf16 digit planes (tensor-core GEMM operands).
+constexpr int kDigitPlanes = 8;
+struct MatRef {
+  const double *p;
+  int rows, cols, ld;
+};
+struct PlaneBuf {
+  DevPtr mem, exps;
+  std::vector<OzOperand> ops;  // plane-0 operand of each matrix (row 0)
+  OzOperand op(size_t i, int row0 = 0) const {
+    OzOperand o = ops[i];
+    o.p += int64_t(row0) * o.ld;
+    return o;
+  }
+};
+
+PlaneBuf split_matrices(nrg_engine *e, const std::vector<MatRef> &mats, std::vector<DevPtr> &hold);
+
+// One tensor-core (Ozaki) grouped-GEMM launch: C = [C +] sum alpha op(A) op(B).
+struct OzList {
+  std::vector<OzGroup> groups;
+  std::vector<OzContrib> contribs;
+  std::vector<GemmTile> tiles;
+  double flops = 0;
+  void out(double *C, int ldc, int M, int N, bool acc, const std::vector<OzContrib> &cs);
+  void launch(nrg_engine *e, std::vector<DevPtr> &hold);
+};
+OzContrib ozc(const OzOperand &A, const OzOperand &B, int K, int trans, double alpha = 1.0);
 
 struct Snapshot {
   std::shared_ptr<SiteData> site;

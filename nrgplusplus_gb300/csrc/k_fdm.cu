@@ -61,16 +61,21 @@ __global__ void k_partial_trace(const TraceTask *__restrict__ tasks, const Trace
   }
 }
 
-// Log-Gaussian broadening of the binned weights (spec.py:27-44).
-__global__ void k_broaden(const double *__restrict__ e, const double *__restrict__ w, int64_t nbins,
+// Log-Gaussian broadening of the binned weights (spec.py:27-44).  `le` holds
+// ln(e_i); the Gaussian argument is formed in FP64 and only the exponential
+// itself runs in FP32 (relative error ~2 ulp = 2.4e-7, inside the 1e-6
+// tolerance of the spectral function), accumulated in FP64.
+__global__ void k_broaden(const double *__restrict__ le, const double *__restrict__ w, int64_t nbins,
                           const double *__restrict__ omegas, double b, double *__restrict__ out) {
   __shared__ double red[32];
   const double x = omegas[blockIdx.x];
   const double lx = log(x);
+  const double ib = 1.0 / b;
   double s = 0.0;
   for (int64_t i = threadIdx.x; i < nbins; i += blockDim.x) {
-    const double z = -b * 0.25 + (lx - log(e[i])) / b;
-    s += w[i] * exp(-z * z);
+    const double z = fma(lx - le[i], ib, -b * 0.25);
+    const double z2 = z * z;
+    if (z2 < 80.0) s = fma(w[i], double(expf(-float(z2))), s);
   }
   for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;

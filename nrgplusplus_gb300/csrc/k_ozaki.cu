@@ -53,6 +53,69 @@ __device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], 
 }
 
 // ---------------------------------------------------------------- split
+// Two grid-wide passes over every element of every task (chunks of 1024
+// elements, task located by binary search on the chunk prefix):
+//   k_split_max:    per-task max |x| by atomicMax on the IEEE bits (for
+//                   non-negative doubles the bit order is the value order);
+//   k_split_digits: exponent from the max, then the 8 digits per element.
+__device__ __forceinline__ int find_task(const int64_t *chunk0, int ntasks, int64_t chunk) {
+  int lo = 0, hi = ntasks - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (chunk0[mid] <= chunk) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+__global__ void __launch_bounds__(256)
+k_split_max(const SplitTask *__restrict__ tasks, const int64_t *__restrict__ chunk0, int ntasks,
+            unsigned long long *__restrict__ maxbits) {
+  const int t = find_task(chunk0, ntasks, blockIdx.x);
+  const SplitTask T = tasks[t];
+  const int64_t base = (int64_t(blockIdx.x) - chunk0[t]) * 1024;
+  const int64_t nel = int64_t(T.rows) * T.cols;
+  double m = 0.0;
+  for (int u = 0; u < 4; ++u) {
+    const int64_t i = base + u * 256 + threadIdx.x;
+    if (i < nel) {
+      const int r = int(i / T.cols), c = int(i - int64_t(r) * T.cols);
+      m = fmax(m, fabs(T.src[int64_t(r) * T.ld + c]));
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0 && m > 0.0)
+    atomicMax(maxbits + t, static_cast<unsigned long long>(__double_as_longlong(m)));
+}
+
+__global__ void __launch_bounds__(256)
+k_split_digits(const SplitTask *__restrict__ tasks, const int64_t *__restrict__ chunk0, int ntasks,
+               const unsigned long long *__restrict__ maxbits) {
+  const int t = find_task(chunk0, ntasks, blockIdx.x);
+  const SplitTask T = tasks[t];
+  const double mx = __longlong_as_double(static_cast<long long>(maxbits[t]));
+  const int e = (mx > 0.0 && isfinite(mx)) ? ilogb(mx) + 1 : 0;
+  if (blockIdx.x == chunk0[t] && threadIdx.x == 0) *T.exp = e;
+  const int64_t base = (int64_t(blockIdx.x) - chunk0[t]) * 1024;
+  const int64_t nel = int64_t(T.rows) * T.ldp;
+  __nv_bfloat16 *pl = static_cast<__nv_bfloat16 *>(T.planes);
+  for (int u = 0; u < 4; ++u) {
+    const int64_t i = base + u * 256 + threadIdx.x;
+    if (i >= nel) break;
+    const int r = int(i / T.ldp), c = int(i - int64_t(r) * T.ldp);
+    long long X = 0;
+    if (c < T.cols) X = llrint(scalbn(T.src[int64_t(r) * T.ld + c], 55 - e));
+    // balanced base-128 digits, least significant first; the most
+    // significant digit is the remainder itself, which lies in [-64, 64]
+#pragma unroll
+    for (int p = kPlanes - 1; p >= 1; --p) {
+      const long long a = ((X + 64) & 127) - 64;
+      X = (X - a) >> 7;
+      pl[int64_t(p) * T.pstride + i] = __float2bfloat16_rn(float(a));
+    }
+    pl[i] = __float2bfloat16_rn(float(X));
+  }
+}
+
 __global__ void __launch_bounds__(256) k_split(const SplitTask *__restrict__ tasks) {
   __shared__ double red[8];
   const SplitTask T = tasks[blockIdx.x];
@@ -235,17 +298,22 @@ k_gemm_oz(const GemmTile *__restrict__ tiles, const OzGroup *__restrict__ groups
         }
         __syncthreads();  // this buffer may be refilled by the next stage
       }
-      // exact group sums -> FP64 (Horner over the groups), into the tile totals
+      // exact group sums -> FP64: Horner over the groups in integers (groups
+      // 0-4 into hi <= 2^53, groups 5-7 into lo <= 2^39), then one FP64 fma
 #pragma unroll
       for (int j = 0; j < 4; ++j)
 #pragma unroll
         for (int v = 0; v < 4; ++v) {
-          double h = acc[0][j][v];
+          long long hi = __float2ll_rz(acc[0][j][v]);
 #pragma unroll
-          for (int d = 1; d < kPlanes; ++d) h = fma(h, 128.0, double(acc[d][j][v]));
+          for (int d = 1; d < 5; ++d) hi = hi * 128 + __float2ll_rz(acc[d][j][v]);
+          long long lo = __float2ll_rz(acc[5][j][v]);
+#pragma unroll
+          for (int d = 6; d < kPlanes; ++d) lo = lo * 128 + __float2ll_rz(acc[d][j][v]);
+          const double h = fma(__ll2double_rn(hi), 2097152.0, __ll2double_rn(lo));  // 128^3
           const int r = wm + (lane >> 2) + (v >> 1) * 8;
           const int col = wn + j * 8 + (lane & 3) * 2 + (v & 1);
-          Ct[r * BN + col] += scale * h;
+          Ct[r * BN + col] = fma(scale, h, Ct[r * BN + col]);
         }
     }
   }
@@ -267,6 +335,15 @@ constexpr size_t kGemmSmem = 4 * size_t(kTileElems) * sizeof(__nv_bfloat16) + BM
 void launch_split(const SplitTask *tasks, int ntasks, cudaStream_t s) {
   if (ntasks == 0) return;
   k_split<<<ntasks, 256, 0, s>>>(tasks);
+}
+
+void launch_split_grid(const SplitTask *tasks, const int64_t *chunk0_max, const int64_t *chunk0_dig,
+                       int ntasks, int64_t nchunk_max, int64_t nchunk_dig, unsigned long long *maxbits,
+                       cudaStream_t s) {
+  if (ntasks == 0) return;
+  cudaMemsetAsync(maxbits, 0, sizeof(unsigned long long) * ntasks, s);
+  if (nchunk_max > 0) k_split_max<<<unsigned(nchunk_max), 256, 0, s>>>(tasks, chunk0_max, ntasks, maxbits);
+  k_split_digits<<<unsigned(nchunk_dig), 256, 0, s>>>(tasks, chunk0_dig, ntasks, maxbits);
 }
 
 void launch_gemm_oz(const GemmTile *tiles, int ntiles, const OzGroup *groups, const OzContrib *contribs,

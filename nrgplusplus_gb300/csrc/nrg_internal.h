@@ -136,6 +136,12 @@ struct OzGroup {
   int c0, c1;
 };
 void launch_split(const SplitTask *tasks, int ntasks, cudaStream_t s);
+// Grid-wide split: chunk0_max / chunk0_dig are per-task prefix counts of
+// 1024-element chunks over rows*cols (max pass) and rows*ldp (digit pass);
+// maxbits: ntasks of scratch.
+void launch_split_grid(const SplitTask *tasks, const int64_t *chunk0_max, const int64_t *chunk0_dig,
+                       int ntasks, int64_t nchunk_max, int64_t nchunk_dig, unsigned long long *maxbits,
+                       cudaStream_t s);
 void launch_gemm_oz(const GemmTile *tiles, int ntiles, const OzGroup *groups, const OzContrib *contribs,
                     cudaStream_t s);
 

@@ -192,8 +192,37 @@ def reference_arm(args):
 # nominal per-GPU peaks for the pipes MEASURED_PEAKS.json does not cover
 FP64_PEAK_TFLOPS = 1.25   # GB300 FP64 (vector and tensor) dense
 FP32_PEAK_TFLOPS = 80.5   # 152 SMs x 128 FP32 lanes x 2 flops x 2.07 GHz
-PEAKS = {"k_gemm_f64": ("fp64", FP64_PEAK_TFLOPS), "k_eig_f64": ("fp64", FP64_PEAK_TFLOPS),
-         "k_eig_f32": ("fp32", FP32_PEAK_TFLOPS)}
+OZ_PAIRS = 36             # bf16 digit-plane products per FP64 product (p + q <= 7 of 8 x 8)
+
+
+def _measured(key, fallback):
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)[key]), "of measured (MEASURED_PEAKS.json %s)" % key
+    except (OSError, KeyError, ValueError):
+        return fallback, "of fallback (%s)" % key
+
+
+def kernel_models():
+    """Per kernel: (bound, peak, unit, multiplier from the recorded work to the
+    unit's numerator, peak source, per-launch work definition)."""
+    bf16, bf16_src = _measured("bf16_tflops_sustained", 1700.0)
+    hbm, hbm_src = _measured("hbm_gbs", 6800.0)
+    fp64 = ("fp64", FP64_PEAK_TFLOPS, "TFLOP/s", 1e-12, "nominal GB300 FP64",
+            "2MNK per GEMM contribution / (10/3) n^3 per eigensolved block")
+    return {
+        "k_gemm_f64": fp64,
+        "k_eig_f64": fp64,
+        "k_eig_bi_f32": ("fp32", FP32_PEAK_TFLOPS, "TFLOP/s", 1e-12, "nominal GB300 FP32",
+                         "(4/3) n^3 per block (Householder reduction + Q accumulation)"),
+        "k_backtransform": ("fp32", FP32_PEAK_TFLOPS, "TFLOP/s", 1e-12, "nominal GB300 FP32",
+                            "2 n^3 per block"),
+        "k_gemm_oz": ("tensor", bf16, "TFLOP/s", OZ_PAIRS * 1e-12, bf16_src,
+                      "36 bf16 digit-plane products x 2MNK per FP64-accurate GEMM contribution"),
+        "k_split": ("hbm", hbm, "GB/s", 1e-9, hbm_src,
+                    "bytes: 8 (max pass) + 8 (digit pass) read + 16 written per element"),
+        "k_oa_update": ("hbm", hbm, "GB/s", 1e-9, hbm_src, "bytes: S, G read + E written, 24 per element"),
+    }
 
 
 def kernel_profile(engine):
@@ -206,17 +235,25 @@ def kernel_profile(engine):
     return kt
 
 
+def _roofline(name, ms, work, n, models):
+    bound, peak, unit, mult, src, per = models[name]
+    achieved = work * mult / (ms * 1e-3) if ms > 0 else 0.0
+    return {"bound": bound, "kernel": name, "achieved": achieved, "peak": peak, "unit": unit,
+            "frac": achieved / peak if peak else None, "traffic": None, "peak_source": src,
+            "launches": n, "ms_total": ms, "per_launch": per}
+
+
 def roofline_from(kt):
-    top = max(kt.items(), key=lambda kv: kv[1][0])
-    name, (ms, work, n) = top
-    bound, peak = PEAKS.get(name, ("fp64", FP64_PEAK_TFLOPS))
-    achieved = work / (ms * 1e-3) / 1e12 if ms > 0 else 0.0
-    return {"bound": bound, "kernel": name, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-            "frac": achieved / peak if peak else None, "traffic": None,
-            "peak_source": "nominal GB300 %s (MEASURED_PEAKS.json has HBM and bf16 only)" % bound,
-            "launches": n, "ms_total": ms,
-            "per_launch": "algorithmic flops summed over the launch's blocks: 2MNK per GEMM "
-                          "contribution, (10/3) n^3 per eigensolved block"}
+    """Roofline of the kernel with the largest share of the step, plus every
+    modelled kernel's own line."""
+    models = kernel_models()
+    known = {k: v for k, v in kt.items() if k in models}
+    top = max(known.items(), key=lambda kv: kv[1][0])
+    rf = _roofline(top[0], *top[1], models)
+    rf["all"] = {k: {"achieved": round(r["achieved"], 2), "unit": r["unit"], "frac": round(r["frac"], 4),
+                     "bound": r["bound"], "ms": round(v[0], 3)}
+                 for k, v in known.items() for r in [_roofline(k, *v, models)]}
+    return rf
 
 
 def main():
@@ -225,7 +262,7 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours")
-    ap.add_argument("--cpu-sites", type=int, default=12,
+    ap.add_argument("--cpu-sites", type=int, default=50,
                     help="forward sites of the bounded CPU-baseline sample")
     ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 comparator")
     ap.add_argument("--sites", type=int, default=50,
@@ -290,6 +327,7 @@ def main():
     e2e_v = ws * BATCH / (esum / args.steps)
     kt = kernel_profile(engine)
     rf = roofline_from(kt)
+    fallbacks = engine.fallback_count()
     engine.close()
     plain = None
     if not args.no_fp64:
@@ -318,6 +356,7 @@ def main():
                 "data": "synthetic (model parameters of the workload; no dataset)",
                 "config": dict(CONFIG, precision_path="mixed: FP32 block solve + FP64-accurate refinement"),
                 "gpu_launches": launches,
+                "fp64_fallback_blocks": fallbacks,
                 "e2e": {"value": e2e_v, "unit": "runs/s", "h2d_bytes_per_step": 4096,
                         "d2h_bytes_per_step": int(d2h)},
                 "plain_fp64": plain, "roofline": rf,

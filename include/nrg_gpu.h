@@ -103,11 +103,16 @@ int nrg_engine_destroy(nrg_engine *eng);
 int nrg_engine_phase_times(nrg_engine *eng, double *out, int cap, int *n);
 /* Number of kernel launches issued by the engine so far. */
 int nrg_engine_launch_count(nrg_engine *eng, uint64_t *out);
+/* Mixed precision: number of blocks whose refinement did not converge and
+ * that were re-solved with the FP64 block solver (0 for NRG_PREC_FP64).
+ * No counterpart in the reference (it has one FP64 path). */
+int nrg_engine_fallback_count(nrg_engine *eng, uint64_t *out);
 /* Per-kernel CUDA-event timing on the engine stream (off by default). */
 int nrg_engine_set_profiling(nrg_engine *eng, int on);
 /* Times recorded since the last call, aggregated per kernel: names (each
- * followed by '\n'), total milliseconds, algorithmic flops and launch
- * counts; nk = kernels written.  Clears the record. */
+ * followed by '\n'), total milliseconds, algorithmic flops (bytes for the
+ * memory-bound k_split and k_oa_update) and launch counts; nk = kernels
+ * written.  Clears the record. */
 int nrg_engine_kernel_times(nrg_engine *eng, char *names, uint64_t names_cap, double *ms,
                             double *work, uint64_t *count, int cap, int *nk);
 int nrg_engine_sync(nrg_engine *eng);

@@ -57,7 +57,8 @@ class RunInfo(C.Structure):
 
 EXPORTS = [
     "nrg_last_error", "nrg_engine_create", "nrg_engine_destroy", "nrg_engine_phase_times",
-    "nrg_engine_launch_count", "nrg_engine_set_profiling", "nrg_engine_kernel_times",
+    "nrg_engine_launch_count", "nrg_engine_fallback_count", "nrg_engine_set_profiling",
+    "nrg_engine_kernel_times",
     "nrg_engine_sync", "nrg_run_create", "nrg_run_destroy",
     "nrg_run_set_parameters", "nrg_run_set_bath", "nrg_run_add_site", "nrg_run_update_state",
     "nrg_run_check_discarded", "nrg_run_get_info", "nrg_run_get_all_eigenvalues",
@@ -168,6 +169,12 @@ class Engine:
         _call(lib().nrg_engine_launch_count, self.h, C.byref(v))
         return v.value
 
+    def fallback_count(self):
+        """Blocks of the mixed path re-solved in FP64 so far."""
+        v = C.c_uint64()
+        _call(lib().nrg_engine_fallback_count, self.h, C.byref(v))
+        return v.value
+
     def sync(self):
         _call(lib().nrg_engine_sync, self.h)
 
@@ -175,7 +182,7 @@ class Engine:
         _call(lib().nrg_engine_set_profiling, self.h, 1 if on else 0)
 
     def kernel_times(self):
-        """{kernel: (ms, algorithmic flops, launches)} recorded since the last call."""
+        """{kernel: (ms, algorithmic flops or bytes, launches)} recorded since the last call."""
         cap = 64
         names = C.create_string_buffer(8192)
         ms = (C.c_double * cap)()

@@ -401,7 +401,10 @@ PlaneBuf split_matrices(nrg_engine *e, const std::vector<MatRef> &mats, std::vec
   DevPtr d;
   char *dp = a.push(e, d);
   hold.push_back(d);
-  Prof pf(e, "k_split");
+  double bytes = 0;  // algorithmic: 8 + 8 bytes read per element, 8 x 2 bytes written per padded element
+  for (size_t i = 0; i < nm; ++i)
+    bytes += 16.0 * mats[i].rows * mats[i].cols + 16.0 * mats[i].rows * ldp[i];
+  Prof pf(e, "k_split", bytes);
   launch_split_grid(at<SplitTask>(dp, ot), at<int64_t>(dp, om), at<int64_t>(dp, od), int(nm), nchunk_max,
                     nchunk_dig, at<unsigned long long>(dp, os), e->stream);
   count_launch(e, 2);
@@ -531,7 +534,7 @@ static void mixed_eigensolve(nrg_engine *e, std::vector<DevBlock *> &blks, int m
   }
   int cur = 0;
   // digit planes for the tensor-core GEMMs (H once, X / Y / E per step)
-  const bool oz = e->ozaki;
+  const bool oz = (e->ozaki & 1) != 0;
   std::vector<int> dims(nb), lds(nb);
   for (size_t b = 0; b < nb; ++b) {
     dims[b] = blks[b]->n;
@@ -594,7 +597,9 @@ static void mixed_eigensolve(nrg_engine *e, std::vector<DevBlock *> &blks, int m
       break;
     }
     {
-      Prof pf(e, "k_oa_update");
+      double bytes = 0;  // S, G read and E written
+      for (size_t b = 0; b < nb; ++b) bytes += 24.0 * blks[b]->n * blks[b]->n;
+      Prof pf(e, "k_oa_update", bytes);
       launch_oa_update(at<RefineBlock>(dp, orb), int(nb), max_n, kClusterTau, s);
       count_launch(e);
       post_launch("refine update");
@@ -849,7 +854,7 @@ static void batch_add_site(nrg_run *const *runs, int nruns, const double *t, int
       for (auto &db : st.site->blocks) blks.push_back(&db);
     std::stable_sort(blks.begin(), blks.end(), [](DevBlock *a, DevBlock *b) { return a->n > b->n; });
     mixed_eigensolve(e, blks, max_n, hold);
-    if (e->ozaki) {  // digit planes of every new U: operands of all rotations of this site
+    if (e->ozaki & 2) {  // digit planes of every new U: operands of all rotations of this site
       std::vector<MatRef> um;
       for (auto &st : steps)
         for (auto &db : st.site->blocks) um.push_back(MatRef{db.U, db.n, db.n, db.ld});

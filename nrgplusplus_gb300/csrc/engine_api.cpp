@@ -478,7 +478,7 @@ int nrg_engine_create(const nrg_engine_opts *opts, nrg_engine **out) {
     for (auto &ev : e->ev) check_cuda(cudaEventCreate(&ev), "event");
     e->eig_smem_f64 = eig_smem_limit_f64();
     e->eig_smem_f32 = eig_smem_limit_f32();
-    if (const char *oz = std::getenv("NRG_OZAKI")) e->ozaki = std::atoi(oz) != 0;
+    if (const char *oz = std::getenv("NRG_OZAKI")) e->ozaki = std::atoi(oz) & 3;
     *out = e;
   });
 }
@@ -555,6 +555,13 @@ int nrg_engine_launch_count(nrg_engine *e, uint64_t *out) {
   return guard([&] {
     if (!e || !out) fail(NRG_E_ARG, "null argument");
     *out = e->launches;
+  });
+}
+
+int nrg_engine_fallback_count(nrg_engine *e, uint64_t *out) {
+  return guard([&] {
+    if (!e || !out) fail(NRG_E_ARG, "null argument");
+    *out = e->fallback_blocks;
   });
 }
 

@@ -141,13 +141,15 @@ struct nrg_engine {
   int *d_status = nullptr;
   size_t status_cap = 0;
   uint64_t fallback_blocks = 0;  // mixed path: blocks re-solved in FP64
-  bool ozaki = true;             // mixed path: FP64-accurate GEMMs on tensor cores
+  // mixed path: FP64-accurate GEMMs on the tensor cores, bit 0 for the
+  // eigenvector refinement, bit 1 for the operator rotations
+  int ozaki = 3;
   // optional per-kernel event timing (nrg_engine_set_profiling)
   bool profile = false;
   struct ProfRec {
     std::string name;
     cudaEvent_t a, b;
-    double work;  // algorithmic flops of the launch
+    double work;  // algorithmic flops (bytes for memory-bound kernels) of the launch
   };
   std::vector<ProfRec> prof;
   std::vector<cudaEvent_t> ev_pool;
@@ -155,7 +157,8 @@ struct nrg_engine {
 
 namespace nrg {
 // Records CUDA events around one kernel launch on the engine stream when
-// profiling is on; `work` is the launch's algorithmic flop count.
+// profiling is on; `work` is the launch's algorithmic flop count (byte count
+// for the memory-bound kernels k_split and k_oa_update).
 struct Prof {
   nrg_engine *e;
   const char *name;

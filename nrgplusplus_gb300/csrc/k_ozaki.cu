@@ -160,6 +160,14 @@ __device__ __forceinline__ void cp_async16(void *dst, const void *src, bool vali
   const int sz = valid ? 16 : 0;  // 0: no bytes read, 16 zero bytes written
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(d), "l"(src), "r"(sz));
 }
+// 8-element vector along k whose tail may run past kend (sub-matrix views
+// whose rows continue with real data): copy the first `nvalid` elements,
+// zero the rest.  cp.async src-size is in bytes (2 per element).
+__device__ __forceinline__ void cp_async16_k(void *dst, const void *src, int nvalid) {
+  const uint32_t d = smem_u32(dst);
+  const int sz = nvalid <= 0 ? 0 : (nvalid >= 8 ? 16 : 2 * nvalid);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 16, %2;\n" ::"r"(d), "l"(src), "r"(sz));
+}
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
 template <int N> __device__ __forceinline__ void cp_async_wait() {
   asm volatile("cp.async.wait_group %0;\n" ::"n"(N));
@@ -182,7 +190,8 @@ __device__ __forceinline__ void stage_tiles(const OzContrib &q, bool ta, bool tb
         const int mm = tid >> 2, v = tid & 3;
         const int gm = m0 + mm, gk = k0 + 8 * v;
         const bool ok = gm < M && gk < kend;
-        cp_async16(As + (p * BM + mm) * kPitchK + 8 * v, ok ? base + int64_t(gm) * q.A.ld + gk : base, ok);
+        cp_async16_k(As + (p * BM + mm) * kPitchK + 8 * v, ok ? base + int64_t(gm) * q.A.ld + gk : base,
+                     ok ? kend - gk : 0);
       } else {    // [k][m], 32 rows x 8 vectors
         const int kk = tid >> 3, v = tid & 7;
         const int gk = k0 + kk, gm = m0 + 8 * v;
@@ -196,7 +205,8 @@ __device__ __forceinline__ void stage_tiles(const OzContrib &q, bool ta, bool tb
         const int nn = tid >> 2, v = tid & 3;
         const int gn = n0 + nn, gk = k0 + 8 * v;
         const bool ok = gn < N && gk < kend;
-        cp_async16(Bs + (p * BN + nn) * kPitchK + 8 * v, ok ? base + int64_t(gn) * q.B.ld + gk : base, ok);
+        cp_async16_k(Bs + (p * BN + nn) * kPitchK + 8 * v, ok ? base + int64_t(gn) * q.B.ld + gk : base,
+                     ok ? kend - gk : 0);
       } else {    // [k][n]
         const int kk = tid >> 3, v = tid & 7;
         const int gk = k0 + kk, gn = n0 + 8 * v;

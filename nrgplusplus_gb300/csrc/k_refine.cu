@@ -26,6 +26,10 @@ constexpr int kThreads = 512;
 constexpr int kWarps = kThreads / 32;
 constexpr int kMaxCluster = 64;
 constexpr int kMaxJacobiSweeps = 30;
+// Largest remaining Newton correction accepted after the last step.  A
+// converged block sits near u |A| / gap <= 1e-16 / tau_rel = 1e-12; a block
+// whose FP32 start was too poor for the fixed step count stays far above.
+constexpr double kConvTol = 1e-10;
 
 __device__ double block_max(double v, double *red) {
   for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
@@ -67,8 +71,10 @@ k_oa_update(const RefineBlock *__restrict__ blocks, double tau_rel) {
 }
 
 // Final Rayleigh-Ritz pass: eigenvalues, cluster diagonalisation, sorted
-// output (E ascending, U columns in the same order).  status[b] = 2 when a
-// cluster exceeds kMaxCluster (the host then re-solves the block in FP64).
+// output (E ascending, U columns in the same order).  status[b] = 2 when
+// the refinement has not converged (non-finite Rayleigh quotients or a
+// remaining correction above kConvTol) or a cluster exceeds kMaxCluster; the
+// host then re-solves the block in FP64.
 __global__ void __launch_bounds__(kThreads)
 k_oa_final(const RefineBlock *__restrict__ blocks, double tau_rel, int *status) {
   extern __shared__ __align__(16) double sm[];
@@ -91,6 +97,22 @@ k_oa_final(const RefineBlock *__restrict__ blocks, double tau_rel, int *status) 
     if (!isfinite(l)) bad = 1.0;
   }
   const double tau = tau_rel * fmax(1.0, block_max(local, red));
+  __syncthreads();  // lam complete
+  // convergence: every entry of the correction one more Newton step would
+  // apply (the k_oa_update formulas; within a cluster only the orthogonality
+  // part) must be below kConvTol, otherwise the block is re-solved in FP64
+  for (int64_t idx = threadIdx.x; idx < int64_t(n) * n && bad == 0.0; idx += kThreads) {
+    const int i = int(idx / n), j = int(idx - int64_t(i) * n);
+    const double g = B.G[int64_t(i) * B.ld + j];
+    double r;
+    if (i == j) {
+      r = 1.0 - g;
+    } else {
+      const double d = lam[j] - lam[i];
+      r = (fabs(d) > tau) ? (B.S[int64_t(i) * B.ld + j] - lam[j] * g) / d : g;
+    }
+    if (!(fabs(r) <= kConvTol)) bad = 1.0;
+  }
   if (block_max(bad, red) > 0.0) {  // refinement broke down: re-solve in FP64
     if (threadIdx.x == 0) status[blockIdx.x] = 2;
     return;

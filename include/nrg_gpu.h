@@ -188,6 +188,29 @@ int nrg_fdm_get(nrg_fdm *f, double *energy_points, double *positive, double *neg
 int nrg_broaden(nrg_engine *eng, const double *energies, const double *weights, uint64_t nbins,
                 const double *omegas, uint64_t nomega, double b, double *out);
 
+/* nrg_broaden on caller-owned DEVICE buffers without any allocation.  No
+ * counterpart in the reference (its broadening is host code on host arrays).
+ * For callers that hold the histogram on the device and may not let a library
+ * allocate device memory (a process whose HBM is reserved up front, e.g. under
+ * an nrg_engine_opts budget or another framework's pool).
+ * - Its one intermediate (ln e_i per bin) lives in a static device array of
+ *   NRG_BROADEN_NOALLOC_MAX_BINS doubles (1 MiB); nbins above that is
+ *   rejected with NRG_E_ARG.  No buffer has to start at zero: each call
+ *   writes the nbins scratch entries it reads and every out[k].
+ * - The current device is used; its first call looks up the scratch address
+ *   (cudaGetSymbolAddress), which may load the kernels' module.  Make that
+ *   first call on each device before any stream capture begins.
+ * - Asynchronous: the kernels are enqueued on `stream` (a cudaStream_t;
+ *   NULL = the legacy default stream) and the call returns; read `out` after
+ *   that stream has completed.  All pointers must stay valid until then.
+ * - The scratch is shared per device: calls whose work may overlap (other
+ *   streams, other host threads on the same device) race on it.  Calls on one
+ *   stream are ordered and safe. */
+#define NRG_BROADEN_NOALLOC_MAX_BINS 131072
+int nrg_broaden_noalloc(const double *energies, const double *weights, uint64_t nbins,
+                        const double *omegas, uint64_t nomega, double b, double *out,
+                        void *stream);
+
 /* ---- thermodynamics (fdmThermodynamics.hpp) ---------------------------- */
 /* ctor (:26-38): nrg_iterations from the run, bath dimension from the bath */
 int nrg_thermo_create(nrg_run *run, const double *temps, int nt, nrg_thermo **out);

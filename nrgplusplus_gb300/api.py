@@ -68,8 +68,9 @@ EXPORTS = [
     "nrg_run_snapshot", "nrg_run_load_snapshot", "nrg_fdm_create", "nrg_fdm_destroy",
     "nrg_fdm_calc", "nrg_fdm_get", "nrg_broaden", "nrg_thermo_create", "nrg_thermo_destroy",
     "nrg_thermo_calc", "nrg_thermo_final", "nrg_batch_add_site", "nrg_batch_update_state",
-    "nrg_eigh_batched", "nrg_dgemm_tc",
+    "nrg_eigh_batched", "nrg_dgemm_tc", "nrg_broaden_noalloc",
 ]
+BROADEN_NOALLOC_MAX_BINS = 131072  # NRG_BROADEN_NOALLOC_MAX_BINS
 
 
 def lib():
@@ -230,6 +231,16 @@ class Engine:
         _call(lib().nrg_broaden, self.h, _dp(e), _dp(w), C.c_uint64(len(e)), _dp(o),
               C.c_uint64(len(o)), C.c_double(b), _dp(out))
         return out
+
+
+def broaden_noalloc(energies_ptr, weights_ptr, nbins, omegas_ptr, nomega, b, out_ptr, stream=0):
+    """nrg_broaden_noalloc: broadening on caller-owned device buffers (raw
+    device addresses of float64 arrays), enqueued on `stream` (a cudaStream_t
+    value, 0 = legacy default stream); allocates nothing.  Returns at once:
+    synchronize the stream before reading `out`."""
+    _call(lib().nrg_broaden_noalloc, C.c_void_p(energies_ptr), C.c_void_p(weights_ptr), C.c_uint64(nbins),
+          C.c_void_p(omegas_ptr), C.c_uint64(nomega), C.c_double(b), C.c_void_p(out_ptr),
+          C.c_void_p(stream))
 
 
 class NrgCore:

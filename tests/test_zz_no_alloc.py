@@ -1,0 +1,75 @@
+"""nrg_broaden_noalloc (static device scratch, no allocation) against the
+existing nrg_broaden entry point.  The file name sorts last so that it also
+runs after every other GPU test; it passes alone in a fresh process too."""
+import numpy as np
+import pytest
+
+from nrgplusplus_gb300 import api
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-6  # the FP32-exponential broadening's tolerance (k_broaden)
+
+
+def _histogram(nbins, seed):
+    """FDM-like histogram: log-spaced bin energies in [1e-10, 10], most bins
+    empty, weights spanning several decades."""
+    rng = np.random.default_rng(seed)
+    e = np.exp(np.linspace(np.log(1e-10), np.log(10.0), nbins))
+    w = 10.0 ** rng.uniform(-12, -1, nbins)
+    w[rng.random(nbins) < 0.7] = 0.0
+    return e, w
+
+
+@pytest.fixture(scope="module")
+def torch_cuda():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return torch
+
+
+@pytest.mark.parametrize("nbins", [100000, api.BROADEN_NOALLOC_MAX_BINS])
+def test_noalloc_broaden_matches_broaden(gpu_engine, torch_cuda, nbins):
+    torch = torch_cuda
+    e, w = _histogram(nbins, 11)
+    om = np.logspace(-8, 0, 801)
+    ref = gpu_engine.broaden(e, w, om, 0.6)
+    de = torch.tensor(e, dtype=torch.float64, device="cuda")
+    dw = torch.tensor(w, dtype=torch.float64, device="cuda")
+    dom = torch.tensor(om, dtype=torch.float64, device="cuda")
+    dout = torch.empty(om.size, dtype=torch.float64, device="cuda")
+    stream = torch.cuda.current_stream().cuda_stream
+
+    def call():
+        api.broaden_noalloc(de.data_ptr(), dw.data_ptr(), nbins, dom.data_ptr(), om.size, 0.6,
+                            dout.data_ptr(), stream)
+
+    def once():
+        dout.fill_(float("nan"))
+        call()
+        torch.cuda.synchronize()
+        return dout.cpu().numpy()
+
+    # first pass: the scratch address lookup of the first call per device and
+    # the lazy loading of the test's own torch kernels happen here
+    once()
+    free0 = torch.cuda.mem_get_info()[0]
+    outs = [once(), once()]  # two calls in a row
+    assert torch.cuda.mem_get_info()[0] == free0  # nothing allocated
+    scale = np.abs(ref).max()
+    assert scale > 0
+    for o in outs:
+        assert np.all(np.isfinite(o))
+        assert np.abs(o - ref).max() <= RTOL * scale
+    assert np.array_equal(outs[0], outs[1])
+
+
+def test_noalloc_broaden_rejects_oversize(torch_cuda):
+    torch = torch_cuda
+    buf = torch.zeros(16, dtype=torch.float64, device="cuda")
+    p = buf.data_ptr()
+    # rejected on the host before any launch
+    with pytest.raises(api.NrgError) as ei:
+        api.broaden_noalloc(p, p, api.BROADEN_NOALLOC_MAX_BINS + 1, p, 16, 0.6, p, 0)
+    assert ei.value.code == 1 and "exceeds the static scratch" in str(ei.value)

@@ -494,7 +494,11 @@ static void mixed_eigensolve(nrg_engine *e, std::vector<DevBlock *> &blks, int m
   float *wbase = static_cast<float *>(mw->ptr);
   // FP32 solve: eigenvectors (as FP64) into X0
   std::vector<EigBlock> eb(nb);
-  std::vector<int4> bt_tiles;
+  std::vector<int2> bt_tiles;
+  int tw = 64, panel = 1;
+  if (!reflect_config(max_n, &tw, &panel))
+    fail(NRG_E_ARG, "block dimension " + std::to_string(max_n) + " exceeds the mixed-precision limit " +
+                        std::to_string(reflect_max_n()));
   for (size_t b = 0; b < nb; ++b) {
     eb[b] = EigBlock{};
     eb[b].H = blks[b]->H;
@@ -506,9 +510,7 @@ static void mixed_eigensolve(nrg_engine *e, std::vector<DevBlock *> &blks, int m
     eb[b].n = blks[b]->n;
     eb[b].ld = blks[b]->ld;
     eb[b].ldu = blks[b]->ld;
-    const int nt = (blks[b]->n + 63) / 64;
-    for (int tm = 0; tm < nt; ++tm)
-      for (int tn = 0; tn < nt; ++tn) bt_tiles.push_back(make_int4(int(b), tm, tn, 0));
+    for (int tn = 0; tn < (blks[b]->n + tw - 1) / tw; ++tn) bt_tiles.push_back(make_int2(int(b), tn));
   }
   std::vector<int> stat(nb + 1, 0);
   std::vector<RefineBlock> rb(nb);
@@ -525,12 +527,12 @@ static void mixed_eigensolve(nrg_engine *e, std::vector<DevBlock *> &blks, int m
     post_launch("eigensolve f32");
   }
   {
-    double f = 0;
+    double f = 0;  // applying the reflectors: 2 n^3 per block
     for (auto &x : eb) f += 2.0 * double(x.n) * x.n * x.n;
-    Prof pf(e, "k_backtransform", f);
-    launch_backtransform(at<EigBlock>(dp, oeb), at<int4>(dp, obt), int(bt_tiles.size()), s);
+    Prof pf(e, "k_reflect", f);
+    launch_reflect(at<EigBlock>(dp, oeb), at<int2>(dp, obt), int(bt_tiles.size()), max_n, tw, panel, s);
     count_launch(e);
-    post_launch("backtransform");
+    post_launch("reflect");
   }
   int cur = 0;
   // digit planes for the tensor-core GEMMs (H once, X / Y / E per step)

@@ -82,15 +82,18 @@ struct Ctl {
 };
 
 // Householder reduction of a (n x n, leading dimension lda, either memory
-// space) to tridiagonal form and accumulation of the orthogonal transform:
-// on return a = Q, d = diagonal, e[i] = coupling of i-1 and i (e[0] = 0).
+// space) to tridiagonal form.  Step i (n-1 down to 1) applies the reflector
+// P_i = I - u u^T / h with u in row i, entries 0..i-1 (scaled; the scale
+// cancels in P_i), h in d[i] (0: no reflector); e[i] = coupling of i-1 and i
+// (e[0] = 0).  On return the diagonal of T is a(i, i), so
+//     A = Q T Q^T,   Q = P_{n-1} P_{n-2} ... P_1.
+// With store_uh, u / h is also written to column i (used by tred2_accumulate).
 // d, e, u, p: shared arrays of n.
 template <typename T>
-__device__ void tred2_acc(T *a, int lda, int n, T *d, T *e, T *u, T *p, T *red) {
+__device__ void tred2_reduce(T *a, int lda, int n, T *d, T *e, T *u, T *p, T *red, bool store_uh) {
   const int tid = threadIdx.x;
   const int warp = tid >> 5, lane = tid & 31;
 #define A(i, j) a[int64_t(i) * lda + (j)]
-  // ---------------- 1. Householder tridiagonalisation
   for (int i = n - 1; i >= 1; --i) {
     const int l = i - 1;
     T scale = T(0);
@@ -128,7 +131,7 @@ __device__ void tred2_acc(T *a, int lda, int n, T *d, T *e, T *u, T *p, T *red) 
       s = warp_sum(s);
       if (lane == 0) {
         p[j] = s / h;
-        A(j, i) = u[j] / h;
+        if (store_uh) A(j, i) = u[j] / h;
       }
     }
     __syncthreads();
@@ -149,7 +152,16 @@ __device__ void tred2_acc(T *a, int lda, int n, T *d, T *e, T *u, T *p, T *red) 
   }
   if (tid == 0) { d[0] = T(0); e[0] = T(0); }
   __syncthreads();
-  // ---------------- 2. accumulate Q
+#undef A
+}
+
+// Accumulation of Q from the reflectors left by tred2_reduce(store_uh):
+// on return a = Q and d = the diagonal of T.
+template <typename T>
+__device__ void tred2_accumulate(T *a, int lda, int n, T *d, T *p) {
+  const int tid = threadIdx.x;
+  const int warp = tid >> 5, lane = tid & 31;
+#define A(i, j) a[int64_t(i) * lda + (j)]
   for (int i = 0; i < n; ++i) {
     const int l = i - 1;
     const bool apply = (d[i] != T(0));
@@ -305,7 +317,7 @@ __device__ void write_sorted(const T *a, int lda, int n, const T *d, int *rank, 
 
 template <typename T>
 __device__ void carve(char *smem, int n, bool matrix_in_smem, T *&amat, T *&d, T *&e, T *&u, T *&p,
-                      T *&red, int *&rank, Ctl *&ctl) {
+                      T *&red, int *&rank, Ctl *&ctl, char **scratch = nullptr) {
   size_t off = 0;
   auto take = [&](size_t bytes) {
     char *q = smem + off;
@@ -319,6 +331,7 @@ __device__ void carve(char *smem, int n, bool matrix_in_smem, T *&amat, T *&d, T
   u = reinterpret_cast<T *>(take(sizeof(T) * n));
   p = reinterpret_cast<T *>(take(sizeof(T) * n));
   rank = reinterpret_cast<int *>(u);  // reused after the solve
+  if (scratch) *scratch = smem + off;  // the matrix area (free once it is reduced) and beyond
   amat = matrix_in_smem ? reinterpret_cast<T *>(take(sizeof(T) * size_t(n) * (n + 1))) : nullptr;
 }
 
@@ -353,7 +366,8 @@ k_eig(const EigBlock *__restrict__ blocks, int max_n_smem, int *status) {
     }
   }
   __syncthreads();
-  tred2_acc<T>(a, lda, n, d, e, u, p, red);
+  tred2_reduce<T>(a, lda, n, d, e, u, p, red, true);
+  tred2_accumulate<T>(a, lda, n, d, p);
   ql_vectors<T>(a, lda, n, d, e, u, p, ctl);
   __syncthreads();
   if (ctl->err) {
@@ -364,15 +378,17 @@ k_eig(const EigBlock *__restrict__ blocks, int max_n_smem, int *status) {
 }
 
 // ------------------------------------------------------------------------
-// FP32 first stage of the mixed path: Householder (tred2_acc) as above, then
-// the tridiagonal problem without the sequential QL chain:
+// FP32 first stage of the mixed path: the Householder reduction
+// (tred2_reduce, reflectors kept instead of forming Q), then the tridiagonal
+// problem without the sequential QL chain:
 //   * Sturm-sequence bisection, one thread per eigenvalue (all in parallel);
 //   * inverse iteration, one thread per eigenvector (tridiagonal LU solve,
 //     vectors stored column-wise so every step is a coalesced row access);
 //   * near-degenerate clusters (gaps <= 1e-3 |T|) redone one warp per
 //     cluster, re-orthogonalising each new iterate against the cluster's
 //     earlier vectors (the classic inverse-iteration/Gram-Schmidt scheme);
-//   * the back-transform X = Q V is a separate tiled kernel (k_backtransform).
+//   * the back-transform X = Q V applies the reflectors to V in a separate
+//     multi-CTA kernel (k_reflect).
 // Accuracy is FP32 (~1e-6); the FP64-accurate refinement follows.
 
 constexpr float kClusterGap = 1e-3f;
@@ -449,7 +465,7 @@ __device__ float inv_solve(const float *d, const float *e, int n, float lam, flo
 }
 
 __global__ void __launch_bounds__(kThreads, 1)
-k_eig_bi(const EigBlock *__restrict__ blocks, int max_n_smem) {
+k_eig_bi(const EigBlock *__restrict__ blocks, int max_n_smem, int smem_total) {
   extern __shared__ __align__(16) char smem[];
   const EigBlock B = blocks[blockIdx.x];
   const int n = B.n;
@@ -458,7 +474,8 @@ k_eig_bi(const EigBlock *__restrict__ blocks, int max_n_smem) {
   float *amat, *d, *e, *u, *p, *red;
   int *rank;
   Ctl *ctl;
-  carve<float>(smem, n, in_smem, amat, d, e, u, p, red, rank, ctl);
+  char *scratch;
+  carve<float>(smem, n, in_smem, amat, d, e, u, p, red, rank, ctl, &scratch);
   float *a = in_smem ? amat : B.W;
   const int lda = in_smem ? n + 1 : B.ld;
   for (int64_t idx = threadIdx.x; idx < int64_t(n) * n; idx += kThreads) {
@@ -466,11 +483,19 @@ k_eig_bi(const EigBlock *__restrict__ blocks, int max_n_smem) {
     a[int64_t(r) * lda + c] = float(B.H[int64_t(r) * B.ld + c]);
   }
   __syncthreads();
-  tred2_acc<float>(a, lda, n, d, e, u, p, red);
-  if (in_smem) {  // Q out to its global buffer for the back-transform
+  tred2_reduce<float>(a, lda, n, d, e, u, p, red, false);
+  // T's diagonal into d; h_i (0: no reflector) onto the diagonal of the
+  // reflector matrix, which k_reflect reads from the block's W buffer
+  for (int i = threadIdx.x; i < n; i += kThreads) {
+    const float h = (i == 0) ? 0.f : d[i];
+    d[i] = a[int64_t(i) * lda + i];
+    a[int64_t(i) * lda + i] = h;
+  }
+  __syncthreads();
+  if (in_smem) {  // reflectors (lower triangle and diagonal) out to W
     for (int64_t idx = threadIdx.x; idx < int64_t(n) * n; idx += kThreads) {
       const int r = int(idx / n), c = int(idx - int64_t(r) * n);
-      B.W[int64_t(r) * B.ld + c] = a[int64_t(r) * lda + c];
+      if (c <= r) B.W[int64_t(r) * B.ld + c] = a[int64_t(r) * lda + c];
     }
   }
   // Gershgorin interval and the norm used for pivots and cluster gaps
@@ -527,27 +552,50 @@ k_eig_bi(const EigBlock *__restrict__ blocks, int max_n_smem) {
   __syncthreads();
   const int ncl = ctl->m;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  for (int q = warp; q < ncl; q += kWarps) {
-    const int c0 = cl[2 * q], c1 = cl[2 * q + 1];
-    for (int j = c0; j < c1; ++j) {
-      for (int rep = 0; rep < 2; ++rep) {
-        if (lane == 0) inv_solve(d, e, n, lam[j], pivmin, 1.f, B.V, B.Bt, B.ld, j);
+  // Each warp iterates its clusters' members in shared memory (the member x
+  // and its LU pivots b: 2n floats per warp, in the area the matrix used),
+  // so the sequential solves run at shared-memory latency.  Without room for
+  // one warp's pair the member is iterated in place in V / Bt.
+  const size_t avail = size_t(smem_total) - size_t(scratch - smem);
+  int nw = int(avail / (sizeof(float) * 2 * size_t(n)));
+  const bool staged = nw > 0;
+  if (nw > kWarps || !staged) nw = kWarps;
+  if (warp < nw) {
+    for (int q = warp; q < ncl; q += nw) {
+      const int c0 = cl[2 * q], c1 = cl[2 * q + 1];
+      for (int j = c0; j < c1; ++j) {
+        float *xv, *bv;
+        int xs;
+        if (staged) {
+          xv = reinterpret_cast<float *>(scratch) + size_t(warp) * 2 * n;
+          bv = xv + n;
+          xs = 1;
+          for (int i = lane; i < n; i += 32) xv[i] = B.V[int64_t(i) * B.ld + j];
+        } else {
+          xv = B.V + j;
+          bv = B.Bt + j;
+          xs = B.ld;
+        }
         __syncwarp();
-        for (int k = c0; k < j; ++k) {
-          float dot = 0.f;
-          for (int i = lane; i < n; i += 32) dot += B.V[int64_t(i) * B.ld + k] * B.V[int64_t(i) * B.ld + j];
-          dot = warp_sum(dot);
-          for (int i = lane; i < n; i += 32) B.V[int64_t(i) * B.ld + j] -= dot * B.V[int64_t(i) * B.ld + k];
+        for (int rep = 0; rep < 2; ++rep) {
+          if (lane == 0) inv_solve(d, e, n, lam[j], pivmin, 1.f, xv, bv, xs, 0);
+          __syncwarp();
+          for (int k = c0; k < j; ++k) {  // earlier members are final in V
+            float dot = 0.f;
+            for (int i = lane; i < n; i += 32) dot += B.V[int64_t(i) * B.ld + k] * xv[int64_t(i) * xs];
+            dot = warp_sum(dot);
+            for (int i = lane; i < n; i += 32) xv[int64_t(i) * xs] -= dot * B.V[int64_t(i) * B.ld + k];
+            __syncwarp();
+          }
+          float nrm = 0.f;
+          for (int i = lane; i < n; i += 32) nrm += xv[int64_t(i) * xs] * xv[int64_t(i) * xs];
+          nrm = warp_sum(nrm);
+          const float sc = rsqrtf(fmaxf(nrm, 1e-37f));
+          for (int i = lane; i < n; i += 32) xv[int64_t(i) * xs] *= sc;
           __syncwarp();
         }
-        float nrm = 0.f;
-        for (int i = lane; i < n; i += 32) {
-          const float v = B.V[int64_t(i) * B.ld + j];
-          nrm += v * v;
-        }
-        nrm = warp_sum(nrm);
-        const float sc = rsqrtf(fmaxf(nrm, 1e-37f));
-        for (int i = lane; i < n; i += 32) B.V[int64_t(i) * B.ld + j] *= sc;
+        if (staged)
+          for (int i = lane; i < n; i += 32) B.V[int64_t(i) * B.ld + j] = xv[i];
         __syncwarp();
       }
     }
@@ -555,53 +603,76 @@ k_eig_bi(const EigBlock *__restrict__ blocks, int max_n_smem) {
   for (int j = threadIdx.x; j < n; j += kThreads) B.E[j] = double(lam[j]);
 }
 
-// X = Q V for every block (FP32 SIMT, 64 x 64 tiles, 4 x 4 per thread);
-// the result is written in FP64 as the first eigenvector estimate.
+// X = Q V for every block, Q = P_{n-1} ... P_1 from the reflectors k_eig_bi
+// left in W (row i: u_i in entries 0..i-1, h_i on the diagonal, 0 = none):
+// the reflectors are applied to X = V in the order P_1, P_2, ..., P_{n-1}.
+// One CTA owns TW columns of one block in shared memory (FP32) and each warp
+// TW / 8 of them, so a reflector needs no CTA barrier: a warp forms u^T x for
+// its columns with lane-strided sums and one shuffle reduction each, then
+// updates them.  Reflector rows are staged in panels of `panel` rows (one
+// barrier per panel).  The result is written in FP64 as the first
+// eigenvector estimate.
+template <int TW>
 __global__ void __launch_bounds__(256)
-k_backtransform(const EigBlock *__restrict__ blocks, const int4 *__restrict__ tiles) {
-  __shared__ float As[16][65];
-  __shared__ float Bs[16][65];
-  const int4 t = tiles[blockIdx.x];
+k_reflect(const EigBlock *__restrict__ blocks, const int2 *__restrict__ tiles, int panel) {
+  constexpr int CPW = TW / 8;  // columns per warp
+  constexpr int XP = TW + 1;   // odd row pitch: lane-strided rows hit distinct banks
+  extern __shared__ __align__(16) float rsm[];
+  const int2 t = tiles[blockIdx.x];
   const EigBlock B = blocks[t.x];
-  const int n = B.n, m0 = t.y * 64, n0 = t.z * 64;
-  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-  float acc[4][4] = {};
-  for (int k0 = 0; k0 < n; k0 += 16) {
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      const int idx = threadIdx.x + q * 256;
-      const int kk = idx & 15, mm = idx >> 4;  // Q tile 64 x 16, k fastest
-      const int gm = m0 + mm, gk = k0 + kk;
-      As[kk][mm] = (gm < n && gk < n) ? B.W[int64_t(gm) * B.ld + gk] : 0.f;
-      const int nn = idx & 63, k2 = idx >> 6;  // V tile 16 x 64, n fastest
-      const int gn = n0 + nn, gk2 = k0 + k2;
-      Bs[k2][nn] = (gn < n && gk2 < n) ? B.V[int64_t(gk2) * B.ld + gn] : 0.f;
+  const int n = B.n, c0 = t.y * TW;
+  const int nc = min(TW, n - c0);
+  float *X = rsm;                      // n x XP
+  float *Up = X + size_t(n) * XP;      // panel x n reflector rows
+  float *hs = Up + size_t(panel) * n;  // panel h values
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int cw = warp * CPW;
+  for (int64_t idx = tid; idx < int64_t(n) * TW; idx += 256) {
+    const int r = int(idx / TW), c = int(idx - int64_t(r) * TW);
+    X[int64_t(r) * XP + c] = (c < nc) ? B.V[int64_t(r) * B.ld + c0 + c] : 0.f;
+  }
+  for (int p0 = 1; p0 < n; p0 += panel) {
+    const int p1 = min(n, p0 + panel);
+    __syncthreads();  // previous panel consumed (and X loaded)
+    for (int q = p0 + warp; q < p1; q += 8) {
+      const float *src = B.W + int64_t(q) * B.ld;
+      float *dst = Up + size_t(q - p0) * n;
+      for (int k = lane; k < q; k += 32) dst[k] = src[k];
+      if (lane == 0) hs[q - p0] = src[q];
     }
     __syncthreads();
+    for (int q = p0; q < p1; ++q) {
+      const float h = hs[q - p0];
+      if (h == 0.f) continue;
+      const float *uq = Up + size_t(q - p0) * n;
+      float w[CPW];
 #pragma unroll
-    for (int kk = 0; kk < 16; ++kk) {
-      float av[4], bv[4];
+      for (int c = 0; c < CPW; ++c) w[c] = 0.f;
+      for (int k = lane; k < q; k += 32) {
+        const float uk = uq[k];
 #pragma unroll
-      for (int i = 0; i < 4; ++i) av[i] = As[kk][ty + 16 * i];
+        for (int c = 0; c < CPW; ++c) w[c] = fmaf(uk, X[k * XP + cw + c], w[c]);
+      }
 #pragma unroll
-      for (int j = 0; j < 4; ++j) bv[j] = Bs[kk][tx + 16 * j];
+      for (int c = 0; c < CPW; ++c) w[c] = warp_sum(w[c]) / h;
+      for (int k = lane; k < q; k += 32) {
+        const float uk = uq[k];
 #pragma unroll
-      for (int i = 0; i < 4; ++i)
-#pragma unroll
-        for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(av[i], bv[j], acc[i][j]);
-    }
-    __syncthreads();
-  }
-#pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    const int gm = m0 + ty + 16 * i;
-    if (gm >= n) continue;
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      const int gn = n0 + tx + 16 * j;
-      if (gn < n) B.U[int64_t(gm) * B.ldu + gn] = double(acc[i][j]);
+        for (int c = 0; c < CPW; ++c) X[k * XP + cw + c] = fmaf(-uk, w[c], X[k * XP + cw + c]);
+      }
     }
   }
+  __syncthreads();
+  for (int64_t idx = tid; idx < int64_t(n) * nc; idx += 256) {
+    const int r = int(idx / nc), c = int(idx - int64_t(r) * nc);
+    B.U[int64_t(r) * B.ldu + c0 + c] = double(X[int64_t(r) * XP + c]);
+  }
+}
+
+constexpr size_t kReflectSmem = 225 * 1024;
+
+size_t reflect_bytes(int n, int tw, int panel) {
+  return sizeof(float) * (size_t(n) * (tw + 1) + size_t(panel) * (n + 1)) + 64;
 }
 
 template <typename T> size_t smem_bytes(int n, bool in_smem) {
@@ -663,12 +734,47 @@ void launch_eig_bisect_f32(const EigBlock *blocks, int nblocks, int max_n, int m
   size_t bytes = smem_bytes<float>(max_n, max_n <= max_n_smem);
   if (max_n > max_n_smem) bytes = std::max(bytes, smem_bytes<float>(max_n_smem, true));
   if (bytes > size_t(kSmemBytes)) bytes = kSmemBytes;
-  k_eig_bi<<<nblocks, kThreads, bytes, s>>>(blocks, max_n_smem);
+  k_eig_bi<<<nblocks, kThreads, bytes, s>>>(blocks, max_n_smem, int(bytes));
 }
 
-void launch_backtransform(const EigBlock *blocks, const int4 *tiles, int ntiles, cudaStream_t s) {
+bool reflect_config(int max_n, int *tw, int *panel) {
+  for (int w = 64; w >= 8; w /= 2) {
+    if (reflect_bytes(max_n, w, 1) > kReflectSmem) continue;
+    int pn = 32;
+    while (pn > 1 && reflect_bytes(max_n, w, pn) > kReflectSmem) --pn;
+    *tw = w;
+    *panel = pn;
+    return true;
+  }
+  return false;
+}
+
+int reflect_max_n() {
+  int n = 8;
+  while (reflect_bytes(n + 1, 8, 1) <= kReflectSmem) ++n;
+  return n;
+}
+
+template <int TW> static void reflect_launch(const EigBlock *blocks, const int2 *tiles, int ntiles, int panel,
+                                             size_t bytes, cudaStream_t s) {
+  static bool cfg = false;
+  if (!cfg) {
+    cudaFuncSetAttribute(k_reflect<TW>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kReflectSmem));
+    cfg = true;
+  }
+  k_reflect<TW><<<ntiles, 256, bytes, s>>>(blocks, tiles, panel);
+}
+
+void launch_reflect(const EigBlock *blocks, const int2 *tiles, int ntiles, int max_n, int tw, int panel,
+                    cudaStream_t s) {
   if (ntiles == 0) return;
-  k_backtransform<<<ntiles, 256, 0, s>>>(blocks, tiles);
+  const size_t bytes = reflect_bytes(max_n, tw, panel);
+  switch (tw) {
+    case 64: reflect_launch<64>(blocks, tiles, ntiles, panel, bytes, s); break;
+    case 32: reflect_launch<32>(blocks, tiles, ntiles, panel, bytes, s); break;
+    case 16: reflect_launch<16>(blocks, tiles, ntiles, panel, bytes, s); break;
+    default: reflect_launch<8>(blocks, tiles, ntiles, panel, bytes, s); break;
+  }
 }
 void launch_eig_f32(const EigBlock *blocks, int nblocks, int max_n, int max_n_smem, int *status,
                     cudaStream_t s) {

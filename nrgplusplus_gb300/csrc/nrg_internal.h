@@ -47,17 +47,23 @@ struct EigBlock {
   double *H;          // input (destroyed when the block is solved in place)
   double *U;          // output eigenvectors as columns, row-major n x ldu
   double *E;          // output eigenvalues, ascending
-  float *W;           // FP32 workspace (n x ld): working matrix, then Q
+  float *W;           // FP32 workspace (n x ld): working matrix, then the reflectors
   float *V, *Bt;      // FP32 tridiagonal eigenvectors and LU pivots (n x ld)
   int n, ld, ldu, pad;
 };
 // FP32 bisection + inverse-iteration solver (mixed path first stage): writes
-// E (FP64) and Q into W, tridiagonal eigenvectors into V; then
-// launch_backtransform writes U = Q V (FP64).  tiles: (block, tile row,
-// tile col, 0) of 64 x 64 output tiles.
+// E (FP64), the Householder reflectors into W (row i: u_i in columns 0..i-1,
+// h_i on the diagonal) and the tridiagonal eigenvectors into V; then
+// launch_reflect writes U = Q V (FP64) by applying the reflectors to V.
+// reflect_config picks the column-tile width tw (64, 32, 16 or 8) and the
+// reflector panel for the largest block of a launch (false: too large);
+// tiles: (block, column tile of width tw).
 void launch_eig_bisect_f32(const EigBlock *blocks, int nblocks, int max_n, int max_n_smem,
                            cudaStream_t s);
-void launch_backtransform(const EigBlock *blocks, const int4 *tiles, int ntiles, cudaStream_t s);
+bool reflect_config(int max_n, int *tw, int *panel);
+int reflect_max_n();
+void launch_reflect(const EigBlock *blocks, const int2 *tiles, int ntiles, int max_n, int tw, int panel,
+                    cudaStream_t s);
 // FP64 Householder tridiagonalisation + implicit QL, one CTA per block.
 // status[b] != 0 if block b hit the QL iteration cap.
 // max_n: largest block of the launch; blocks with n <= max_n_smem are solved

@@ -214,7 +214,7 @@ def kernel_models():
         "k_gemm_f64": fp64,
         "k_eig_f64": fp64,
         "k_eig_bi_f32": ("fp32", FP32_PEAK_TFLOPS, "TFLOP/s", 1e-12, "nominal GB300 FP32",
-                         "(4/3) n^3 per block (Householder reduction + Q accumulation)"),
+                         "(4/3) n^3 per block (Householder reduction)"),
         "k_reflect": ("fp32", FP32_PEAK_TFLOPS, "TFLOP/s", 1e-12, "nominal GB300 FP32",
                       "2 n^3 per block (Householder reflectors applied to the tridiagonal eigenvectors)"),
         "k_gemm_oz": ("tensor", bf16, "TFLOP/s", OZ_PAIRS * 1e-12, bf16_src,

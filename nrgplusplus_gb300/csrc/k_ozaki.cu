@@ -11,9 +11,9 @@
 // sums while |sum| <= 2^24: grouping the pairs by d = p + q (d <= 7; the
 // dropped groups weigh below 2^-51 of the result scale) and accumulating each
 // group over at most 512 k-terms keeps every partial sum an exact integer.
-// The 8 group sums are combined once per output element and K-chunk in FP64
-// by Horner (h = G_0; h = 128 h + G_d), so the FP64 pipe does 8 FMAs per
-// output element instead of K.  The bf16 products use mma.sync m16n8k16 with
+// The 8 group sums are combined once per output element and K-chunk by an
+// integer Horner (h = G_0; h = 128 h + G_d) and one FP64 fma, so the FP64
+// pipe does a few operations per output element instead of K.  The bf16 products use mma.sync m16n8k16 with
 // FP32 accumulation; the result matches an FP64 GEMM to FP64 round-off.
 #include <cuda_bf16.h>
 
@@ -231,20 +231,57 @@ k_gemm_oz(const GemmTile *__restrict__ tiles, const OzGroup *__restrict__ groups
   const int wm = (warp & 3) * 16, wn = (warp >> 2) * 32;
   for (int i = tid; i < BM * BN; i += kThreads) Ct[i] = 0.0;
 
+  // Group sums of consecutive contributions (and K-chunks) that share the
+  // scale |alpha| 2^(eA+eB-61) stay in the same FP32 accumulators while their
+  // total depth is <= kChunkK (every partial sum stays an exact integer below
+  // 2^24); a negative alpha flips the sign bits of the A fragments.  The
+  // accumulators are folded into the FP64 tile only when the scale changes,
+  // the depth is used up, or the list ends.
+  float acc[kPlanes][4][4];
+#pragma unroll
+  for (int d = 0; d < kPlanes; ++d)
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+      for (int v = 0; v < 4; ++v) acc[d][j][v] = 0.f;
+  int kacc = 0;          // depth accumulated since the last fold
+  double acc_scale = 0;  // its scale
+
+  auto fold = [&]() {
+    // exact group sums -> FP64: 32-bit conversions, Horner over the groups in
+    // integers (groups 0-4 into hi <= 2^53, groups 5-7 into lo <= 2^39),
+    // then one FP64 fma per element
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        long long hi = __float2int_rz(acc[0][j][v]);
+#pragma unroll
+        for (int d = 1; d < 5; ++d) hi = hi * 128 + __float2int_rz(acc[d][j][v]);
+        long long lo = __float2int_rz(acc[5][j][v]);
+#pragma unroll
+        for (int d = 6; d < kPlanes; ++d) lo = lo * 128 + __float2int_rz(acc[d][j][v]);
+        const double h = fma(__ll2double_rn(hi), 2097152.0, __ll2double_rn(lo));  // 128^3
+        const int r = wm + (lane >> 2) + (v >> 1) * 8;
+        const int col = wn + j * 8 + (lane & 3) * 2 + (v & 1);
+        Ct[r * BN + col] = fma(acc_scale, h, Ct[r * BN + col]);
+#pragma unroll
+        for (int d = 0; d < kPlanes; ++d) acc[d][j][v] = 0.f;
+      }
+    kacc = 0;
+  };
+
   for (int c = g.c0; c < g.c1; ++c) {
     const OzContrib q = contribs[c];
     const bool ta = q.trans & 1, tb = (q.trans >> 1) & 1;
-    const double scale = q.alpha * scalbn(1.0, *q.A.exp + *q.B.exp - 61);
+    const double scale = fabs(q.alpha) * scalbn(1.0, *q.A.exp + *q.B.exp - 61);
+    const uint32_t neg = (q.alpha < 0.0) ? 0x80008000u : 0u;
     for (int kc = 0; kc < q.K; kc += kChunkK) {
       const int kend = min(q.K, kc + kChunkK);
       const int nst = (kend - kc + BK - 1) / BK;
-      float acc[kPlanes][4][4];
-#pragma unroll
-      for (int d = 0; d < kPlanes; ++d)
-#pragma unroll
-        for (int j = 0; j < 4; ++j)
-#pragma unroll
-          for (int v = 0; v < 4; ++v) acc[d][j][v] = 0.f;
+      if (kacc > 0 && (scale != acc_scale || kacc + (kend - kc) > kChunkK)) fold();
+      acc_scale = scale;
+      kacc += kend - kc;
       __syncthreads();  // previous users of both buffers are done
       stage_tiles(q, ta, tb, g.M, g.N, m0, n0, kc, kend, As0, Bs0);
       cp_async_commit();
@@ -276,6 +313,8 @@ k_gemm_oz(const GemmTile *__restrict__ tiles, const OzGroup *__restrict__ groups
               const __nv_bfloat16 *ptr = As + (p * BK + ks + (mi >> 1) * 8 + (lane & 7)) * kPitchMN + wm + (mi & 1) * 8;
               ldsm_x4_t(smem_u32(ptr), fa.a[p][0], fa.a[p][1], fa.a[p][2], fa.a[p][3]);
             }
+#pragma unroll
+            for (int x = 0; x < 4; ++x) fa.a[p][x] ^= neg;
           }
 #pragma unroll
           for (int qd = 0; qd < kPlanes; ++qd) {
@@ -308,25 +347,9 @@ k_gemm_oz(const GemmTile *__restrict__ tiles, const OzGroup *__restrict__ groups
         }
         __syncthreads();  // this buffer may be refilled by the next stage
       }
-      // exact group sums -> FP64: Horner over the groups in integers (groups
-      // 0-4 into hi <= 2^53, groups 5-7 into lo <= 2^39), then one FP64 fma
-#pragma unroll
-      for (int j = 0; j < 4; ++j)
-#pragma unroll
-        for (int v = 0; v < 4; ++v) {
-          long long hi = __float2ll_rz(acc[0][j][v]);
-#pragma unroll
-          for (int d = 1; d < 5; ++d) hi = hi * 128 + __float2ll_rz(acc[d][j][v]);
-          long long lo = __float2ll_rz(acc[5][j][v]);
-#pragma unroll
-          for (int d = 6; d < kPlanes; ++d) lo = lo * 128 + __float2ll_rz(acc[d][j][v]);
-          const double h = fma(__ll2double_rn(hi), 2097152.0, __ll2double_rn(lo));  // 128^3
-          const int r = wm + (lane >> 2) + (v >> 1) * 8;
-          const int col = wn + j * 8 + (lane & 3) * 2 + (v & 1);
-          Ct[r * BN + col] = fma(scale, h, Ct[r * BN + col]);
-        }
     }
   }
+  if (kacc > 0) fold();
   __syncthreads();
   for (int i = tid; i < BM * BN; i += kThreads) {
     const int r = i / BN, col = i - r * BN;

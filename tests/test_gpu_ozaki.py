@@ -29,3 +29,17 @@ def test_dgemm_tc_matches_fp64(gpu_engine, kind, ta, tb):
         ref = (A.T if ta else A) @ (B.T if tb else B)
         tol = K * 2.0 ** -52 * max(np.abs(A).max(), 1e-300) * max(np.abs(B).max(), 1e-300)
         assert np.abs(C - ref).max() <= tol, (kind, ta, tb, M, N, K, np.abs(C - ref).max(), tol)
+
+
+@pytest.mark.parametrize("alpha", [-1.0, -0.75, 3.0])
+def test_dgemm_tc_alpha(gpu_engine, alpha):
+    """Scaled and negated products (a negative alpha flips the sign bits of
+    the A digit planes inside the kernel)."""
+    rng = np.random.default_rng(5)
+    for M, N, K in SHAPES:
+        A = _mat(rng, M, K, "normal")
+        B = _mat(rng, K, N, "wide")
+        C = gpu_engine.dgemm_tc(A, B, False, False, alpha)
+        ref = alpha * (A @ B)
+        tol = abs(alpha) * K * 2.0 ** -52 * np.abs(A).max() * np.abs(B).max()
+        assert np.abs(C - ref).max() <= tol, (alpha, M, N, K, np.abs(C - ref).max(), tol)

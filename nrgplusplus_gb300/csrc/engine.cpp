@@ -470,13 +470,23 @@ constexpr double kClusterTau = 1e-4;  // relative gap below which levels form a 
 // QL (k_eig<float>), then kRefineSteps Ogita-Aishima Newton steps with
 // FP64-accurate grouped GEMMs and a final Rayleigh-Ritz pass with FP64
 // Jacobi on near-degenerate clusters (k_refine.cu).  Writes U and E of every
-// block; blocks whose cluster exceeds the in-kernel limit are re-solved with
-// the FP64 solver.  H is left intact.
-static void mixed_eigensolve(nrg_engine *e, std::vector<DevBlock *> &blks, int max_n,
-                             std::vector<DevPtr> &hold) {
+// block; blocks whose refinement did not converge are re-solved with the FP64
+// solver in a launch gated on the device by the refinement status, so no host
+// round trip is needed.  H is left intact (except in re-solved blocks too
+// large for shared memory, which the FP64 solver reduces in place).  Returns
+// the device status arrays
+// (in `hold`), which the caller reads at its next synchronisation.
+struct MixedStatus {
+  const int *refine = nullptr;  // per block: 0 ok, 2 re-solved in FP64
+  const int *fp64 = nullptr;    // per block: FP64 re-solve status (0 ok)
+  int nb = 0;
+};
+
+static MixedStatus mixed_eigensolve(nrg_engine *e, std::vector<DevBlock *> &blks, int max_n,
+                                    std::vector<DevPtr> &hold) {
   cudaStream_t s = e->stream;
   const size_t nb = blks.size();
-  if (nb == 0) return;
+  if (nb == 0) return {};
   int64_t sz = 0, esz = 0;
   std::vector<int64_t> off(nb), eoff(nb);
   for (size_t b = 0; b < nb; ++b) {
@@ -514,8 +524,18 @@ static void mixed_eigensolve(nrg_engine *e, std::vector<DevBlock *> &blks, int m
   }
   std::vector<int> stat(nb + 1, 0);
   std::vector<RefineBlock> rb(nb);
+  std::vector<EigBlock> eb64(nb);  // FP64 re-solve of flagged blocks, in place
+  for (size_t b = 0; b < nb; ++b) {
+    eb64[b] = EigBlock{};
+    eb64[b].H = blks[b]->H;
+    eb64[b].U = blks[b]->U;
+    eb64[b].E = blks[b]->E;
+    eb64[b].n = blks[b]->n;
+    eb64[b].ld = blks[b]->ld;
+    eb64[b].ldu = blks[b]->ld;
+  }
   Arena a;
-  size_t oeb = a.add(eb), ost = a.add(stat), obt = a.add(bt_tiles);
+  size_t oeb = a.add(eb), ost = a.add(stat), obt = a.add(bt_tiles), oeb64 = a.add(eb64), ost64 = a.add(stat);
   const size_t orb = a.add(rb);  // filled per step below (host copy re-uploaded)
   DevPtr dd;
   char *dp = a.push(e, dd);
@@ -626,38 +646,39 @@ static void mixed_eigensolve(nrg_engine *e, std::vector<DevBlock *> &blks, int m
     }
     cur = 1 - cur;
   }
-  check_cuda(cudaMemcpyAsync(stat.data(), dp + ost, nb * sizeof(int), cudaMemcpyDeviceToHost, s),
-             "refine status");
-  check_cuda(cudaStreamSynchronize(s), "refine");
-  std::vector<EigBlock> redo;
-  for (size_t b = 0; b < nb; ++b) {
-    if (stat[b] == 1) fail(NRG_E_EIG, "FP32 block eigensolver did not converge");
-    if (stat[b] == 2) {
-      EigBlock x{};
-      x.H = blks[b]->H;
-      x.U = blks[b]->U;
-      x.E = blks[b]->E;
-      x.n = blks[b]->n;
-      x.ld = blks[b]->ld;
-      x.ldu = blks[b]->ld;
-      redo.push_back(x);
+  {
+    Prof pf(e, "k_eig_f64_fallback");
+    launch_eig_f64(at<EigBlock>(dp, oeb64), int(nb), max_n, e->eig_smem_f64, at<int>(dp, ost64), s,
+                   at<int>(dp, ost));
+    count_launch(e);
+    post_launch("eigensolve f64 (refinement fallback)");
+  }
+  return MixedStatus{at<int>(dp, ost), at<int>(dp, ost64), int(nb)};
+}
+
+// Host copies of a MixedStatus, filled by enqueue() and checked after the
+// caller's synchronisation.
+struct MixedCheck {
+  std::vector<int> refine, fp64;
+  void enqueue(const MixedStatus &m, cudaStream_t s) {
+    refine.assign(m.nb, 0);
+    fp64.assign(m.nb, 0);
+    if (m.nb == 0) return;
+    check_cuda(cudaMemcpyAsync(refine.data(), m.refine, m.nb * sizeof(int), cudaMemcpyDeviceToHost, s),
+               "refine status");
+    check_cuda(cudaMemcpyAsync(fp64.data(), m.fp64, m.nb * sizeof(int), cudaMemcpyDeviceToHost, s),
+               "fallback status");
+  }
+  void check(nrg_engine *e) const {
+    for (size_t b = 0; b < refine.size(); ++b) {
+      if (refine[b] == 1) fail(NRG_E_EIG, "FP32 block eigensolver did not converge");
+      if (refine[b] == 2) {
+        ++e->fallback_blocks;
+        if (fp64[b]) fail(NRG_E_EIG, "block eigensolver did not converge (FP64 re-solve)");
+      }
     }
   }
-  if (!redo.empty()) {  // large near-degenerate cluster: FP64 solve of that block
-    Arena r;
-    std::vector<int> st2(redo.size() + 1, 0);
-    size_t o1 = r.add(redo), o2 = r.add(st2);
-    DevPtr rd;
-    char *rp = r.push(e, rd);
-    hold.push_back(rd);
-    int mn = 0;
-    for (auto &x : redo) mn = std::max(mn, x.n);
-    launch_eig_f64(at<EigBlock>(rp, o1), int(redo.size()), mn, e->eig_smem_f64, at<int>(rp, o2), s);
-    count_launch(e);
-    post_launch("eigensolve f64 (cluster fallback)");
-    e->fallback_blocks += redo.size();
-  }
-}
+};
 
 static void batch_add_site(nrg_run *const *runs, int nruns, const double *t, int nt,
                            const double *rescale) {
@@ -842,6 +863,7 @@ static void batch_add_site(nrg_run *const *runs, int nruns, const double *t, int
   if (max_n > eig_max_n_f64())
     fail(NRG_E_ARG, "block dimension " + std::to_string(max_n) + " exceeds the solver limit " +
                         std::to_string(eig_max_n_f64()));
+  MixedStatus mstat;
   if (e->precision == NRG_PREC_FP64) {
     Prof pf(e, "k_eig_f64", eig_flops(eblk_sorted));
     launch_eig_f64(at<EigBlock>(d, o_eblk), int(eblk_sorted.size()), max_n, e->eig_smem_f64,
@@ -855,7 +877,7 @@ static void batch_add_site(nrg_run *const *runs, int nruns, const double *t, int
     for (auto &st : steps)
       for (auto &db : st.site->blocks) blks.push_back(&db);
     std::stable_sort(blks.begin(), blks.end(), [](DevBlock *a, DevBlock *b) { return a->n > b->n; });
-    mixed_eigensolve(e, blks, max_n, hold);
+    mstat = mixed_eigensolve(e, blks, max_n, hold);
     if (e->ozaki & 2) {  // digit planes of every new U: operands of all rotations of this site
       std::vector<MatRef> um;
       for (auto &st : steps)
@@ -889,6 +911,8 @@ static void batch_add_site(nrg_run *const *runs, int nruns, const double *t, int
                              cudaMemcpyDeviceToHost, s), "result D2H");
   check_cuda(cudaMemcpyAsync(stat.data(), d + o_stat, eblk_sorted.size() * sizeof(int),
                              cudaMemcpyDeviceToHost, s), "status D2H");
+  MixedCheck mcheck;
+  mcheck.enqueue(mstat, s);
   std::vector<std::vector<double>> sorted(nruns), evals(nruns);
   for (int i = 0; i < nruns; ++i) {
     RunStep &st = steps[i];
@@ -902,6 +926,7 @@ static void batch_add_site(nrg_run *const *runs, int nruns, const double *t, int
                "eigenvalues D2H");
   }
   check_cuda(cudaStreamSynchronize(s), "site step");
+  mcheck.check(e);
   for (size_t b = 0; b < eblk_sorted.size(); ++b)
     if (stat[b]) fail(NRG_E_EIG, "block eigensolver did not converge (n = " +
                                      std::to_string(eblk_sorted[b].n) + ")");
@@ -1140,7 +1165,10 @@ extern "C" int nrg_eigh_batched(nrg_engine *e, int nblk, const int *dims, const 
       std::vector<DevBlock *> ptrs;
       for (auto &b : blocks) ptrs.push_back(&b);
       std::stable_sort(ptrs.begin(), ptrs.end(), [](DevBlock *x, DevBlock *y) { return x->n > y->n; });
-      mixed_eigensolve(e, ptrs, max_n, hold);
+      MixedCheck mc;
+      mc.enqueue(mixed_eigensolve(e, ptrs, max_n, hold), s);
+      check_cuda(cudaStreamSynchronize(s), "eigh");
+      mc.check(e);
     }
     eo = 0;
     io = 0;

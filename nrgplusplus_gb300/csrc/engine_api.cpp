@@ -443,7 +443,9 @@ static void fdm_calc(nrg_fdm *f, double scale) {
   f->reduced_k = std::move(red_k);
   f->have_reduced = true;
   f->last = false;
-  check_cuda(cudaStreamSynchronize(s), "fdm step");
+  // no synchronisation: every buffer above is freed stream-ordered and every
+  // host array was staged by its copy call, so the host may queue the next
+  // shell while this one runs (errors surface at the next synchronising call)
 }
 
 }  // namespace nrg

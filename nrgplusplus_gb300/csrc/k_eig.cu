@@ -337,8 +337,9 @@ __device__ void carve(char *smem, int n, bool matrix_in_smem, T *&amat, T *&d, T
 
 template <typename T>
 __global__ void __launch_bounds__(kThreads, 1)
-k_eig(const EigBlock *__restrict__ blocks, int max_n_smem, int *status) {
+k_eig(const EigBlock *__restrict__ blocks, int max_n_smem, int *status, const int *gate) {
   extern __shared__ __align__(16) char smem[];
+  if (gate && gate[blockIdx.x] != 2) return;  // re-solve only the flagged blocks
   const EigBlock B = blocks[blockIdx.x];
   const int n = B.n;
   if (n == 0) return;
@@ -689,7 +690,7 @@ template <typename T> int smem_limit() {
 
 template <typename T>
 void launch(const EigBlock *blocks, int nblocks, int max_n, int max_n_smem, int *status,
-            cudaStream_t s) {
+            cudaStream_t s, const int *gate = nullptr) {
   if (nblocks == 0) return;
   static bool configured = false;
   if (!configured) {
@@ -700,7 +701,7 @@ void launch(const EigBlock *blocks, int nblocks, int max_n, int max_n_smem, int 
   size_t bytes = smem_bytes<T>(max_n, max_n <= max_n_smem);
   if (max_n > max_n_smem) bytes = std::max(bytes, smem_bytes<T>(max_n_smem, true));
   if (bytes > size_t(kSmemBytes)) bytes = kSmemBytes;
-  k_eig<T><<<nblocks, kThreads, bytes, s>>>(blocks, max_n_smem, status);
+  k_eig<T><<<nblocks, kThreads, bytes, s>>>(blocks, max_n_smem, status, gate);
 }
 
 }  // namespace
@@ -719,8 +720,8 @@ int eig_max_n_f64() { return max_block<double>(); }
 int eig_max_n_f32() { return max_block<float>(); }
 
 void launch_eig_f64(const EigBlock *blocks, int nblocks, int max_n, int max_n_smem, int *status,
-                    cudaStream_t s) {
-  launch<double>(blocks, nblocks, max_n, max_n_smem, status, s);
+                    cudaStream_t s, const int *gate) {
+  launch<double>(blocks, nblocks, max_n, max_n_smem, status, s, gate);
 }
 
 void launch_eig_bisect_f32(const EigBlock *blocks, int nblocks, int max_n, int max_n_smem,

@@ -67,9 +67,10 @@ void launch_reflect(const EigBlock *blocks, const int2 *tiles, int ntiles, int m
 // FP64 Householder tridiagonalisation + implicit QL, one CTA per block.
 // status[b] != 0 if block b hit the QL iteration cap.
 // max_n: largest block of the launch; blocks with n <= max_n_smem are solved
-// in shared memory, larger ones in their own global buffer.
+// in shared memory, larger ones in their own global buffer.  With a gate,
+// only blocks with gate[b] == 2 are solved (the others return at once).
 void launch_eig_f64(const EigBlock *blocks, int nblocks, int max_n, int max_n_smem, int *status,
-                    cudaStream_t s);
+                    cudaStream_t s, const int *gate = nullptr);
 // Same algorithm in FP32 (mixed path first stage); writes U and E in FP64.
 void launch_eig_f32(const EigBlock *blocks, int nblocks, int max_n, int max_n_smem, int *status,
                     cudaStream_t s);

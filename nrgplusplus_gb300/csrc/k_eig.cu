@@ -81,6 +81,76 @@ struct Ctl {
   int m, istop, done, err;
 };
 
+// One reduction step's matrix-vector product p_j = (A u)_j / h (j <= l) and
+// rank-2 update A -= u q^T + q u^T for an FP32 matrix in global memory with
+// an even leading dimension: every warp streams four rows at a time in 8-byte
+// column pairs, so each lane keeps several independent L2 loads in flight
+// (one row per warp is latency bound out of L2).  The last pair may cover
+// column l + 1, which the caller neutralises with u[l+1] = q[l+1] = 0.
+__device__ void matvec_rows_f2(const float *a, int lda, int l, const float *u, float *p, float h) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int npair = (l + 2) >> 1;
+  const float2 *u2 = reinterpret_cast<const float2 *>(u);
+  for (int j0 = warp; j0 <= l; j0 += 4 * kWarps) {
+    const float2 *row[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      const int j = j0 + r * kWarps;
+      row[r] = reinterpret_cast<const float2 *>(a + int64_t(j <= l ? j : j0) * lda);
+    }
+    float s[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll 2
+    for (int c = lane; c < npair; c += 32) {
+      float2 v[4];
+#pragma unroll
+      for (int r = 0; r < 4; ++r) v[r] = row[r][c];
+      const float2 uu = u2[c];
+#pragma unroll
+      for (int r = 0; r < 4; ++r) s[r] = fmaf(v[r].x, uu.x, fmaf(v[r].y, uu.y, s[r]));
+    }
+#pragma unroll
+    for (int r = 0; r < 4; ++r) s[r] = warp_sum(s[r]);
+    if (lane == 0)
+#pragma unroll
+      for (int r = 0; r < 4; ++r)
+        if (j0 + r * kWarps <= l) p[j0 + r * kWarps] = s[r] / h;
+  }
+}
+
+__device__ void update_rows_f2(float *a, int lda, int l, const float *u, const float *q) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int npair = (l + 2) >> 1;
+  const float2 *u2 = reinterpret_cast<const float2 *>(u);
+  const float2 *q2 = reinterpret_cast<const float2 *>(q);
+  for (int j0 = warp; j0 <= l; j0 += 4 * kWarps) {
+    float2 *row[4];
+    float uj[4], qj[4];
+    bool ok[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      const int j = j0 + r * kWarps;
+      ok[r] = j <= l;
+      row[r] = reinterpret_cast<float2 *>(a + int64_t(ok[r] ? j : j0) * lda);
+      uj[r] = ok[r] ? u[j] : 0.f;
+      qj[r] = ok[r] ? q[j] : 0.f;
+    }
+    for (int c = lane; c < npair; c += 32) {
+      float2 v[4];
+#pragma unroll
+      for (int r = 0; r < 4; ++r) v[r] = row[r][c];
+      const float2 uu = u2[c], qq = q2[c];
+#pragma unroll
+      for (int r = 0; r < 4; ++r) {
+        v[r].x -= uj[r] * qq.x + qj[r] * uu.x;
+        v[r].y -= uj[r] * qq.y + qj[r] * uu.y;
+      }
+#pragma unroll
+      for (int r = 0; r < 4; ++r)
+        if (ok[r]) row[r][c] = v[r];
+    }
+  }
+}
+
 // Householder reduction of a (n x n, leading dimension lda, either memory
 // space) to tridiagonal form.  Step i (n-1 down to 1) applies the reflector
 // P_i = I - u u^T / h with u in row i, entries 0..i-1 (scaled; the scale
@@ -88,9 +158,11 @@ struct Ctl {
 // (e[0] = 0).  On return the diagonal of T is a(i, i), so
 //     A = Q T Q^T,   Q = P_{n-1} P_{n-2} ... P_1.
 // With store_uh, u / h is also written to column i (used by tred2_accumulate).
-// d, e, u, p: shared arrays of n.
+// wide (FP32, global memory, even lda, no store_uh): the streaming
+// matvec_rows_f2 / update_rows_f2 forms.  d, e, u, p: shared arrays of n.
 template <typename T>
-__device__ void tred2_reduce(T *a, int lda, int n, T *d, T *e, T *u, T *p, T *red, bool store_uh) {
+__device__ void tred2_reduce(T *a, int lda, int n, T *d, T *e, T *u, T *p, T *red, bool store_uh,
+                             bool wide = false) {
   const int tid = threadIdx.x;
   const int warp = tid >> 5, lane = tid & 31;
 #define A(i, j) a[int64_t(i) * lda + (j)]
@@ -119,11 +191,29 @@ __device__ void tred2_reduce(T *a, int lda, int n, T *d, T *e, T *u, T *p, T *re
       h -= f * g;
       A(i, l) = f - g;
       u[l] = f - g;
+      u[i] = T(0);  // column l + 1 = i of the wide forms' last pair
+      p[i] = T(0);
       red[kWarps] = h;
     }
     __syncthreads();
     h = red[kWarps];
     __syncthreads();
+    if constexpr (sizeof(T) == sizeof(float)) {
+      if (wide) {
+        matvec_rows_f2(a, lda, l, u, p, h);
+        __syncthreads();
+        T fs = T(0);
+        for (int j = tid; j <= l; j += kThreads) fs += p[j] * u[j];
+        const T f = block_sum(fs, red);
+        const T hh = f / (h + h);
+        for (int j = tid; j <= l; j += kThreads) p[j] = p[j] - hh * u[j];  // q
+        __syncthreads();
+        update_rows_f2(a, lda, l, u, p);
+        if (tid == 0) d[i] = h;
+        __syncthreads();
+        continue;
+      }
+    }
     // p_j = (A u)_j / h, and u_j / h stored in column i
     for (int j = warp; j <= l; j += kWarps) {
       T s = T(0);
@@ -406,13 +496,18 @@ __device__ __forceinline__ float block_minf(float v, float *red) {
   return m;
 }
 
-// number of eigenvalues of the tridiagonal (d, e) below x
+// number of eigenvalues of the tridiagonal (d, e) below x.  A pivot smaller
+// than 1e-30 in magnitude (an exact zero included) is replaced by -1e-30
+// before it is counted, so the count and the recurrence see the same sign;
+// counting a zero pivot as non-negative while continuing with a negative one
+// shifts the count by one and sends the bisection to a neighbouring level.
 __device__ __forceinline__ int sturm_count(const float *d, const float *e, int n, float x) {
   float q = d[0] - x;
+  if (fabsf(q) < 1e-30f) q = -1e-30f;
   int cnt = q < 0.f;
   for (int i = 1; i < n; ++i) {
-    if (fabsf(q) < 1e-30f) q = -1e-30f;
     q = (d[i] - x) - e[i] * e[i] / q;
+    if (fabsf(q) < 1e-30f) q = -1e-30f;
     cnt += q < 0.f;
   }
   return cnt;
@@ -484,7 +579,7 @@ k_eig_bi(const EigBlock *__restrict__ blocks, int max_n_smem, int smem_total) {
     a[int64_t(r) * lda + c] = float(B.H[int64_t(r) * B.ld + c]);
   }
   __syncthreads();
-  tred2_reduce<float>(a, lda, n, d, e, u, p, red, false);
+  tred2_reduce<float>(a, lda, n, d, e, u, p, red, false, !in_smem && (lda % 2 == 0));
   // T's diagonal into d; h_i (0: no reflector) onto the diagonal of the
   // reflector matrix, which k_reflect reads from the block's W buffer
   for (int i = threadIdx.x; i < n; i += kThreads) {

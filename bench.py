@@ -328,6 +328,7 @@ def main():
     kt = kernel_profile(engine)
     rf = roofline_from(kt)
     fallbacks = engine.fallback_count()
+    hbm_peak = engine.memory()[1]
     engine.close()
     plain = None
     if not args.no_fp64:
@@ -357,6 +358,7 @@ def main():
                 "config": dict(CONFIG, precision_path="mixed: FP32 block solve + FP64-accurate refinement"),
                 "gpu_launches": launches,
                 "fp64_fallback_blocks": fallbacks,
+                "hbm_peak_bytes": hbm_peak,
                 "e2e": {"value": e2e_v, "unit": "runs/s", "h2d_bytes_per_step": 4096,
                         "d2h_bytes_per_step": int(d2h)},
                 "plain_fp64": plain, "roofline": rf,

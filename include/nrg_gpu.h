@@ -107,6 +107,9 @@ int nrg_engine_launch_count(nrg_engine *eng, uint64_t *out);
  * that were re-solved with the FP64 block solver (0 for NRG_PREC_FP64).
  * No counterpart in the reference (it has one FP64 path). */
 int nrg_engine_fallback_count(nrg_engine *eng, uint64_t *out);
+/* Device bytes the engine holds now and its high-water mark since creation
+ * (or the last reset_peak != 0 call).  No counterpart in the reference. */
+int nrg_engine_memory(nrg_engine *eng, uint64_t *used, uint64_t *peak, int reset_peak);
 /* Per-kernel CUDA-event timing on the engine stream (off by default). */
 int nrg_engine_set_profiling(nrg_engine *eng, int on);
 /* Times recorded since the last call, aggregated per kernel: names (each

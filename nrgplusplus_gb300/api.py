@@ -57,7 +57,7 @@ class RunInfo(C.Structure):
 
 EXPORTS = [
     "nrg_last_error", "nrg_engine_create", "nrg_engine_destroy", "nrg_engine_phase_times",
-    "nrg_engine_launch_count", "nrg_engine_fallback_count", "nrg_engine_set_profiling",
+    "nrg_engine_launch_count", "nrg_engine_fallback_count", "nrg_engine_memory", "nrg_engine_set_profiling",
     "nrg_engine_kernel_times",
     "nrg_engine_sync", "nrg_run_create", "nrg_run_destroy",
     "nrg_run_set_parameters", "nrg_run_set_bath", "nrg_run_add_site", "nrg_run_update_state",
@@ -169,6 +169,12 @@ class Engine:
         v = C.c_uint64()
         _call(lib().nrg_engine_launch_count, self.h, C.byref(v))
         return v.value
+
+    def memory(self, reset_peak=False):
+        """(device bytes held now, high-water mark) of this engine."""
+        u, p = C.c_uint64(), C.c_uint64()
+        _call(lib().nrg_engine_memory, self.h, C.byref(u), C.byref(p), int(reset_peak))
+        return u.value, p.value
 
     def fallback_count(self):
         """Blocks of the mixed path re-solved in FP64 so far."""

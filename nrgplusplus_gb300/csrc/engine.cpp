@@ -49,6 +49,7 @@ static DevPtr dalloc(nrg_engine *e, size_t bytes) {
   check_cuda(cudaMallocAsync(&m->ptr, bytes, e->stream), "cudaMallocAsync");
   m->bytes = bytes;
   e->used += bytes;
+  if (e->used > e->peak) e->peak = e->used;
   return m;
 }
 

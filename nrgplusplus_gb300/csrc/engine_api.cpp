@@ -560,6 +560,15 @@ int nrg_engine_launch_count(nrg_engine *e, uint64_t *out) {
   });
 }
 
+int nrg_engine_memory(nrg_engine *e, uint64_t *used, uint64_t *peak, int reset_peak) {
+  return guard([&] {
+    if (!e || !used || !peak) fail(NRG_E_ARG, "null argument");
+    *used = e->used;
+    *peak = e->peak;
+    if (reset_peak) e->peak = e->used;
+  });
+}
+
 int nrg_engine_fallback_count(nrg_engine *e, uint64_t *out) {
   return guard([&] {
     if (!e || !out) fail(NRG_E_ARG, "null argument");

@@ -132,6 +132,7 @@ struct nrg_engine {
   int precision = NRG_PREC_FP64;
   uint64_t budget = 0;
   uint64_t used = 0;
+  uint64_t peak = 0;  // high-water mark of `used`
   int verbose = 0;
   cudaStream_t stream = nullptr;
   cudaEvent_t ev[8] = {};

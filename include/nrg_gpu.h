@@ -90,7 +90,7 @@ typedef struct {
   int64_t n_device_blocks;    /* non-empty sectors held on the device */
   int64_t max_block;          /* largest block dimension this iteration */
   int64_t n_snapshots;
-  int64_t device_bytes;       /* device memory held by this run */
+  int64_t device_bytes;       /* device memory held by this run (sites, f-dagger, snapshots) */
 } nrg_run_info;
 
 /* ---- engine ------------------------------------------------------------ */
@@ -242,6 +242,72 @@ int nrg_dgemm_tc(nrg_engine *eng, int transA, int transB, int M, int N, int K, d
 int nrg_batch_add_site(nrg_run *const *runs, int nruns, const double *t, int nt,
                        const double *rescale);
 int nrg_batch_update_state(nrg_run *const *runs, int nruns);
+
+/* ---- serving loop: continuous batching of whole runs ------------------- */
+/* No counterpart in the reference (its drivers run one nrgcore at a time).
+ * A server owns a worker thread that drives one engine: requests submitted
+ * from any thread queue up, are admitted while fewer than max_active runs
+ * are active and their estimated device footprint fits hbm_budget_bytes
+ * (0 = no budget; an idle server admits one request regardless), and every
+ * tick advances all active runs by one Wilson site in shared launches
+ * (nrg_batch_add_site per hopping count), then runs the backward passes
+ * (FDM spectrum, thermodynamics) of the runs that finished.  Results are
+ * kept until nrg_server_release.  The engine must not be used by other
+ * threads while a server drives it. */
+typedef struct nrg_server nrg_server;
+typedef struct {
+  int max_active;             /* runs stepped together (>= 1) */
+  uint64_t hbm_budget_bytes;  /* admission budget, 0 = none */
+} nrg_server_opts;
+typedef struct {
+  const nrg_site_desc *impurity, *bath;
+  uint64_t nkeep;
+  int nsites;                 /* add_bath_site calls */
+  int nt;                     /* hoppings per site */
+  const double *t;            /* nsites * nt */
+  const double *rescale;      /* nsites */
+  const nrg_op_desc *ops;     /* tracked operators, NULL = none; created after the
+                                 first site, in the impurity's sector basis */
+  int fdm;                    /* 1: T = 0 FDM spectrum of ops */
+  int ntemps;                 /* thermodynamics on temps[ntemps], 0 = none */
+  const double *temps;
+  const double *shell_scale;  /* nsites: energy scale of the shell kept after each site */
+  int first_shell_site;       /* shells are kept after sites >= this one that discard states */
+  int keep_eigenvalues;       /* 1: return all_eigenvalue after every site */
+} nrg_request;
+typedef struct {
+  int done;                   /* 1 when finished (ok or failed) */
+  int status;                 /* NRG_OK or the failing call's code */
+  double latency_s;           /* submit -> finish */
+  double queue_s;             /* submit -> admission */
+  int nsites, nops, npts, ntemps;
+  int64_t n_eig_total;        /* sum of the per-site all_eigenvalue sizes */
+  uint64_t peak_device_bytes; /* largest device footprint the run showed */
+  char message[256];          /* error text when status != NRG_OK */
+} nrg_result_info;
+typedef struct {
+  uint64_t submitted, completed, failed, queued, max_active_seen, ticks;
+  double busy_s;              /* worker time spent in ticks */
+  double p50_latency_s, p99_latency_s, mean_latency_s, max_latency_s;
+  double footprint_coef;      /* admission estimate: coef * nsites * (bath states * nkeep)^2 bytes */
+} nrg_server_stats_t;
+int nrg_server_create(nrg_engine *eng, const nrg_server_opts *opts, nrg_server **out);
+/* stops the worker after its current tick; unfinished requests fail */
+int nrg_server_destroy(nrg_server *srv);
+/* copies the request; thread-safe */
+int nrg_server_submit(nrg_server *srv, const nrg_request *req, uint64_t *id);
+int nrg_server_wait(nrg_server *srv, uint64_t id, double timeout_s, int *done);
+int nrg_server_result_info(nrg_server *srv, uint64_t id, nrg_result_info *info);
+/* any output may be NULL; sizes from nrg_result_info (eigs: n_eig_total,
+ * eig_counts: nsites, energy_points: npts, positive / negative: nops x npts,
+ * entropy / cv: ntemps) */
+int nrg_server_get_result(nrg_server *srv, uint64_t id, double *eigs, uint64_t *eig_counts,
+                          double *energy_points, double *positive, double *negative,
+                          double *entropy, double *cv);
+int nrg_server_release(nrg_server *srv, uint64_t id);
+/* latency percentiles over the requests completed since creation or the
+ * last reset != 0 call (nearest rank) */
+int nrg_server_stats(nrg_server *srv, nrg_server_stats_t *stats, int reset);
 
 #ifdef __cplusplus
 }

@@ -69,6 +69,8 @@ EXPORTS = [
     "nrg_fdm_calc", "nrg_fdm_get", "nrg_broaden", "nrg_thermo_create", "nrg_thermo_destroy",
     "nrg_thermo_calc", "nrg_thermo_final", "nrg_batch_add_site", "nrg_batch_update_state",
     "nrg_eigh_batched", "nrg_dgemm_tc", "nrg_broaden_noalloc",
+    "nrg_server_create", "nrg_server_destroy", "nrg_server_submit", "nrg_server_wait",
+    "nrg_server_result_info", "nrg_server_get_result", "nrg_server_release", "nrg_server_stats",
 ]
 BROADEN_NOALLOC_MAX_BINS = 131072  # NRG_BROADEN_NOALLOC_MAX_BINS
 
@@ -403,6 +405,24 @@ class NrgCore:
         return out
 
 
+def _op_buffers(ops):
+    """nrg_op_desc for a list of {(row sector, col sector): block} operators;
+    returns (arrays to keep alive, desc)."""
+    opi, rows, cols, nr, nc, data = [], [], [], [], [], []
+    for ip, d in enumerate(ops):
+        for (i, j), m in sorted(d.items()):
+            m = np.ascontiguousarray(m, float)
+            opi.append(ip)
+            rows.append(i)
+            cols.append(j)
+            nr.append(m.shape[0])
+            nc.append(m.shape[1])
+            data.append(m.ravel())
+    arrs = [np.array(x, dtype=np.int32) for x in (opi, rows, cols, nr, nc)]
+    keep = arrs + [np.ascontiguousarray(np.concatenate(data) if data else np.zeros(1))]
+    return keep, _OpDesc(len(ops), len(opi), *[_ip(a) for a in arrs], _dp(keep[-1]))
+
+
 class OperatorSet:
     """Block-sparse operators tracked through the iteration (a device-resident
     vector<qOperator>), given in the run's current previous basis."""
@@ -410,19 +430,7 @@ class OperatorSet:
     def __init__(self, run, ops):
         self.run = run
         self.nops = len(ops)
-        opi, rows, cols, nr, nc, data = [], [], [], [], [], []
-        for ip, d in enumerate(ops):
-            for (i, j), m in sorted(d.items()):
-                m = np.ascontiguousarray(m, float)
-                opi.append(ip)
-                rows.append(i)
-                cols.append(j)
-                nr.append(m.shape[0])
-                nc.append(m.shape[1])
-                data.append(m.ravel())
-        arrs = [np.array(x, dtype=np.int32) for x in (opi, rows, cols, nr, nc)]
-        self._keep = arrs + [np.ascontiguousarray(np.concatenate(data) if data else np.zeros(1))]
-        desc = _OpDesc(self.nops, len(opi), *[_ip(a) for a in arrs], _dp(self._keep[-1]))
+        self._keep, desc = _op_buffers(ops)
         self.h = C.c_void_p()
         _call(lib().nrg_opset_create, run.h, C.byref(desc), C.byref(self.h))
         run.engine._adopt(self)
@@ -544,3 +552,127 @@ def batch_add_site(runs, t, rescale):
 def batch_update_state(runs):
     arr = (C.c_void_p * len(runs))(*[r.h.value for r in runs])
     _call(lib().nrg_batch_update_state, arr, len(runs))
+
+
+# ---------------------------------------------------------------- serving loop
+class _ServerOpts(C.Structure):
+    _fields_ = [("max_active", C.c_int), ("hbm_budget_bytes", C.c_uint64)]
+
+
+class _Request(C.Structure):
+    _fields_ = [("impurity", C.POINTER(_SiteDesc)), ("bath", C.POINTER(_SiteDesc)), ("nkeep", C.c_uint64),
+                ("nsites", C.c_int), ("nt", C.c_int), ("t", C.POINTER(C.c_double)),
+                ("rescale", C.POINTER(C.c_double)), ("ops", C.POINTER(_OpDesc)), ("fdm", C.c_int),
+                ("ntemps", C.c_int), ("temps", C.POINTER(C.c_double)),
+                ("shell_scale", C.POINTER(C.c_double)), ("first_shell_site", C.c_int),
+                ("keep_eigenvalues", C.c_int)]
+
+
+class _ResultInfo(C.Structure):
+    _fields_ = [("done", C.c_int), ("status", C.c_int), ("latency_s", C.c_double), ("queue_s", C.c_double),
+                ("nsites", C.c_int), ("nops", C.c_int), ("npts", C.c_int), ("ntemps", C.c_int),
+                ("n_eig_total", C.c_int64), ("peak_device_bytes", C.c_uint64), ("message", C.c_char * 256)]
+
+
+class _ServerStats(C.Structure):
+    _fields_ = [(n, C.c_uint64) for n in ("submitted", "completed", "failed", "queued", "max_active_seen",
+                                           "ticks")] + \
+               [(n, C.c_double) for n in ("busy_s", "p50_latency_s", "p99_latency_s", "mean_latency_s",
+                                          "max_latency_s", "footprint_coef")]
+
+
+class Server:
+    """Continuous-batching serving loop over one engine (nrg_server_*): whole
+    NRG runs are submitted from any thread, admitted by count and HBM budget,
+    stepped together one Wilson site per tick, and their backward passes run
+    when they finish.  The engine must not be used elsewhere while it serves."""
+
+    def __init__(self, engine, max_active=16, hbm_budget_bytes=0):
+        self.engine = engine
+        self.h = C.c_void_p()
+        opts = _ServerOpts(max_active, hbm_budget_bytes)
+        _call(lib().nrg_server_create, engine.h, C.byref(opts), C.byref(self.h))
+
+    def submit(self, impurity, bath, nkeep, t, rescale, ops=None, fdm=False, temps=None, shell_scale=None,
+               first_shell_site=0, keep_eigenvalues=False):
+        imp = _SiteBuffers(impurity, False)
+        bt = _SiteBuffers(bath, True)
+        t = np.ascontiguousarray(t, float)
+        nsites, nt = t.shape
+        rs = np.ascontiguousarray(rescale, float)
+        keep = [imp, bt, t, rs]
+        opd = None
+        if ops is not None:
+            k, opd = _op_buffers(ops)
+            keep += k
+        tp = np.ascontiguousarray(temps if temps is not None else np.zeros(0), float)
+        sc = np.ascontiguousarray(shell_scale, float) if shell_scale is not None else None
+        keep += [tp, sc]
+        req = _Request(C.pointer(imp.desc), C.pointer(bt.desc), nkeep, nsites, nt, _dp(t), _dp(rs),
+                       C.pointer(opd) if opd is not None else None, int(fdm), len(tp),
+                       _dp(tp) if len(tp) else None, _dp(sc) if sc is not None else None,
+                       first_shell_site, int(keep_eigenvalues))
+        rid = C.c_uint64()
+        _call(lib().nrg_server_submit, self.h, C.byref(req), C.byref(rid))
+        return rid.value
+
+    def wait(self, rid, timeout=600.0):
+        done = C.c_int()
+        _call(lib().nrg_server_wait, self.h, C.c_uint64(rid), C.c_double(timeout), C.byref(done))
+        return bool(done.value)
+
+    def info(self, rid):
+        inf = _ResultInfo()
+        _call(lib().nrg_server_result_info, self.h, C.c_uint64(rid), C.byref(inf))
+        return inf
+
+    def result(self, rid, release=True):
+        """Results of a finished request; raises NrgError if it failed."""
+        inf = self.info(rid)
+        if not inf.done:
+            raise NrgError(2, "request not finished")
+        if inf.status != 0:
+            msg = inf.message.decode()
+            if release:
+                _call(lib().nrg_server_release, self.h, C.c_uint64(rid))
+            raise NrgError(inf.status, msg)
+        eigs = np.zeros(max(1, inf.n_eig_total))
+        counts = np.zeros(max(1, inf.nsites), dtype=np.uint64)
+        ep = np.zeros(max(1, inf.npts))
+        pos = np.zeros((max(1, inf.nops), max(1, inf.npts)))
+        neg = np.zeros_like(pos)
+        ent = np.zeros(max(1, inf.ntemps))
+        cv = np.zeros_like(ent)
+        _call(lib().nrg_server_get_result, self.h, C.c_uint64(rid), _dp(eigs),
+              counts.ctypes.data_as(C.POINTER(C.c_uint64)), _dp(ep), _dp(pos), _dp(neg), _dp(ent), _dp(cv))
+        out = {"latency_s": inf.latency_s, "queue_s": inf.queue_s, "peak_device_bytes": inf.peak_device_bytes}
+        if inf.n_eig_total:
+            o, eig = 0, []
+            for c in counts[:inf.nsites]:
+                eig.append(eigs[o:o + int(c)].copy())
+                o += int(c)
+            out["eig"] = eig
+        if inf.npts:
+            out.update({"GreenFnEnergyPoints": ep, "GreenFnPositiveWeight": pos[:inf.nops],
+                        "GreenFnNegativeWeight": neg[:inf.nops]})
+        if inf.ntemps:
+            out.update({"entropy": ent[:inf.ntemps], "specificHeat": cv[:inf.ntemps]})
+        if release:
+            _call(lib().nrg_server_release, self.h, C.c_uint64(rid))
+        return out
+
+    def stats(self, reset=False):
+        st = _ServerStats()
+        _call(lib().nrg_server_stats, self.h, C.byref(st), int(reset))
+        return {n: getattr(st, n) for n, _ in _ServerStats._fields_}
+
+    def close(self):
+        if self.h:
+            lib().nrg_server_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

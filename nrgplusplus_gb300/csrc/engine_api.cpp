@@ -6,6 +6,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <numeric>
+#include <set>
 
 #include "engine_core.h"
 
@@ -684,7 +685,31 @@ int nrg_run_get_info(nrg_run *r, nrg_run_info *info) {
       for (auto &b : r->site->blocks) info->max_block = std::max<int64_t>(info->max_block, b.n);
     }
     info->n_snapshots = int64_t(r->snaps.size());
-    info->device_bytes = int64_t(r->eng->used);
+    // device bytes this run holds: its current and previous site, f-dagger
+    // blocks and every snapshot (buffers shared between them counted once)
+    std::set<const DevMem *> seen;
+    int64_t bytes = 0;
+    auto add = [&](const DevPtr &m) {
+      if (m && m->ptr && seen.insert(m.get()).second) bytes += int64_t(m->bytes);
+    };
+    auto add_site = [&](const std::shared_ptr<SiteData> &sd) {
+      if (!sd) return;
+      add(sd->mem_U);
+      add(sd->mem_E);
+      add(sd->mem_Uplanes);
+      add(sd->mem_Uexps);
+    };
+    add_site(r->site);
+    add_site(r->prev_site);
+    add(r->mem_H);
+    add(r->mem_sorted);
+    add(r->fprev_mem);
+    add(r->fcur_mem);
+    for (auto &kv : r->snaps) {
+      add_site(kv.second->site);
+      add(kv.second->ops_mem);
+    }
+    info->device_bytes = bytes;
   });
 }
 

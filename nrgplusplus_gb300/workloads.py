@@ -98,3 +98,19 @@ def spectral_function(engine, energies, pos, neg, b=0.6, decades=(-8, 0), per_de
     n = (decades[1] - decades[0]) * per_decade + 1
     om = np.logspace(decades[0], decades[1], n)
     return om, engine.broaden(energies, pos, om, b), engine.broaden(energies, neg, om, b)
+
+
+def siam_request(nkeep, nsites, lam, V, eps=-0.25, U=0.5, fdm=False, thermo=False, keep_eigs=True):
+    """Keyword arguments of Server.submit for the SIAM run that run_nrg(...,
+    'siam', ...) drives through the API: the V site, then nsites Wilson sites;
+    shells kept after the Wilson sites, scaled Lambda^(-(it-1)/2) as in the
+    backward loops of run_nrg (examples/fdmSpectrumSiam, examples/entropySIAM)."""
+    imp, bath = build_models("siam", eps, U)
+    nops = len(imp.fdag)
+    t = [[V] * nops] + [[M.hopping(it, lam)] * nops for it in range(nsites)]
+    rescale = [1.0] + [math.sqrt(lam) if it > 0 else 1.0 for it in range(nsites)]
+    scale = [1.0] + [lam ** (-(it) / 2.0) for it in range(nsites)]
+    return dict(impurity=imp, bath=bath, nkeep=nkeep, t=np.array(t), rescale=np.array(rescale),
+                ops=M.d_dag_chi() if fdm else None, fdm=fdm,
+                temps=temperature_grid() if thermo else None, shell_scale=np.array(scale),
+                first_shell_site=1, keep_eigenvalues=keep_eigs)

@@ -13,6 +13,9 @@ temperature grid.  The reference publishes no number for this metric.
           copied to host buffers inside the timed region
   --impl reference : the reference's CPU algorithm (the numpy port of the
           oracle) timed on this host's cores on the same workload
+  serving : the same runs as requests to the continuous-batching server
+          (nrg_server_*), seeded Poisson arrivals at 80 % of the measured
+          batch throughput: p50 / p99 request latency and served runs/s
 
 usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 """
@@ -36,6 +39,41 @@ CONFIG = {"workload": "siam_fdm_spectral_c2", "impurity": "spinhalf(eps_d=-0.4,U
           "thermo": "entropy + C on 200-point T grid",
           "l2": "flushed (256 MiB write) between steps", "runs_per_step": BATCH}
 METRIC = "SIAM runs/s (full FDM spectral run, Nkeep=1024, 50 sites)"
+
+
+def serving_run(engine, rate, n, seed=2024, max_active=16):
+    """Seeded Poisson stream of n workload requests at `rate` per second into
+    the serving loop; latency = submission to completed results."""
+    import threading
+    import numpy as np
+    from nrgplusplus_gb300 import api, workloads
+    w = WORK
+    req = workloads.siam_request(w["nkeep"], w["nsites"], w["lam"], w["V"], eps=w["eps"], U=w["U"],
+                                 fdm=True, thermo=True, keep_eigs=False)
+    gaps = np.random.default_rng(seed).exponential(1.0 / rate, size=n)
+    srv = api.Server(engine, max_active=max_active)
+    ids = []
+
+    def arrivals():
+        for g in gaps:
+            time.sleep(float(g))
+            ids.append(srv.submit(**req))
+
+    t0 = time.perf_counter()
+    th = threading.Thread(target=arrivals)
+    th.start()
+    th.join()
+    for i in ids:
+        srv.wait(i, 3600.0)
+        srv.result(i)
+    wall = time.perf_counter() - t0
+    st = srv.stats()
+    srv.close()
+    return {"requests": n, "arrival_rate_per_s": rate, "seed": seed, "max_active": max_active,
+            "runs_per_s": st["completed"] / wall, "p50_latency_s": st["p50_latency_s"],
+            "p99_latency_s": st["p99_latency_s"], "mean_latency_s": st["mean_latency_s"],
+            "max_active_seen": int(st["max_active_seen"]), "failed": int(st["failed"]),
+            "arrivals": "Poisson, seeded; every request the full workload run (FDM + thermodynamics)"}
 
 
 def _dist():
@@ -265,6 +303,8 @@ def main():
     ap.add_argument("--cpu-sites", type=int, default=50,
                     help="forward sites of the bounded CPU-baseline sample")
     ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 comparator")
+    ap.add_argument("--no-serving", action="store_true", help="skip the serving-loop measurement")
+    ap.add_argument("--serving-requests", type=int, default=32)
     ap.add_argument("--sites", type=int, default=50,
                     help="Wilson sites per run (50 = the workload; fewer only for profiling captures)")
     args = ap.parse_args()
@@ -329,6 +369,9 @@ def main():
     rf = roofline_from(kt)
     fallbacks = engine.fallback_count()
     hbm_peak = engine.memory()[1]
+    serving = None
+    if not args.no_serving:
+        serving = serving_run(engine, 0.8 * BATCH / per, args.serving_requests)
     engine.close()
     plain = None
     if not args.no_fp64:
@@ -361,7 +404,7 @@ def main():
                 "hbm_peak_bytes": hbm_peak,
                 "e2e": {"value": e2e_v, "unit": "runs/s", "h2d_bytes_per_step": 4096,
                         "d2h_bytes_per_step": int(d2h)},
-                "plain_fp64": plain, "roofline": rf,
+                "serving": serving, "plain_fp64": plain, "roofline": rf,
                 "kernels_ms_per_step": {k: round(v[0], 3) for k, v in kt.items()},
                 "cpu_baseline": cpu, "clocks": clk.summary()}
         print(json.dumps(line))

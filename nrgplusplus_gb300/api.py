@@ -16,7 +16,8 @@ import weakref
 import numpy as np
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
-_LIBPATH = os.path.join(_HERE, "libnrggpu.so")
+# NRG_GPU_LIB: path of another build of the library (A/B timing of two builds)
+_LIBPATH = os.environ.get("NRG_GPU_LIB") or os.path.join(_HERE, "libnrggpu.so")
 _lib = None
 
 PREC_FP64, PREC_MIXED = 0, 1

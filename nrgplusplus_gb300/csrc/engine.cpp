@@ -76,6 +76,15 @@ template <class T> static T *at(char *base, size_t off) { return reinterpret_cas
 
 static void count_launch(nrg_engine *e, int n = 1) { e->launches += n; }
 
+void check_kernel_error(nrg_engine *e) {
+  int h = 0;
+  check_cuda(cudaMemcpy(&h, e->d_kerr, sizeof(int), cudaMemcpyDeviceToHost), "kernel error word");
+  if (h) {
+    cudaMemset(e->d_kerr, 0, sizeof(int));
+    fail(NRG_E_CUDA, "a tensor-core GEMM wait timed out (results of that launch are incomplete)");
+  }
+}
+
 static void post_launch(const char *what) { check_cuda(cudaGetLastError(), what); }
 
 // ---------------------------------------------------------------- models
@@ -437,8 +446,8 @@ void OzList::out(double *C, int ldc, int M, int N, bool acc, const std::vector<O
   g.c1 = int(contribs.size());
   const int gi = int(groups.size());
   groups.push_back(g);
-  for (int tm = 0; tm < (M + GEMM_TILE - 1) / GEMM_TILE; ++tm)
-    for (int tn = 0; tn < (N + GEMM_TILE - 1) / GEMM_TILE; ++tn) tiles.push_back({gi, tm, tn, 0});
+  for (int tm = 0; tm < (M + OZ_TILE_M - 1) / OZ_TILE_M; ++tm)
+    for (int tn = 0; tn < (N + OZ_TILE_N - 1) / OZ_TILE_N; ++tn) tiles.push_back({gi, tm, tn, 0});
 }
 
 void OzList::launch(nrg_engine *e, std::vector<DevPtr> &hold) {
@@ -449,7 +458,8 @@ void OzList::launch(nrg_engine *e, std::vector<DevPtr> &hold) {
   char *p = a.push(e, d);
   hold.push_back(d);
   Prof pf(e, "k_gemm_oz", flops);
-  launch_gemm_oz(at<GemmTile>(p, ot), int(tiles.size()), at<OzGroup>(p, og), at<OzContrib>(p, oc), e->stream);
+  launch_gemm_oz(at<GemmTile>(p, ot), int(tiles.size()), at<OzGroup>(p, og), at<OzContrib>(p, oc), e->d_kerr,
+                 e->stream);
   count_launch(e);
   post_launch("ozaki gemm");
 }
@@ -927,6 +937,7 @@ static void batch_add_site(nrg_run *const *runs, int nruns, const double *t, int
                "eigenvalues D2H");
   }
   check_cuda(cudaStreamSynchronize(s), "site step");
+  check_kernel_error(e);
   mcheck.check(e);
   for (size_t b = 0; b < eblk_sorted.size(); ++b)
     if (stat[b]) fail(NRG_E_EIG, "block eigensolver did not converge (n = " +
@@ -1169,6 +1180,7 @@ extern "C" int nrg_eigh_batched(nrg_engine *e, int nblk, const int *dims, const 
       MixedCheck mc;
       mc.enqueue(mixed_eigensolve(e, ptrs, max_n, hold), s);
       check_cuda(cudaStreamSynchronize(s), "eigh");
+      check_kernel_error(e);
       mc.check(e);
     }
     eo = 0;
@@ -1233,6 +1245,7 @@ extern "C" int nrg_dgemm_tc(nrg_engine *e, int transA, int transB, int M, int N,
     l.launch(e, hold);
     check_cuda(cudaMemcpy2DAsync(C, ldc * 8, dc->ptr, N * 8, N * 8, M, cudaMemcpyDeviceToHost, s), "C");
     check_cuda(cudaStreamSynchronize(s), "dgemm_tc");
+    check_kernel_error(e);
     return NRG_OK;
   } catch (const Error &x) {
     g_err = x.msg;

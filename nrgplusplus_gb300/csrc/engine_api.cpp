@@ -481,6 +481,8 @@ int nrg_engine_create(const nrg_engine_opts *opts, nrg_engine **out) {
     for (auto &ev : e->ev) check_cuda(cudaEventCreate(&ev), "event");
     e->eig_smem_f64 = eig_smem_limit_f64();
     e->eig_smem_f32 = eig_smem_limit_f32();
+    check_cuda(cudaMalloc(&e->d_kerr, sizeof(int)), "cudaMalloc (kernel error word)");
+    check_cuda(cudaMemset(e->d_kerr, 0, sizeof(int)), "cudaMemset");
     if (const char *oz = std::getenv("NRG_OZAKI")) e->ozaki = std::atoi(oz) & 3;
     *out = e;
   });
@@ -490,6 +492,7 @@ int nrg_engine_destroy(nrg_engine *e) {
   return guard([&] {
     if (!e) return;
     cudaStreamSynchronize(e->stream);
+    if (e->d_kerr) cudaFree(e->d_kerr);
     for (auto &ev : e->ev) cudaEventDestroy(ev);
     cudaStreamDestroy(e->stream);
     delete e;
@@ -581,6 +584,7 @@ int nrg_engine_sync(nrg_engine *e) {
   return guard([&] {
     if (!e) fail(NRG_E_ARG, "null engine");
     check_cuda(cudaStreamSynchronize(e->stream), "sync");
+    check_kernel_error(e);
   });
 }
 

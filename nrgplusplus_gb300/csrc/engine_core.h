@@ -139,8 +139,7 @@ struct nrg_engine {
   double phase_ms[5] = {0, 0, 0, 0, 0};
   uint64_t launches = 0;
   int eig_smem_f64 = 0, eig_smem_f32 = 0;
-  int *d_status = nullptr;
-  size_t status_cap = 0;
+  int *d_kerr = nullptr;  // set by kernels whose bounded waits ran out (k_gemm_oz)
   uint64_t fallback_blocks = 0;  // mixed path: blocks re-solved in FP64
   // mixed path: FP64-accurate GEMMs on the tensor cores, bit 0 for the
   // eigenvector refinement, bit 1 for the operator rotations
@@ -157,6 +156,9 @@ struct nrg_engine {
 };
 
 namespace nrg {
+// Fails with NRG_E_CUDA (and clears the word) when a kernel has reported a
+// timed-out wait; call after a stream synchronisation.
+void check_kernel_error(nrg_engine *e);
 // Records CUDA events around one kernel launch on the engine stream when
 // profiling is on; `work` is the launch's algorithmic flop count (byte count
 // for the memory-bound kernels k_split and k_oa_update).

@@ -11,10 +11,21 @@
 // sums while |sum| <= 2^24: grouping the pairs by d = p + q (d <= 7; the
 // dropped groups weigh below 2^-51 of the result scale) and accumulating each
 // group over at most 512 k-terms keeps every partial sum an exact integer.
-// The 8 group sums are combined once per output element and K-chunk by an
-// integer Horner (h = G_0; h = 128 h + G_d) and one FP64 fma, so the FP64
-// pipe does a few operations per output element instead of K.  The bf16 products use mma.sync m16n8k16 with
-// FP32 accumulation; the result matches an FP64 GEMM to FP64 round-off.
+//
+// k_gemm_oz runs the 36 pair products on the 5th-generation tensor cores:
+// one CTA owns a 128 x 64 output tile, the eight group sums live in tensor
+// memory (TMEM: 8 accumulators x 64 FP32 columns = all 512 columns, lane =
+// output row), and one thread issues tcgen05.mma (kind::f16, bf16 inputs,
+// FP32 accumulation, M = 128, N = 64, K = 16) on operand tiles that all
+// threads stage in shared memory with 16-byte cp.async copies in the
+// canonical no-swizzle core-matrix layouts (K-major or MN-major per operand,
+// so transposed operands need no transpose).  A four-stage ring overlaps the
+// copies of later k-steps with the MMAs of the current one; tcgen05.commit
+// arrives on one mbarrier per stage when its MMAs are done.  The group sums
+// are folded into the FP64 output once per run of contributions that share a
+// scale (at most 512 deep): tcgen05.ld to registers, integer Horner over the
+// groups, one FP64 fma per element.  Every mbarrier wait is bounded; a wait
+// that runs out sets *err, and the kernel drains and releases TMEM.
 #include <cuda_bf16.h>
 
 #include "nrg_internal.h"
@@ -24,32 +35,8 @@ namespace {
 
 constexpr int kPlanes = 8;
 constexpr int kChunkK = 512;
-constexpr int BM = 64, BN = 64, BK = 32;
-constexpr int kThreads = 256;
-// shared-memory row pitches (bf16 elements): 80-byte and 144-byte rows make
-// the 8 row addresses of every ldmatrix fall in distinct 16-byte bank groups
-constexpr int kPitchK = BK + 8;   // tiles stored [m or n][k]
-constexpr int kPitchMN = BM + 8;  // tiles stored [k][m or n]
-constexpr int kTileElems = kPlanes * BM * kPitchK;  // >= kPlanes * BK * kPitchMN
-
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-
-__device__ __forceinline__ void ldsm_x4(uint32_t addr, uint32_t &r0, uint32_t &r1, uint32_t &r2, uint32_t &r3) {
-  asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
-               : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3) : "r"(addr));
-}
-__device__ __forceinline__ void ldsm_x4_t(uint32_t addr, uint32_t &r0, uint32_t &r1, uint32_t &r2, uint32_t &r3) {
-  asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];\n"
-               : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3) : "r"(addr));
-}
-__device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
-  asm volatile(
-      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-      "{%0,%1,%2,%3};\n"
-      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
 }
 
 // ---------------------------------------------------------------- split
@@ -151,10 +138,6 @@ __global__ void __launch_bounds__(256) k_split(const SplitTask *__restrict__ tas
 }
 
 // ----------------------------------------------------------------- GEMM
-struct Frag {
-  uint32_t a[kPlanes][4];
-};
-
 __device__ __forceinline__ void cp_async16(void *dst, const void *src, bool valid) {
   const uint32_t d = smem_u32(dst);
   const int sz = valid ? 16 : 0;  // 0: no bytes read, 16 zero bytes written
@@ -173,195 +156,287 @@ template <int N> __device__ __forceinline__ void cp_async_wait() {
   asm volatile("cp.async.wait_group %0;\n" ::"n"(N));
 }
 
-// Stage one 32-deep k-slice of every digit plane of op(A) (64 x 32) and
-// op(B) (32 x 64) into shared memory with 16-byte cp.async copies.  Plane
-// rows are zero-padded to a multiple of 8 elements and row starts are
-// 16-byte aligned, so every 8-element vector is either wholly inside the
-// operand or zero-filled.
-__device__ __forceinline__ void stage_tiles(const OzContrib &q, bool ta, bool tb, int M, int N, int m0,
-                                            int n0, int k0, int kend, __nv_bfloat16 *As,
-                                            __nv_bfloat16 *Bs) {
-  const int tid = threadIdx.x;
-#pragma unroll
+constexpr int TM = 128, TN = 64, TK = 16;  // output tile, k-step (one MMA)
+constexpr int kStages = 4;
+constexpr int kTcThreads = 256;
+constexpr int kATile = TM * TK * 2, kBTile = TN * TK * 2;  // bytes per plane
+constexpr int kStageBytes = kPlanes * (kATile + kBTile);   // 48 KB
+constexpr uint32_t kLBO = 128, kSBO = 256;                 // core-matrix strides (K = 16)
+constexpr int kWaitLimit = 1 << 24;                        // bounded mbarrier polls
+constexpr int kLag = 1;            // producer copy groups in flight before a hand-over
+
+// byte offset of the 16-byte core-matrix row holding element (r, k) of an
+// R x 16 operand tile: K-major rows are 8 consecutive k, MN-major rows are
+// 8 consecutive r (r, k multiples of 8 at the row start)
+__device__ __forceinline__ uint32_t tile_off(int r, int k, bool kmajor) {
+  return uint32_t(r >> 3) * kSBO + uint32_t(k >> 3) * kLBO + (kmajor ? uint32_t(r & 7) * 16 : uint32_t(k & 7) * 16);
+}
+
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
+  return uint64_t((addr >> 4) & 0x3FFF) | (uint64_t(kLBO >> 4) << 16) | (uint64_t(kSBO >> 4) << 32) |
+         (uint64_t(1) << 46);  // descriptor version; base offset 0; no swizzle
+}
+
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+  for (int it = 0; it < kWaitLimit; ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred P1;\n mbarrier.try_wait.parity.shared::cta.b64 P1, [%1], %2;\n"
+        " selp.b32 %0, 1, 0, P1;\n}\n"
+        : "=r"(done) : "r"(bar), "r"(parity) : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+// Stage the k-step [k0, k0 + 16) of all 8 planes of op(A) (128 x 16) and
+// op(B) (64 x 16): 3072 rows of 16 bytes, 24 per producer thread (tp =
+// 0..127): per plane two A rows and one B row.
+__device__ __forceinline__ void stage_step(const OzContrib &q, int M, int N, int m0, int n0, int k0, int kend,
+                                           unsigned char *st, int tp) {
+  const bool ta = q.trans & 1, tb = (q.trans >> 1) & 1;
+#pragma unroll 2
   for (int p = 0; p < kPlanes; ++p) {
-    {  // A: 256 vectors per plane, one per thread
-      const __nv_bfloat16 *base = q.A.p + int64_t(p) * q.A.pstride;
-      if (!ta) {  // [m][k], 64 rows x 4 vectors
-        const int mm = tid >> 2, v = tid & 3;
-        const int gm = m0 + mm, gk = k0 + 8 * v;
+    unsigned char *As = st + p * kATile;
+    unsigned char *Bs = st + kPlanes * kATile + p * kBTile;
+    const __nv_bfloat16 *a = q.A.p + int64_t(p) * q.A.pstride;
+    const __nv_bfloat16 *b = q.B.p + int64_t(p) * q.B.pstride;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {  // A: 256 rows
+      const int r = tp + 128 * h;
+      if (!ta) {  // stored [m][k]: 128 m x 2 k-halves
+        const int m = r >> 1, kh = (r & 1) * 8;
+        const int gm = m0 + m, gk = k0 + kh;
         const bool ok = gm < M && gk < kend;
-        cp_async16_k(As + (p * BM + mm) * kPitchK + 8 * v, ok ? base + int64_t(gm) * q.A.ld + gk : base,
-                     ok ? kend - gk : 0);
-      } else {    // [k][m], 32 rows x 8 vectors
-        const int kk = tid >> 3, v = tid & 7;
-        const int gk = k0 + kk, gm = m0 + 8 * v;
+        cp_async16_k(As + tile_off(m, kh, true), ok ? a + int64_t(gm) * q.A.ld + gk : a, ok ? kend - gk : 0);
+      } else {    // stored [k][m]: 16 k x 16 m-octets
+        const int k = r >> 4, mo = (r & 15) * 8;
+        const int gk = k0 + k, gm = m0 + mo;
         const bool ok = gk < kend && gm < M;
-        cp_async16(As + (p * BK + kk) * kPitchMN + 8 * v, ok ? base + int64_t(gk) * q.A.ld + gm : base, ok);
+        cp_async16(As + tile_off(mo, k, false), ok ? a + int64_t(gk) * q.A.ld + gm : a, ok);
       }
     }
-    {  // B
-      const __nv_bfloat16 *base = q.B.p + int64_t(p) * q.B.pstride;
-      if (tb) {   // [n][k]
-        const int nn = tid >> 2, v = tid & 3;
-        const int gn = n0 + nn, gk = k0 + 8 * v;
-        const bool ok = gn < N && gk < kend;
-        cp_async16_k(Bs + (p * BN + nn) * kPitchK + 8 * v, ok ? base + int64_t(gn) * q.B.ld + gk : base,
-                     ok ? kend - gk : 0);
-      } else {    // [k][n]
-        const int kk = tid >> 3, v = tid & 7;
-        const int gk = k0 + kk, gn = n0 + 8 * v;
-        const bool ok = gk < kend && gn < N;
-        cp_async16(Bs + (p * BK + kk) * kPitchMN + 8 * v, ok ? base + int64_t(gk) * q.B.ld + gn : base, ok);
-      }
+    if (tb) {   // B stored [n][k]: 64 n x 2 k-halves
+      const int n = tp >> 1, kh = (tp & 1) * 8;
+      const int gn = n0 + n, gk = k0 + kh;
+      const bool ok = gn < N && gk < kend;
+      cp_async16_k(Bs + tile_off(n, kh, true), ok ? b + int64_t(gn) * q.B.ld + gk : b, ok ? kend - gk : 0);
+    } else {    // stored [k][n]: 16 k x 8 n-octets
+      const int k = tp >> 3, no = (tp & 7) * 8;
+      const int gk = k0 + k, gn = n0 + no;
+      const bool ok = gk < kend && gn < N;
+      cp_async16(Bs + tile_off(no, k, false), ok ? b + int64_t(gk) * q.B.ld + gn : b, ok);
     }
   }
 }
 
-__global__ void __launch_bounds__(kThreads, 1)
+// Walks the k-steps of a group's contribution list (skipping empty ones).
+struct StepIt {
+  int c, k0;
+  __device__ void skip_empty(const OzGroup &g, const OzContrib *cs) {
+    while (c < g.c1 && cs[c].K <= 0) ++c;
+  }
+  __device__ void next(const OzGroup &g, const OzContrib *cs) {
+    k0 += TK;
+    if (k0 >= cs[c].K) {
+      ++c;
+      k0 = 0;
+      skip_empty(g, cs);
+    }
+  }
+};
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void mma_commit(uint32_t bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void consumer_sync() {  // warps 0-3 only
+  asm volatile("bar.sync 1, 128;" ::: "memory");
+}
+
+// Warp roles: warps 4-7 stage k-steps into a ring of kStages buffers (a
+// stage is released by the tcgen05.commit of its MMAs on empty[stage] and
+// handed over on full[stage] once its copies have landed); warp 0 lane 0
+// issues the 36 MMAs of each step; warps 0-3 (the 128 TMEM lanes) fold the
+// group sums whenever the scale changes, 512 k-terms are used up, or the
+// list ends (after a drain commit on `drain`).  No CTA-wide barrier sits in
+// the k-loop.
+__global__ void __launch_bounds__(kTcThreads, 1)
 k_gemm_oz(const GemmTile *__restrict__ tiles, const OzGroup *__restrict__ groups,
-          const OzContrib *__restrict__ contribs) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  __nv_bfloat16 *As0 = reinterpret_cast<__nv_bfloat16 *>(smem_raw);
-  __nv_bfloat16 *Bs0 = As0 + 2 * kTileElems;
-  double *Ct = reinterpret_cast<double *>(Bs0 + 2 * kTileElems);  // BM x BN FP64 totals
+          const OzContrib *__restrict__ contribs, int *err) {
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  __shared__ __align__(8) uint64_t full[kStages], empty[kStages], drain;
+  __shared__ uint32_t tmem_slot;
+  __shared__ volatile int abort_flag;
+  unsigned char *ring = smem_raw;
   const GemmTile t = tiles[blockIdx.x];
   const OzGroup g = groups[t.group];
-  const int m0 = t.tm * BM, n0 = t.tn * BN;
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int wm = (warp & 3) * 16, wn = (warp >> 2) * 32;
-  for (int i = tid; i < BM * BN; i += kThreads) Ct[i] = 0.0;
+  const int m0 = t.tm * TM, n0 = t.tn * TN;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
-  // Group sums of consecutive contributions (and K-chunks) that share the
-  // scale |alpha| 2^(eA+eB-61) stay in the same FP32 accumulators while their
-  // total depth is <= kChunkK (every partial sum stays an exact integer below
-  // 2^24); a negative alpha flips the sign bits of the A fragments.  The
-  // accumulators are folded into the FP64 tile only when the scale changes,
-  // the depth is used up, or the list ends.
-  float acc[kPlanes][4][4];
-#pragma unroll
-  for (int d = 0; d < kPlanes; ++d)
-#pragma unroll
-    for (int j = 0; j < 4; ++j)
-#pragma unroll
-      for (int v = 0; v < 4; ++v) acc[d][j][v] = 0.f;
-  int kacc = 0;          // depth accumulated since the last fold
-  double acc_scale = 0;  // its scale
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
+                 "r"(512));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  if (tid == 0) {
+    for (int i = 0; i < kStages; ++i) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 128;" ::"r"(smem_u32(&full[i])));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&empty[i])));
+    }
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&drain)));
+    asm volatile("fence.mbarrier_init.release.cluster;");
+    abort_flag = 0;
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  const uint32_t tmem = tmem_slot;
 
-  auto fold = [&]() {
-    // exact group sums -> FP64: 32-bit conversions, Horner over the groups in
-    // integers (groups 0-4 into hi <= 2^53, groups 5-7 into lo <= 2^39),
-    // then one FP64 fma per element
-#pragma unroll
-    for (int j = 0; j < 4; ++j)
-#pragma unroll
-      for (int v = 0; v < 4; ++v) {
-        long long hi = __float2int_rz(acc[0][j][v]);
-#pragma unroll
-        for (int d = 1; d < 5; ++d) hi = hi * 128 + __float2int_rz(acc[d][j][v]);
-        long long lo = __float2int_rz(acc[5][j][v]);
-#pragma unroll
-        for (int d = 6; d < kPlanes; ++d) lo = lo * 128 + __float2int_rz(acc[d][j][v]);
-        const double h = fma(__ll2double_rn(hi), 2097152.0, __ll2double_rn(lo));  // 128^3
-        const int r = wm + (lane >> 2) + (v >> 1) * 8;
-        const int col = wn + j * 8 + (lane & 3) * 2 + (v & 1);
-        Ct[r * BN + col] = fma(acc_scale, h, Ct[r * BN + col]);
-#pragma unroll
-        for (int d = 0; d < kPlanes; ++d) acc[d][j][v] = 0.f;
-      }
-    kacc = 0;
-  };
+  int nsteps = 0;
+  for (int c = g.c0; c < g.c1; ++c)
+    if (contribs[c].K > 0) nsteps += (contribs[c].K + TK - 1) / TK;
 
-  for (int c = g.c0; c < g.c1; ++c) {
-    const OzContrib q = contribs[c];
-    const bool ta = q.trans & 1, tb = (q.trans >> 1) & 1;
-    const double scale = fabs(q.alpha) * scalbn(1.0, *q.A.exp + *q.B.exp - 61);
-    const uint32_t neg = (q.alpha < 0.0) ? 0x80008000u : 0u;
-    for (int kc = 0; kc < q.K; kc += kChunkK) {
-      const int kend = min(q.K, kc + kChunkK);
-      const int nst = (kend - kc + BK - 1) / BK;
-      if (kacc > 0 && (scale != acc_scale || kacc + (kend - kc) > kChunkK)) fold();
-      acc_scale = scale;
-      kacc += kend - kc;
-      __syncthreads();  // previous users of both buffers are done
-      stage_tiles(q, ta, tb, g.M, g.N, m0, n0, kc, kend, As0, Bs0);
+  if (warp >= 4) {
+    // ------------------------------------------------------------ producers
+    const int tp = tid - 128;
+    StepIt it{g.c0, 0};
+    it.skip_empty(g, contribs);
+    for (int s = 0; s < nsteps; ++s) {
+      const int st = s % kStages, use = s / kStages;
+      if (use > 0 && !mbar_wait(smem_u32(&empty[st]), uint32_t((use - 1) & 1))) abort_flag = 1;
+      if (abort_flag) break;
+      const OzContrib &q = contribs[it.c];
+      stage_step(q, g.M, g.N, m0, n0, it.k0, q.K, ring + st * kStageBytes, tp);
       cp_async_commit();
-      for (int st = 0; st < nst; ++st) {
-        const int buf = st & 1;
-        if (st + 1 < nst) {
-          stage_tiles(q, ta, tb, g.M, g.N, m0, n0, kc + (st + 1) * BK, kend, As0 + (buf ^ 1) * kTileElems,
-                      Bs0 + (buf ^ 1) * kTileElems);
-          cp_async_commit();
-          cp_async_wait<1>();
-        } else {
-          cp_async_wait<0>();
-        }
-        __syncthreads();
-        const __nv_bfloat16 *As = As0 + buf * kTileElems;
-        const __nv_bfloat16 *Bs = Bs0 + buf * kTileElems;
+      it.next(g, contribs);
+      if (s >= kLag) {  // the copies of step s - kLag have landed: hand it over
+        cp_async_wait<kLag>();
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        mbar_arrive(smem_u32(&full[(s - kLag) % kStages]));
+      }
+    }
+    cp_async_wait<0>();
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    if (!abort_flag)
+      for (int s = (nsteps > kLag ? nsteps - kLag : 0); s < nsteps; ++s) mbar_arrive(smem_u32(&full[s % kStages]));
+  } else {
+    // ------------------------------------------------ MMA issue and folds
+    StepIt it{g.c0, 0};
+    it.skip_empty(g, contribs);
+    int kacc = 0;
+    double acc_scale = 0;
+    bool first_fold = true;
+    uint32_t drain_phase = 0;
+    const uint64_t d0 = smem_desc(smem_u32(ring));
+    const uint32_t tl = tmem + (uint32_t(32 * warp) << 16);
+    const int gm = m0 + 32 * warp + lane;
+
+    // Every consumer thread makes the same fold() calls (the fold points
+    // depend only on the contribution list), so the named barrier at its end
+    // is always reached by all 128; after an abort the waits and TMEM reads
+    // are skipped (decided per warp, as tcgen05.ld is warp-collective).
+    auto fold = [&]() {
+      // drain: every MMA issued so far has completed
+      if (__shfl_sync(0xffffffffu, abort_flag, 0) == 0) {
+        if (tid == 0) mma_commit(smem_u32(&drain));
+        if (!mbar_wait(smem_u32(&drain), drain_phase)) abort_flag = 1;
+      }
+      drain_phase ^= 1u;
+      asm volatile("tcgen05.fence::after_thread_sync;");
+      if (__shfl_sync(0xffffffffu, abort_flag, 0) == 0) {
+        for (int cc = 0; cc < TN; cc += 8) {
+          uint32_t v[kPlanes][8];
 #pragma unroll
-        for (int ks = 0; ks < BK; ks += 16) {
-          Frag fa;
+          for (int d = 0; d < kPlanes; ++d)
+            asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                         : "=r"(v[d][0]), "=r"(v[d][1]), "=r"(v[d][2]), "=r"(v[d][3]), "=r"(v[d][4]),
+                           "=r"(v[d][5]), "=r"(v[d][6]), "=r"(v[d][7])
+                         : "r"(tl + uint32_t(64 * d + cc)));
+          asm volatile("tcgen05.wait::ld.sync.aligned;");
+          if (gm < g.M) {
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+              const int gn = n0 + cc + j;
+              if (gn >= g.N) continue;
+              long long hi = __float2int_rz(__uint_as_float(v[0][j]));
+#pragma unroll
+              for (int d = 1; d < 5; ++d) hi = hi * 128 + __float2int_rz(__uint_as_float(v[d][j]));
+              long long lo = __float2int_rz(__uint_as_float(v[5][j]));
+#pragma unroll
+              for (int d = 6; d < kPlanes; ++d) lo = lo * 128 + __float2int_rz(__uint_as_float(v[d][j]));
+              const double h = fma(__ll2double_rn(hi), 2097152.0, __ll2double_rn(lo));  // 128^3
+              double *cp = g.C + int64_t(gm) * g.ldc + gn;
+              const double base = (first_fold && !g.accumulate) ? 0.0 : *cp;
+              *cp = fma(acc_scale, h, base);
+            }
+          }
+        }
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;");
+      consumer_sync();  // TMEM read out before the next MMAs overwrite it
+      kacc = 0;
+      first_fold = false;
+    };
+
+    for (int s = 0; s < nsteps; ++s) {
+      const OzContrib &q = contribs[it.c];
+      const double scale = fabs(q.alpha) * scalbn(1.0, *q.A.exp + *q.B.exp - 61);
+      if (kacc > 0 && (scale != acc_scale || kacc + TK > kChunkK)) fold();
+      acc_scale = scale;
+      if (tid == 0 && !abort_flag) {
+        const int st = s % kStages;
+        if (!mbar_wait(smem_u32(&full[st]), uint32_t((s / kStages) & 1))) {
+          abort_flag = 1;
+        } else {
+          asm volatile("tcgen05.fence::after_thread_sync;");
+          const bool ta = q.trans & 1, tb = (q.trans >> 1) & 1;
+          const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | (uint32_t(q.alpha < 0.0) << 13) |
+                                 (uint32_t(ta) << 15) | (uint32_t(!tb) << 16) | (uint32_t(TN >> 3) << 17) |
+                                 (uint32_t(TM >> 4) << 24);
+          const uint64_t ds = d0 + uint64_t((st * kStageBytes) >> 4);
+          const uint32_t first = kacc == 0 ? 0u : 1u;
 #pragma unroll
           for (int p = 0; p < kPlanes; ++p) {
-            if (!ta) {
-              // As[m][k]: rows wm + (lane % 16), k ks + (lane / 16) * 8
-              const __nv_bfloat16 *ptr = As + (p * BM + wm + (lane & 15)) * kPitchK + ks + (lane >> 4) * 8;
-              ldsm_x4(smem_u32(ptr), fa.a[p][0], fa.a[p][1], fa.a[p][2], fa.a[p][3]);
-            } else {
-              // As[k][m]: matrix mi = lane / 8 covers k ks + (mi/2)*8, m wm + (mi%2)*8
-              const int mi = lane >> 3;
-              const __nv_bfloat16 *ptr = As + (p * BK + ks + (mi >> 1) * 8 + (lane & 7)) * kPitchMN + wm + (mi & 1) * 8;
-              ldsm_x4_t(smem_u32(ptr), fa.a[p][0], fa.a[p][1], fa.a[p][2], fa.a[p][3]);
-            }
 #pragma unroll
-            for (int x = 0; x < 4; ++x) fa.a[p][x] ^= neg;
-          }
-#pragma unroll
-          for (int qd = 0; qd < kPlanes; ++qd) {
-            uint32_t b[4][2];
-#pragma unroll
-            for (int h = 0; h < 2; ++h) {
-              // matrices (n-tile 2h, k 0-7), (2h, k 8-15), (2h+1, k 0-7), (2h+1, k 8-15)
-              const int mi = lane >> 3;
-              const int ntile = 2 * h + (mi >> 1), khalf = mi & 1;
-              uint32_t r0, r1, r2, r3;
-              if (tb) {  // Bs[n][k]
-                const __nv_bfloat16 *ptr = Bs + (qd * BN + wn + ntile * 8 + (lane & 7)) * kPitchK + ks + khalf * 8;
-                ldsm_x4(smem_u32(ptr), r0, r1, r2, r3);
-              } else {   // Bs[k][n]
-                const __nv_bfloat16 *ptr = Bs + (qd * BK + ks + khalf * 8 + (lane & 7)) * kPitchMN + wn + ntile * 8;
-                ldsm_x4_t(smem_u32(ptr), r0, r1, r2, r3);
-              }
-              b[2 * h][0] = r0;
-              b[2 * h][1] = r1;
-              b[2 * h + 1][0] = r2;
-              b[2 * h + 1][1] = r3;
-            }
-#pragma unroll
-            for (int p = 0; p < kPlanes; ++p) {
-              if (p + qd >= kPlanes) continue;
-#pragma unroll
-              for (int j = 0; j < 4; ++j) mma_bf16(acc[p + qd][j], fa.a[p], b[j][0], b[j][1]);
+            for (int qd = 0; qd < kPlanes - p; ++qd) {
+              const uint64_t ad = ds + uint64_t((p * kATile) >> 4);
+              const uint64_t bd = ds + uint64_t((kPlanes * kATile + qd * kBTile) >> 4);
+              const uint32_t acc = p > 0 ? 1u : first;  // the first pair of each group starts it
+              asm volatile(
+                  "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                  " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
+                      tmem + uint32_t(64 * (p + qd))),
+                  "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
             }
           }
+          mma_commit(smem_u32(&empty[st]));
         }
-        __syncthreads();  // this buffer may be refilled by the next stage
+      }
+      kacc += TK;
+      it.next(g, contribs);
+    }
+    if (nsteps > 0) fold();
+    if (nsteps == 0 && !g.accumulate) {  // empty contribution list: C = 0
+      for (int i = tid; i < TM * TN; i += 128) {
+        const int r = i / TN, c = i - r * TN;
+        if (m0 + r < g.M && n0 + c < g.N) g.C[int64_t(m0 + r) * g.ldc + n0 + c] = 0.0;
       }
     }
-  }
-  if (kacc > 0) fold();
-  __syncthreads();
-  for (int i = tid; i < BM * BN; i += kThreads) {
-    const int r = i / BN, col = i - r * BN;
-    const int gm = m0 + r, gn = n0 + col;
-    if (gm < g.M && gn < g.N) {
-      double *cp = g.C + int64_t(gm) * g.ldc + gn;
-      *cp = g.accumulate ? (*cp + Ct[i]) : Ct[i];
+    if (abort_flag && tid == 0) {  // let issued MMAs finish (bounded) before TMEM is released
+      mma_commit(smem_u32(&drain));
+      mbar_wait(smem_u32(&drain), drain_phase);
+      atomicExch(err, 1);
     }
   }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512));
 }
 
-constexpr size_t kGemmSmem = 4 * size_t(kTileElems) * sizeof(__nv_bfloat16) + BM * BN * sizeof(double);
+constexpr size_t kGemmSmem = size_t(kStages) * kStageBytes;
 
 }  // namespace
 
@@ -380,14 +455,14 @@ void launch_split_grid(const SplitTask *tasks, const int64_t *chunk0_max, const 
 }
 
 void launch_gemm_oz(const GemmTile *tiles, int ntiles, const OzGroup *groups, const OzContrib *contribs,
-                    cudaStream_t s) {
+                    int *err, cudaStream_t s) {
   if (ntiles == 0) return;
   static bool cfg = false;
   if (!cfg) {
     cudaFuncSetAttribute(k_gemm_oz, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kGemmSmem));
     cfg = true;
   }
-  k_gemm_oz<<<ntiles, kThreads, kGemmSmem, s>>>(tiles, groups, contribs);
+  k_gemm_oz<<<ntiles, kTcThreads, kGemmSmem, s>>>(tiles, groups, contribs, err);
 }
 
 }  // namespace nrg

@@ -149,8 +149,11 @@ void launch_split(const SplitTask *tasks, int ntasks, cudaStream_t s);
 void launch_split_grid(const SplitTask *tasks, const int64_t *chunk0_max, const int64_t *chunk0_dig,
                        int ntasks, int64_t nchunk_max, int64_t nchunk_dig, unsigned long long *maxbits,
                        cudaStream_t s);
+// tiles: (group, 128-row tile, 64-column tile); *err is set when a bounded
+// wait inside the kernel runs out (the launch then leaves its tile unfinished)
+constexpr int OZ_TILE_M = 128, OZ_TILE_N = 64;
 void launch_gemm_oz(const GemmTile *tiles, int ntiles, const OzGroup *groups, const OzContrib *contribs,
-                    cudaStream_t s);
+                    int *err, cudaStream_t s);
 
 // ------------------------------------------------------------- truncation
 struct TruncRun {

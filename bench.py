@@ -162,23 +162,29 @@ def one_run(engine, e2e, batch=None):
         if e2e:
             d2h += sum(r.all_eigenvalue.nbytes for r in runs)
     om = np.logspace(-8, 0, 801)
+    # backward passes of all runs shell by shell, the FDM of every run in one
+    # batched call per shell (the thermodynamics are host sums)
+    fs = [api.FdmSpectrum(r, 2) for r in runs]
+    ths = [api.FdmThermodynamics(r, workloads.temperature_grid()) for r in runs]
+    cnt = [r.nrg_iterations_cnt for r in runs]
+    for it in range(w["nsites"], min(min_it), -1):
+        todo = [k for k in range(B) if it > min_it[k]]
+        for k in todo:
+            cnt[k] -= 1
+            datas[k].loadCurrentData(cnt[k])
+        sc = lam ** (-(it - 1.0) / 2.0)
+        api.fdm_calc_batch([fs[k] for k in todo], [sc] * len(todo))
+        for k in todo:
+            ths[k].calcThermodynamics(sc)
     for k, run in enumerate(runs):
-        f = api.FdmSpectrum(run, 2)
-        th = api.FdmThermodynamics(run, workloads.temperature_grid())
-        cnt = run.nrg_iterations_cnt
-        for it in range(w["nsites"], min_it[k], -1):
-            cnt -= 1
-            datas[k].loadCurrentData(cnt)
-            f.calcSpectrum(lam ** (-(it - 1.0) / 2.0))
-            th.calcThermodynamics(lam ** (-(1.0 * it - 1.0) / 2.0))
-        spec = f.saveFinalData()
+        spec = fs[k].saveFinalData()
         A = [engine.broaden(spec["GreenFnEnergyPoints"], spec[key][ip], om, 0.6)
              for key in ("GreenFnPositiveWeight", "GreenFnNegativeWeight") for ip in range(2)]
-        tdat = th.saveFinalData()
+        tdat = ths[k].saveFinalData()
         d2h += spec["GreenFnPositiveWeight"].nbytes * 2 + sum(a.nbytes for a in A)
         d2h += tdat["entropy"].nbytes * 2
-        f.close()
-        th.close()
+        fs[k].close()
+        ths[k].close()
         ops[k].close()
         run.close()
     return d2h

@@ -182,6 +182,10 @@ int nrg_run_load_snapshot(nrg_run *run, int64_t iteration);
 int nrg_fdm_create(nrg_run *run, int nops, nrg_fdm **out);     /* ctor + setOperator */
 int nrg_fdm_destroy(nrg_fdm *f);
 int nrg_fdm_calc(nrg_fdm *f, double energy_scale);               /* calcSpectrum :55-63 */
+/* calcSpectrum of n FDM objects of different runs on one engine, each with
+ * its snapshot loaded, in shared launches (one per phase); same results as
+ * n nrg_fdm_calc calls.  No counterpart in the reference (it runs one). */
+int nrg_fdm_calc_batch(nrg_fdm *const *fdms, int n, const double *energy_scales);
 /* saveFinalData (:322-337): energy points and the positive/negative weights,
  * each nops x npts; npts = 100000 */
 int nrg_fdm_get(nrg_fdm *f, double *energy_points, double *positive, double *negative,

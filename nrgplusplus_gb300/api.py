@@ -67,7 +67,7 @@ EXPORTS = [
     "nrg_run_get_coupled", "nrg_run_get_eigenvectors", "nrg_run_get_fdag_block",
     "nrg_opset_create", "nrg_opset_destroy", "nrg_opset_update", "nrg_opset_get_block",
     "nrg_run_snapshot", "nrg_run_load_snapshot", "nrg_fdm_create", "nrg_fdm_destroy",
-    "nrg_fdm_calc", "nrg_fdm_get", "nrg_broaden", "nrg_thermo_create", "nrg_thermo_destroy",
+    "nrg_fdm_calc", "nrg_fdm_calc_batch", "nrg_fdm_get", "nrg_broaden", "nrg_thermo_create", "nrg_thermo_destroy",
     "nrg_thermo_calc", "nrg_thermo_final", "nrg_batch_add_site", "nrg_batch_update_state",
     "nrg_eigh_batched", "nrg_dgemm_tc", "nrg_broaden_noalloc",
     "nrg_server_create", "nrg_server_destroy", "nrg_server_submit", "nrg_server_wait",
@@ -548,6 +548,13 @@ def batch_add_site(runs, t, rescale):
     t = np.ascontiguousarray(t, float).reshape(len(runs), -1)
     rs = np.ascontiguousarray(rescale, float)
     _call(lib().nrg_batch_add_site, arr, len(runs), _dp(t), t.shape[1], _dp(rs))
+
+
+def fdm_calc_batch(fdms, scales):
+    """calcSpectrum for FDM objects of different runs in shared launches."""
+    arr = (C.c_void_p * len(fdms))(*[f.h.value for f in fdms])
+    sc = np.ascontiguousarray(scales, float)
+    _call(lib().nrg_fdm_calc_batch, arr, len(fdms), _dp(sc))
 
 
 def batch_update_state(runs):

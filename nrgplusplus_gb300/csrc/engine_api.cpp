@@ -230,220 +230,310 @@ static void opset_update(nrg_opset *o) {
 }
 
 // ------------------------------------------------------------- FDM (T = 0)
-static void fdm_calc(nrg_fdm *f, double scale) {
-  nrg_run *r = f->run;
-  if (!r->loaded) fail(NRG_E_STATE, "calcSpectrum needs a loaded snapshot");
-  nrg_engine *e = r->eng;
+// One backward-pass shell (fdmSpectrum::calcSpectrum, fdmSpectrum.hpp:55-63)
+// for every FDM object of the batch: each must belong to a different run with
+// a loaded snapshot.  All of them share one launch per phase: rho set-up,
+// digit split, the B rho / rho B GEMMs, binning, rho <- U rho U^T and the
+// partial trace.  A single object is the batch of one.
+static void fdm_calc_batch(const std::vector<nrg_fdm *> &fs, const std::vector<double> &scales) {
+  if (fs.empty()) return;
+  nrg_engine *e = fs[0]->run->eng;
   cudaStream_t s = e->stream;
-  Snapshot &S = *r->loaded;
-  SiteData &sd = *S.site;
-  const int nsec = int(sd.cur_q.size());
-  // setCurrentIndex (fdmSpectrum.hpp:289-298)
-  if (!f->have_cur) {
-    f->cur_kept.assign(nsec, 0);
-    f->have_cur = true;
-  } else {
-    f->cur_kept = f->prev_kept;
-  }
-  f->prev_kept = sd.kept_prev;
-  if (int(f->cur_kept.size()) != nsec) fail(NRG_E_STATE, "snapshot order does not match the backward pass");
-  // setRhoZero (:165-199)
-  std::vector<std::vector<double>> boltz;
-  if (f->last) {  // setLocalPartitionFunction (:122-155)
-    double gs = 0;
-    for (auto &v : sd.E_host)
-      if (!v.empty()) gs = std::min(gs, *std::min_element(v.begin(), v.end()));
-    double z = 0;
-    for (auto &v : sd.E_host)
-      for (double x : v)
-        if (std::fabs(x - gs) < kFdmEnergyErrorbar) z += 1.0;
-    boltz.resize(nsec);
-    for (int i = 0; i < nsec; ++i) {
-      boltz[i].resize(sd.E_host[i].size());
-      for (size_t x = 0; x < sd.E_host[i].size(); ++x)
-        boltz[i][x] = std::fabs(sd.E_host[i][x] - gs) < kFdmEnergyErrorbar ? 1.0 / z : 0.0;
+  const size_t nf = fs.size();
+  struct Work {
+    nrg_fdm *f;
+    SiteData *sd;
+    Snapshot *S;
+    std::vector<double *> rp, rot;
+    DevPtr rho, pm, xm, rm;
+    bool oz;
+  };
+  std::vector<Work> W(nf);
+  std::vector<DevPtr> hold;
+  // ---- setCurrentIndex (:289-298), setRhoZero (:165-199), rho blocks
+  std::vector<RhoTask> rtasks;
+  std::vector<double> diag_host;     // Boltzmann diagonals of last shells, staged once
+  std::vector<std::pair<size_t, size_t>> diag_fix;  // (task, offset into diag_host)
+  int64_t rchunks = 0;
+  for (size_t w = 0; w < nf; ++w) {
+    nrg_fdm *f = fs[w];
+    nrg_run *r = f->run;
+    if (!r->loaded) fail(NRG_E_STATE, "calcSpectrum needs a loaded snapshot");
+    if (r->eng != e) fail(NRG_E_ARG, "FDM objects of one batch must share an engine");
+    for (size_t v = 0; v < w; ++v)
+      if (fs[v]->run == r) fail(NRG_E_ARG, "FDM objects of one batch must belong to different runs");
+    Work &wk = W[w];
+    wk.f = f;
+    wk.S = r->loaded.get();
+    wk.sd = wk.S->site.get();
+    SiteData &sd = *wk.sd;
+    const int nsec = int(sd.cur_q.size());
+    if (!f->have_cur) {
+      f->cur_kept.assign(nsec, 0);
+      f->have_cur = true;
+    } else {
+      f->cur_kept = f->prev_kept;
     }
-    f->local_gs = gs;
-    f->local_z = z;
-  }
-  f->partitions.push_back(f->local_z);
-  int64_t rsz = 0;
-  for (auto &db : sd.blocks) rsz += int64_t(db.n) * db.n;
-  DevPtr rho = engine_alloc(e, rsz * sizeof(double) + 8);
-  check_cuda(cudaMemsetAsync(rho->ptr, 0, rsz * sizeof(double), s), "rho zero");
-  std::vector<double *> rp(sd.blocks.size());
-  int64_t ro = 0;
-  for (size_t b = 0; b < sd.blocks.size(); ++b) {
-    const DevBlock &db = sd.blocks[b];
-    rp[b] = static_cast<double *>(rho->ptr) + ro;
-    ro += int64_t(db.n) * db.n;
-    if (f->last)
-      check_cuda(cudaMemcpy2DAsync(rp[b], (db.n + 1) * sizeof(double), boltz[db.sector].data(),
-                                   sizeof(double), sizeof(double), db.n, cudaMemcpyHostToDevice, s),
-                 "rho diag");
-    if (f->have_reduced) {
-      const int kc = int(f->cur_kept[db.sector]);
-      if (kc > 0) {
-        if (f->reduced_k[db.sector] != kc) fail(NRG_E_STATE, "reduced density matrix size mismatch");
-        check_cuda(cudaMemcpy2DAsync(rp[b], db.n * sizeof(double), f->reduced[db.sector],
-                                     kc * sizeof(double), kc * sizeof(double), kc,
-                                     cudaMemcpyDeviceToDevice, s),
-                   "rho kept block");
+    f->prev_kept = sd.kept_prev;
+    if (int(f->cur_kept.size()) != nsec) fail(NRG_E_STATE, "snapshot order does not match the backward pass");
+    std::vector<std::vector<double>> boltz;
+    if (f->last) {  // setLocalPartitionFunction (:122-155)
+      double gs = 0;
+      for (auto &v : sd.E_host)
+        if (!v.empty()) gs = std::min(gs, *std::min_element(v.begin(), v.end()));
+      double z = 0;
+      for (auto &v : sd.E_host)
+        for (double x : v)
+          if (std::fabs(x - gs) < kFdmEnergyErrorbar) z += 1.0;
+      boltz.resize(nsec);
+      for (int i = 0; i < nsec; ++i) {
+        boltz[i].resize(sd.E_host[i].size());
+        for (size_t x = 0; x < sd.E_host[i].size(); ++x)
+          boltz[i][x] = std::fabs(sd.E_host[i][x] - gs) < kFdmEnergyErrorbar ? 1.0 / z : 0.0;
       }
+      f->local_gs = gs;
+      f->local_z = z;
     }
+    f->partitions.push_back(f->local_z);
+    int64_t rsz = 0;
+    for (auto &db : sd.blocks) rsz += int64_t(db.n) * db.n;
+    wk.rho = engine_alloc(e, rsz * sizeof(double) + 8);
+    wk.rp.resize(sd.blocks.size());
+    int64_t ro = 0;
+    for (size_t b = 0; b < sd.blocks.size(); ++b) {
+      const DevBlock &db = sd.blocks[b];
+      wk.rp[b] = static_cast<double *>(wk.rho->ptr) + ro;
+      ro += int64_t(db.n) * db.n;
+      RhoTask t{};
+      t.rho = wk.rp[b];
+      t.n = db.n;
+      if (f->last) {
+        diag_fix.push_back({rtasks.size(), diag_host.size()});
+        diag_host.insert(diag_host.end(), boltz[db.sector].begin(), boltz[db.sector].end());
+      }
+      if (f->have_reduced) {
+        const int kc = int(f->cur_kept[db.sector]);
+        if (kc > 0) {
+          if (f->reduced_k[db.sector] != kc) fail(NRG_E_STATE, "reduced density matrix size mismatch");
+          t.red = f->reduced[db.sector];
+          t.kc = kc;
+        }
+      }
+      t.chunk0 = rchunks;
+      rchunks += (int64_t(db.n) * db.n + 255) / 256;
+      rtasks.push_back(t);
+    }
+    wk.oz = sd.has_uplanes;
   }
-  // rhoDotOperators (:207-277): B rho_j and rho_i B, then binning
-  GemmBatch g;
-  std::vector<FdmPair> pairs;
-  int64_t psz = 0;
-  for (auto &kv : S.ops) {
-    const int i = std::get<1>(kv.first), j = std::get<2>(kv.first);
-    if (sd.sectors[i].dev < 0 || sd.sectors[j].dev < 0) continue;
-    psz += 2 * int64_t(sd.blocks[sd.sectors[i].dev].n) * sd.blocks[sd.sectors[j].dev].n;
+  if (!rtasks.empty()) {
+    DevPtr dd;
+    if (!diag_host.empty()) {
+      Staged sd0;
+      size_t od = sd0.add(diag_host);
+      char *dp = sd0.push(e, dd);
+      for (auto &fx : diag_fix) rtasks[fx.first].diag = at<double>(dp, od) + fx.second;
+    }
+    Staged st;
+    size_t ot = st.add(rtasks);
+    DevPtr h;
+    char *d = st.push(e, h);
+    launch_rho_init(at<RhoTask>(d, ot), int(rtasks.size()), rchunks, s);
+    engine_count_launch(e, 1);
+    check_cuda(cudaGetLastError(), "rho init");
+    hold.push_back(dd);
+    hold.push_back(h);
   }
-  DevPtr pm = engine_alloc(e, psz * sizeof(double) + 8);
-  int64_t po = 0, chunk = 0;
-  // tensor-core variant (mixed path): digit planes of rho and of the operator blocks
-  const bool oz = sd.has_uplanes;
-  std::vector<DevPtr> ozhold;
-  PlaneBuf prho, pB;
-  std::map<const double *, size_t> bidx;
-  OzList ozg;
-  if (oz) {
-    std::vector<MatRef> rm, bm;
-    for (size_t b = 0; b < sd.blocks.size(); ++b) rm.push_back(MatRef{rp[b], sd.blocks[b].n, sd.blocks[b].n, sd.blocks[b].n});
-    for (auto &kv : S.ops) {
+  // ---- rhoDotOperators (:207-277): B rho_j and rho_i B, then binning
+  const bool oz = W[0].oz;
+  for (auto &wk : W)
+    if (wk.oz != oz) fail(NRG_E_ARG, "FDM objects of one batch must share the precision path");
+  std::vector<MatRef> rmats, bmats;
+  std::vector<size_t> r0(nf), b0(nf);
+  std::vector<std::map<const double *, size_t>> bidx(nf);
+  for (size_t w = 0; w < nf; ++w) {
+    Work &wk = W[w];
+    SiteData &sd = *wk.sd;
+    r0[w] = rmats.size();
+    b0[w] = bmats.size();
+    for (size_t b = 0; b < sd.blocks.size(); ++b)
+      rmats.push_back(MatRef{wk.rp[b], sd.blocks[b].n, sd.blocks[b].n, sd.blocks[b].n});
+    for (auto &kv : wk.S->ops) {
       const int i = std::get<1>(kv.first), j = std::get<2>(kv.first);
       if (sd.sectors[i].dev < 0 || sd.sectors[j].dev < 0) continue;
-      bidx[kv.second.p] = bm.size();
-      bm.push_back(MatRef{kv.second.p, kv.second.rows, kv.second.cols, kv.second.ld});
+      bidx[w][kv.second.p] = bmats.size() - b0[w];
+      bmats.push_back(MatRef{kv.second.p, kv.second.rows, kv.second.cols, kv.second.ld});
     }
-    prho = split_matrices(e, rm, ozhold);
-    pB = split_matrices(e, bm, ozhold);
   }
-  for (auto &kv : S.ops) {
-    const int ip = std::get<0>(kv.first), i = std::get<1>(kv.first), j = std::get<2>(kv.first);
-    if (ip < 0 || ip >= f->nops) fail(NRG_E_ARG, "snapshot operator index exceeds the FDM operator count");
-    if (sd.sectors[i].dev < 0 || sd.sectors[j].dev < 0) continue;
-    const int bi = sd.sectors[i].dev, bj = sd.sectors[j].dev;
-    const DevBlock &Bi = sd.blocks[bi], &Bj = sd.blocks[bj];
-    const FBlock &B = kv.second;
-    double *rhoA = static_cast<double *>(pm->ptr) + po;
-    po += int64_t(Bi.n) * Bj.n;
-    double *ARho = static_cast<double *>(pm->ptr) + po;
-    po += int64_t(Bi.n) * Bj.n;
-    if (oz) {
-      const size_t q = bidx.at(B.p);
-      ozg.out(rhoA, Bj.n, Bi.n, Bj.n, false, {ozc(pB.op(q), prho.op(bj), Bj.n, 0)});
-      ozg.out(ARho, Bj.n, Bi.n, Bj.n, false, {ozc(prho.op(bi), pB.op(q), Bi.n, 0)});
-    } else {
-      g.out(rhoA, Bj.n, Bi.n, Bj.n, false, {gc(B.p, B.ld, rp[bj], Bj.n, Bj.n, 0, 1.0)});
-      g.out(ARho, Bj.n, Bi.n, Bj.n, false, {gc(rp[bi], Bi.n, B.p, B.ld, Bi.n, 0, 1.0)});
+  PlaneBuf prho, pB;
+  if (oz) {
+    prho = split_matrices(e, rmats, hold);
+    pB = split_matrices(e, bmats, hold);
+  }
+  GemmBatch g;
+  OzList ozg;
+  std::vector<FdmPair> pairs;
+  int64_t chunk = 0;
+  for (size_t w = 0; w < nf; ++w) {
+    Work &wk = W[w];
+    nrg_fdm *f = wk.f;
+    SiteData &sd = *wk.sd;
+    int64_t psz = 0;
+    for (auto &kv : wk.S->ops) {
+      const int i = std::get<1>(kv.first), j = std::get<2>(kv.first);
+      if (sd.sectors[i].dev < 0 || sd.sectors[j].dev < 0) continue;
+      psz += 2 * int64_t(sd.blocks[sd.sectors[i].dev].n) * sd.blocks[sd.sectors[j].dev].n;
     }
-    FdmPair fp{};
-    fp.rhoA = rhoA;
-    fp.ARho = ARho;
-    fp.B = B.p;
-    fp.Ei = Bi.E;
-    fp.Ej = Bj.E;
-    fp.ni = Bi.n;
-    fp.nj = Bj.n;
-    fp.kci = int(f->cur_kept[i]);
-    fp.kcj = int(f->cur_kept[j]);
-    fp.op = ip;
-    fp.chunk0 = chunk;
-    chunk += (int64_t(Bi.n) * Bj.n + 255) / 256;
-    pairs.push_back(fp);
-    if (B.ld != Bj.n) fail(NRG_E_STATE, "operator block layout");
+    wk.pm = engine_alloc(e, psz * sizeof(double) + 8);
+    int64_t po = 0;
+    double *hist = static_cast<double *>(f->hist->ptr);
+    for (auto &kv : wk.S->ops) {
+      const int ip = std::get<0>(kv.first), i = std::get<1>(kv.first), j = std::get<2>(kv.first);
+      if (ip < 0 || ip >= f->nops) fail(NRG_E_ARG, "snapshot operator index exceeds the FDM operator count");
+      if (sd.sectors[i].dev < 0 || sd.sectors[j].dev < 0) continue;
+      const int bi = sd.sectors[i].dev, bj = sd.sectors[j].dev;
+      const DevBlock &Bi = sd.blocks[bi], &Bj = sd.blocks[bj];
+      const FBlock &B = kv.second;
+      if (B.ld != Bj.n) fail(NRG_E_STATE, "operator block layout");
+      double *rhoA = static_cast<double *>(wk.pm->ptr) + po;
+      po += int64_t(Bi.n) * Bj.n;
+      double *ARho = static_cast<double *>(wk.pm->ptr) + po;
+      po += int64_t(Bi.n) * Bj.n;
+      if (oz) {
+        const size_t q = b0[w] + bidx[w].at(B.p);
+        ozg.out(rhoA, Bj.n, Bi.n, Bj.n, false, {ozc(pB.op(q), prho.op(r0[w] + bj), Bj.n, 0)});
+        ozg.out(ARho, Bj.n, Bi.n, Bj.n, false, {ozc(prho.op(r0[w] + bi), pB.op(q), Bi.n, 0)});
+      } else {
+        g.out(rhoA, Bj.n, Bi.n, Bj.n, false, {gc(B.p, B.ld, wk.rp[bj], Bj.n, Bj.n, 0, 1.0)});
+        g.out(ARho, Bj.n, Bi.n, Bj.n, false, {gc(wk.rp[bi], Bi.n, B.p, B.ld, Bi.n, 0, 1.0)});
+      }
+      FdmPair fp{};
+      fp.rhoA = rhoA;
+      fp.ARho = ARho;
+      fp.B = B.p;
+      fp.Ei = Bi.E;
+      fp.Ej = Bj.E;
+      fp.pos = hist + int64_t(ip) * kFdmPts;
+      fp.neg = hist + (int64_t(f->nops) + ip) * kFdmPts;
+      fp.scale = scales[w];
+      fp.ni = Bi.n;
+      fp.nj = Bj.n;
+      fp.kci = int(f->cur_kept[i]);
+      fp.kcj = int(f->cur_kept[j]);
+      fp.chunk0 = chunk;
+      chunk += (int64_t(Bi.n) * Bj.n + 255) / 256;
+      pairs.push_back(fp);
+    }
   }
   g.run(e);
-  ozg.launch(e, ozhold);
+  ozg.launch(e, hold);
   if (!pairs.empty()) {
     Staged st;
     size_t op = st.add(pairs);
-    DevPtr hold;
-    char *d = st.push(e, hold);
-    double *hist = static_cast<double *>(f->hist->ptr);
+    DevPtr h;
+    char *d = st.push(e, h);
+    hold.push_back(h);
     Prof pf(e, "k_fdm_bin");
-    launch_fdm_bin(at<FdmPair>(d, op), int(pairs.size()), chunk, scale, fdm_delE(), hist,
-                   hist + int64_t(f->nops) * kFdmPts, kFdmPts, s);
+    launch_fdm_bin(at<FdmPair>(d, op), int(pairs.size()), chunk, fdm_delE(), kFdmPts, s);
     engine_count_launch(e, 1);
     check_cuda(cudaGetLastError(), "fdm binning");
   }
-  // setReduceDensityMatrix (:71-114): rho <- U rho U^T, then the partial trace
-  DevPtr xm = engine_alloc(e, rsz * sizeof(double) + 8), rm = engine_alloc(e, rsz * sizeof(double) + 8);
+  // ---- setReduceDensityMatrix (:71-114): rho <- U rho U^T, then the partial trace
   GemmBatch g1, g2;
   OzList o1, o2;
-  std::vector<double *> rot(sd.blocks.size());
   std::vector<MatRef> xmats;
-  int64_t xo = 0;
-  for (size_t b = 0; b < sd.blocks.size(); ++b) {
-    const DevBlock &db = sd.blocks[b];
-    double *X = static_cast<double *>(xm->ptr) + xo;
-    rot[b] = static_cast<double *>(rm->ptr) + xo;
-    xo += int64_t(db.n) * db.n;
-    if (oz) {
-      o1.out(X, db.n, db.n, db.n, false, {ozc(prho.op(b), db.uop, db.n, 2)});  // rho U^T
-      xmats.push_back(MatRef{X, db.n, db.n, db.n});
-      continue;
-    }
-    g1.out(X, db.n, db.n, db.n, false, {gc(rp[b], db.n, db.U, db.ld, db.n, 2, 1.0)});  // rho U^T
-    g2.out(rot[b], db.n, db.n, db.n, false, {gc(db.U, db.ld, X, db.n, db.n, 0, 1.0)});  // U X
-  }
-  if (oz) {
-    o1.launch(e, ozhold);
-    PlaneBuf px = split_matrices(e, xmats, ozhold);
+  for (size_t w = 0; w < nf; ++w) {
+    Work &wk = W[w];
+    SiteData &sd = *wk.sd;
+    int64_t rsz = 0;
+    for (auto &db : sd.blocks) rsz += int64_t(db.n) * db.n;
+    wk.xm = engine_alloc(e, rsz * sizeof(double) + 8);
+    wk.rm = engine_alloc(e, rsz * sizeof(double) + 8);
+    wk.rot.resize(sd.blocks.size());
+    int64_t xo = 0;
     for (size_t b = 0; b < sd.blocks.size(); ++b) {
       const DevBlock &db = sd.blocks[b];
-      o2.out(rot[b], db.n, db.n, db.n, false, {ozc(db.uop, px.op(b), db.n, 0)});  // U X
+      double *X = static_cast<double *>(wk.xm->ptr) + xo;
+      wk.rot[b] = static_cast<double *>(wk.rm->ptr) + xo;
+      xo += int64_t(db.n) * db.n;
+      if (oz) {
+        o1.out(X, db.n, db.n, db.n, false, {ozc(prho.op(r0[w] + b), db.uop, db.n, 2)});  // rho U^T
+        xmats.push_back(MatRef{X, db.n, db.n, db.n});
+        continue;
+      }
+      g1.out(X, db.n, db.n, db.n, false, {gc(wk.rp[b], db.n, db.U, db.ld, db.n, 2, 1.0)});  // rho U^T
+      g2.out(wk.rot[b], db.n, db.n, db.n, false, {gc(db.U, db.ld, X, db.n, db.n, 0, 1.0)});  // U X
     }
-    o2.launch(e, ozhold);
+  }
+  if (oz) {
+    o1.launch(e, hold);
+    PlaneBuf px = split_matrices(e, xmats, hold);
+    size_t q = 0;
+    for (size_t w = 0; w < nf; ++w) {
+      SiteData &sd = *W[w].sd;
+      for (size_t b = 0; b < sd.blocks.size(); ++b, ++q) {
+        const DevBlock &db = sd.blocks[b];
+        o2.out(W[w].rot[b], db.n, db.n, db.n, false, {ozc(db.uop, px.op(q), db.n, 0)});  // U X
+      }
+    }
+    o2.launch(e, hold);
   } else {
     g1.run(e);
     g2.run(e);
   }
-  const int npre = int(sd.pre_q.size());
-  std::vector<DevPtr> red_mem(npre);
-  std::vector<double *> red(npre, nullptr);
-  std::vector<int64_t> red_k(npre, 0);
-  std::vector<std::vector<TraceIn>> ins(npre);
-  for (int i = 0; i < nsec; ++i) {
-    const Sector &Sc = sd.sectors[i];
-    if (Sc.dev < 0) continue;
-    for (auto &sb : Sc.subs) ins[sb.ii].push_back({rot[Sc.dev], sd.blocks[Sc.dev].n, sb.off, sb.d, 0});
-  }
   std::vector<TraceTask> tasks;
   std::vector<TraceIn> flat;
   int maxk = 0;
-  for (int ii = 0; ii < npre; ++ii) {
-    const int k = int(sd.kept_prev[ii]);
-    red_k[ii] = k;
-    if (k == 0) continue;
-    red_mem[ii] = engine_alloc(e, int64_t(k) * k * sizeof(double));
-    red[ii] = static_cast<double *>(red_mem[ii]->ptr);
-    TraceTask t{};
-    t.out = red[ii];
-    t.k = k;
-    t.in0 = int(flat.size());
-    flat.insert(flat.end(), ins[ii].begin(), ins[ii].end());
-    t.in1 = int(flat.size());
-    tasks.push_back(t);
-    maxk = std::max(maxk, k);
+  std::vector<std::vector<DevPtr>> red_mem(nf);
+  std::vector<std::vector<double *>> red(nf);
+  std::vector<std::vector<int64_t>> red_k(nf);
+  for (size_t w = 0; w < nf; ++w) {
+    Work &wk = W[w];
+    SiteData &sd = *wk.sd;
+    const int npre = int(sd.pre_q.size());
+    const int nsec = int(sd.cur_q.size());
+    red_mem[w].resize(npre);
+    red[w].assign(npre, nullptr);
+    red_k[w].assign(npre, 0);
+    std::vector<std::vector<TraceIn>> ins(npre);
+    for (int i = 0; i < nsec; ++i) {
+      const Sector &Sc = sd.sectors[i];
+      if (Sc.dev < 0) continue;
+      for (auto &sb : Sc.subs) ins[sb.ii].push_back({wk.rot[Sc.dev], sd.blocks[Sc.dev].n, sb.off, sb.d, 0});
+    }
+    for (int ii = 0; ii < npre; ++ii) {
+      const int k = int(sd.kept_prev[ii]);
+      red_k[w][ii] = k;
+      if (k == 0) continue;
+      red_mem[w][ii] = engine_alloc(e, int64_t(k) * k * sizeof(double));
+      red[w][ii] = static_cast<double *>(red_mem[w][ii]->ptr);
+      TraceTask t{};
+      t.out = red[w][ii];
+      t.k = k;
+      t.in0 = int(flat.size());
+      flat.insert(flat.end(), ins[ii].begin(), ins[ii].end());
+      t.in1 = int(flat.size());
+      tasks.push_back(t);
+      maxk = std::max(maxk, k);
+    }
   }
   if (!tasks.empty()) {
     Staged st;
     size_t ot = st.add(tasks), oi = st.add(flat);
-    DevPtr hold;
-    char *d = st.push(e, hold);
+    DevPtr h;
+    char *d = st.push(e, h);
+    hold.push_back(h);
     launch_partial_trace(at<TraceTask>(d, ot), int(tasks.size()), at<TraceIn>(d, oi), maxk, s);
     engine_count_launch(e, 1);
     check_cuda(cudaGetLastError(), "partial trace");
   }
-  f->reduced_mem = std::move(red_mem);
-  f->reduced = std::move(red);
-  f->reduced_k = std::move(red_k);
-  f->have_reduced = true;
-  f->last = false;
+  for (size_t w = 0; w < nf; ++w) {
+    nrg_fdm *f = W[w].f;
+    f->reduced_mem = std::move(red_mem[w]);
+    f->reduced = std::move(red[w]);
+    f->reduced_k = std::move(red_k[w]);
+    f->have_reduced = true;
+    f->last = false;
+  }
   // no synchronisation: every buffer above is freed stream-ordered and every
   // host array was staged by its copy call, so the host may queue the next
   // shell while this one runs (errors surface at the next synchronising call)
@@ -923,7 +1013,17 @@ int nrg_fdm_destroy(nrg_fdm *f) {
 int nrg_fdm_calc(nrg_fdm *f, double scale) {
   return guard([&] {
     if (!f) fail(NRG_E_ARG, "null fdm");
-    fdm_calc(f, scale);
+    fdm_calc_batch({f}, {scale});
+  });
+}
+
+int nrg_fdm_calc_batch(nrg_fdm *const *fs, int n, const double *scales) {
+  return guard([&] {
+    if (n < 0 || (n > 0 && (!fs || !scales))) fail(NRG_E_ARG, "bad argument");
+    std::vector<nrg_fdm *> v(fs, fs + n);
+    for (auto *f : v)
+      if (!f) fail(NRG_E_ARG, "null fdm");
+    fdm_calc_batch(v, std::vector<double>(scales, scales + n));
   });
 }
 

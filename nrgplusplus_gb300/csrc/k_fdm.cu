@@ -14,8 +14,7 @@ constexpr double kFdmWeightErrorbar = 1e-20;  // fdmSpectrum.hpp:343
 //   w+ = |(B rho_j)(v,v') A(v',v)|,  w- = |(rho_i B)(v,v') A(v',v)|
 //   bin = int(ln(1 + |s (E_i[v] - E_j[v'])| / 1e-10) * delE)
 // Weights above 1e-20 in bins [0, npts) are added to the op's histograms.
-__global__ void k_fdm_bin(const FdmPair *__restrict__ pairs, int npairs, double scale, double delE,
-                          double *__restrict__ pos, double *__restrict__ neg, int npts) {
+__global__ void k_fdm_bin(const FdmPair *__restrict__ pairs, int npairs, double delE, int npts) {
   const int64_t chunk = blockIdx.x;
   int lo = 0, hi = npairs - 1;
   while (lo < hi) {
@@ -31,11 +30,32 @@ __global__ void k_fdm_bin(const FdmPair *__restrict__ pairs, int npairs, double 
   const double a = P.B[e];
   const double aa = P.rhoA[e] * a;
   const double bv = P.ARho[e] * a;
-  const int bin = int(log(1 + (fabs(scale * (P.Ei[iv] - P.Ej[ivp])) / kFdmMinEnergy)) * delE);
+  const int bin = int(log(1 + (fabs(P.scale * (P.Ei[iv] - P.Ej[ivp])) / kFdmMinEnergy)) * delE);
   if (bin < npts && bin >= 0) {
-    if (fabs(aa) > kFdmWeightErrorbar) atomicAdd(pos + int64_t(P.op) * npts + bin, fabs(aa));
-    if (fabs(bv) > kFdmWeightErrorbar) atomicAdd(neg + int64_t(P.op) * npts + bin, fabs(bv));
+    if (fabs(aa) > kFdmWeightErrorbar) atomicAdd(P.pos + bin, fabs(aa));
+    if (fabs(bv) > kFdmWeightErrorbar) atomicAdd(P.neg + bin, fabs(bv));
   }
+}
+
+// One shell's density-matrix blocks, written whole (no separate zeroing):
+// the reduced density matrix of the later shell in the kept x kept corner,
+// the Boltzmann weights on the diagonal of the last shell, zero elsewhere
+// (fdmSpectrum::setRhoZero, fdmSpectrum.hpp:165-199).
+__global__ void k_rho_init(const RhoTask *__restrict__ tasks, int ntasks) {
+  const int64_t chunk = blockIdx.x;
+  int lo = 0, hi = ntasks - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (tasks[mid].chunk0 <= chunk) lo = mid; else hi = mid - 1;
+  }
+  const RhoTask T = tasks[lo];
+  const int64_t e = (chunk - T.chunk0) * blockDim.x + threadIdx.x;
+  if (e >= int64_t(T.n) * T.n) return;
+  const int r = int(e / T.n), c = int(e - int64_t(r) * T.n);
+  double v = 0.0;
+  if (T.red && r < T.kc && c < T.kc) v = T.red[int64_t(r) * T.kc + c];
+  else if (T.diag && r == c) v = T.diag[r];
+  T.rho[e] = v;
 }
 
 // reducedRho[ii](it,it') = sum over the sub-blocks (ii, bb) of every block
@@ -151,10 +171,14 @@ __global__ void k_thermo(const double *__restrict__ disc, const int64_t *__restr
 
 }  // namespace
 
-void launch_fdm_bin(const FdmPair *pairs, int npairs, int64_t nchunks, double scale, double delE,
-                    double *pos, double *neg, int npts, cudaStream_t s) {
+void launch_fdm_bin(const FdmPair *pairs, int npairs, int64_t nchunks, double delE, int npts, cudaStream_t s) {
   if (npairs == 0 || nchunks == 0) return;
-  k_fdm_bin<<<unsigned(nchunks), 256, 0, s>>>(pairs, npairs, scale, delE, pos, neg, npts);
+  k_fdm_bin<<<unsigned(nchunks), 256, 0, s>>>(pairs, npairs, delE, npts);
+}
+
+void launch_rho_init(const RhoTask *tasks, int ntasks, int64_t nchunks, cudaStream_t s) {
+  if (ntasks == 0 || nchunks == 0) return;
+  k_rho_init<<<unsigned(nchunks), 256, 0, s>>>(tasks, ntasks);
 }
 
 void launch_partial_trace(const TraceTask *tasks, int ntask, const TraceIn *ins, int maxk,

@@ -181,13 +181,22 @@ struct FdmPair {          // one (op, i, j) spectral contribution
   const double *ARho;     // rho_i B   (n_i x n_j, ld nj)
   const double *B;        // operator block (n_i x n_j, ld nj)
   const double *Ei, *Ej;  // eigenvalues of blocks i and j
+  double *pos, *neg;      // this op's histograms (npts each) of the pair's run
+  double scale;           // energy scale of the pair's shell
   int ni, nj, kci, kcj;   // sizes and current kept counts
-  int op, pad;
   int64_t chunk0;
 };
 // chunks of 256 elements; chunk0 of each pair is increasing
-void launch_fdm_bin(const FdmPair *pairs, int npairs, int64_t nchunks, double scale, double delE,
-                    double *pos, double *neg, int npts, cudaStream_t s);
+void launch_fdm_bin(const FdmPair *pairs, int npairs, int64_t nchunks, double delE, int npts, cudaStream_t s);
+struct RhoTask {          // one n x n block of a shell's density matrix
+  double *rho;
+  const double *diag;     // last shell: Boltzmann weights on the diagonal (or null)
+  const double *red;      // earlier shells: reduced density matrix, kc x kc (or null)
+  int n, kc;
+  int64_t chunk0;         // prefix of 256-element chunks
+};
+// rho = red in the kept x kept corner, diag on the diagonal elsewhere, 0 otherwise
+void launch_rho_init(const RhoTask *tasks, int ntasks, int64_t nchunks, cudaStream_t s);
 struct TraceTask {        // one reduced-density-matrix output (k x k)
   double *out;
   int k, in0, in1, pad;

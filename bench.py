@@ -152,8 +152,8 @@ def one_run(engine, e2e, batch=None):
     min_it = [0] * B
     for it in range(w["nsites"]):
         api.batch_add_site(runs, [[M.hopping(it, lam)] * 2] * B, [math.sqrt(lam) if it > 0 else 1.0] * B)
+        api.update_system_operator_batch(runs, ops)
         for k in range(B):
-            api.update_system_operator(runs[k], ops[k])
             if runs[k].checkHigherEnergyDiscarded():
                 datas[k].saveCurrentData(ops[k])
             else:

@@ -167,6 +167,10 @@ int nrg_opset_create(nrg_run *run, const nrg_op_desc *ops, nrg_opset **out);
 int nrg_opset_destroy(nrg_opset *ops);
 /* update_system_operator(nrg, ops): call after add_site, before update_state */
 int nrg_opset_update(nrg_opset *ops);
+/* update_system_operator for n operator sets (of runs on one engine, each
+ * after its add_site) in shared launches; same results as n calls.  No
+ * counterpart in the reference. */
+int nrg_opset_update_batch(nrg_opset *const *ops, int n);
 /* block (ip, i, j) of the tracked operator in the current basis */
 int nrg_opset_get_block(nrg_opset *ops, int ip, int64_t i, int64_t j, double *out, uint64_t cap,
                         int64_t *rows, int64_t *cols);

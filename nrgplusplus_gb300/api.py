@@ -65,7 +65,7 @@ EXPORTS = [
     "nrg_run_check_discarded", "nrg_run_get_info", "nrg_run_get_all_eigenvalues",
     "nrg_run_get_relgs", "nrg_run_get_sectors", "nrg_run_get_eigenvalues_q", "nrg_run_get_kept",
     "nrg_run_get_coupled", "nrg_run_get_eigenvectors", "nrg_run_get_fdag_block",
-    "nrg_opset_create", "nrg_opset_destroy", "nrg_opset_update", "nrg_opset_get_block",
+    "nrg_opset_create", "nrg_opset_destroy", "nrg_opset_update", "nrg_opset_update_batch", "nrg_opset_get_block",
     "nrg_run_snapshot", "nrg_run_load_snapshot", "nrg_fdm_create", "nrg_fdm_destroy",
     "nrg_fdm_calc", "nrg_fdm_calc_batch", "nrg_fdm_get", "nrg_broaden", "nrg_thermo_create", "nrg_thermo_destroy",
     "nrg_thermo_calc", "nrg_thermo_final", "nrg_batch_add_site", "nrg_batch_update_state",
@@ -548,6 +548,12 @@ def batch_add_site(runs, t, rescale):
     t = np.ascontiguousarray(t, float).reshape(len(runs), -1)
     rs = np.ascontiguousarray(rescale, float)
     _call(lib().nrg_batch_add_site, arr, len(runs), _dp(t), t.shape[1], _dp(rs))
+
+
+def update_system_operator_batch(runs, opsets):
+    """update_system_operator for several runs' operator sets in shared launches."""
+    arr = (C.c_void_p * len(opsets))(*[o.h.value for o in opsets])
+    _call(lib().nrg_opset_update_batch, arr, len(opsets))
 
 
 def fdm_calc_batch(fdms, scales):

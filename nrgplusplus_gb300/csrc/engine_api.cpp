@@ -108,126 +108,139 @@ static GemmContrib gc(const double *A, int lda, const double *B, int ldb, int K,
 // O_new(i,j) = sum over sub-block pairs with the same bath sector bb of
 // U_i[rows (ii,bb,il)]^T O_prev(ii,ii')[:k,:k'] U_j[rows (ii',bb,il)]
 // (sysOperator.hpp:36-133), as two grouped-GEMM passes through Y = O U_j.
-static void opset_update(nrg_opset *o) {
-  nrg_run *r = o->run;
-  if (!r->have_site) fail(NRG_E_STATE, "update_system_operator needs add_site first");
-  nrg_engine *e = r->eng;
-  SiteData &sd = *r->site;
-  const SiteModel &bath = r->bath;
-  const int nb = int(bath.q.size());
-  std::map<std::pair<int, int>, std::pair<int, int>> sub_of;
-  for (size_t s = 0; s < sd.sectors.size(); ++s)
-    for (auto &sb : sd.sectors[s].subs) sub_of[{sb.ii, sb.bb}] = {int(s), sb.off};
-  struct YTask {
-    int ip, si, sj, off_i, k;
-    double *Y;
-    int ldy;
+static void opset_update_batch(const std::vector<nrg_opset *> &os) {
+  if (os.empty()) return;
+  nrg_engine *e = os[0]->run->eng;
+  struct P1 { size_t o; OzOperand u; int kp, k, nj; double *Y; };
+  struct Per {
+    nrg_opset *o;
+    std::map<OpKey, FBlock> nb_blocks;
+    DevPtr ymem, omem;
+    std::map<OpKey, std::vector<GemmContrib>> p2c;
+    std::vector<P1> p1oz;
+    std::map<OpKey, std::vector<std::pair<OzOperand, size_t>>> p2oz;  // (U_i rows, Y index)
   };
-  std::vector<YTask> yt;
+  std::vector<Per> P(os.size());
   GemmBatch p1, p2;
-  int64_t ysz = 0;
-  std::vector<std::tuple<const FBlock *, int, int, int, int, int, int>> pend;  // block, ip, ii, iip, bb, il
-  std::map<OpKey, int> outs;
-  for (auto &kv : o->blocks) {
-    const int ip = std::get<0>(kv.first), ii = std::get<1>(kv.first), iip = std::get<2>(kv.first);
-    const int k = int(r->kept[ii]), kp = int(r->kept[iip]);
-    for (int bb = 0; bb < nb; ++bb) {
-      auto a = sub_of.find({ii, bb});
-      auto b = sub_of.find({iip, bb});
-      // the output block exists whenever both sub-blocks do (hasValue, :244-248)
-      const int si = a != sub_of.end() ? a->second.first : -1;
-      const int sj = b != sub_of.end() ? b->second.first : -1;
-      if (si < 0 || sj < 0) continue;
-      outs.emplace(OpKey{ip, si, sj}, 0);
-      if (k == 0 || kp == 0) continue;
-      for (int il = 0; il < int(bath.E[bb].size()); ++il) {
-        pend.emplace_back(&kv.second, ip, ii, iip, bb, il, 0);
-        ysz += int64_t(k) * sd.blocks[sd.sectors[sj].dev].n;
+  std::vector<MatRef> omats, ymats;
+  bool oz = false;
+  for (size_t w = 0; w < os.size(); ++w) {
+    nrg_opset *o = os[w];
+    Per &pw = P[w];
+    pw.o = o;
+    nrg_run *r = o->run;
+    if (!r->have_site) fail(NRG_E_STATE, "update_system_operator needs add_site first");
+    if (r->eng != e) fail(NRG_E_ARG, "operator sets of one batch must share an engine");
+    SiteData &sd = *r->site;
+    if (w == 0) oz = sd.has_uplanes;
+    else if (oz != sd.has_uplanes) fail(NRG_E_ARG, "operator sets of one batch must share the precision path");
+    const SiteModel &bath = r->bath;
+    const int nb = int(bath.q.size());
+    std::map<std::pair<int, int>, std::pair<int, int>> sub_of;
+    for (size_t s = 0; s < sd.sectors.size(); ++s)
+      for (auto &sb : sd.sectors[s].subs) sub_of[{sb.ii, sb.bb}] = {int(s), sb.off};
+    int64_t ysz = 0;
+    std::vector<std::tuple<const FBlock *, int, int, int, int, int>> pend;  // block, ip, ii, iip, bb, il
+    std::map<OpKey, int> outs;
+    for (auto &kv : o->blocks) {
+      const int ip = std::get<0>(kv.first), ii = std::get<1>(kv.first), iip = std::get<2>(kv.first);
+      const int k = int(r->kept[ii]), kp = int(r->kept[iip]);
+      for (int bb = 0; bb < nb; ++bb) {
+        auto a = sub_of.find({ii, bb});
+        auto b = sub_of.find({iip, bb});
+        // the output block exists whenever both sub-blocks do (hasValue, :244-248)
+        const int si = a != sub_of.end() ? a->second.first : -1;
+        const int sj = b != sub_of.end() ? b->second.first : -1;
+        if (si < 0 || sj < 0) continue;
+        outs.emplace(OpKey{ip, si, sj}, 0);
+        if (k == 0 || kp == 0) continue;
+        for (int il = 0; il < int(bath.E[bb].size()); ++il) {
+          pend.emplace_back(&kv.second, ip, ii, iip, bb, il);
+          ysz += int64_t(k) * sd.blocks[sd.sectors[sj].dev].n;
+        }
       }
     }
-  }
-  DevPtr ymem = engine_alloc(e, ysz * sizeof(double) + 8);
-  int64_t yo = 0;
-  std::map<OpKey, std::vector<GemmContrib>> p2c;
-  // tensor-core variant (mixed path): digit planes of the O views and of Y
-  const bool oz = sd.has_uplanes;
-  std::vector<MatRef> omats, ymats;
-  std::map<const double *, size_t> oidx;
-  struct P1 { size_t o; OzOperand u; int kp, k, nj; double *Y; };
-  std::vector<P1> p1oz;
-  std::map<OpKey, std::vector<std::pair<OzOperand, size_t>>> p2oz;  // (U_i rows, Y index)
-  for (auto &t : pend) {
-    const FBlock *F = std::get<0>(t);
-    const int ip = std::get<1>(t), ii = std::get<2>(t), iip = std::get<3>(t), bb = std::get<4>(t),
-              il = std::get<5>(t);
-    const int k = int(r->kept[ii]), kp = int(r->kept[iip]);
-    auto a = sub_of.at({ii, bb});
-    auto b = sub_of.at({iip, bb});
-    const DevBlock &bi = sd.blocks[sd.sectors[a.first].dev];
-    const DevBlock &bj = sd.blocks[sd.sectors[b.first].dev];
-    double *Y = static_cast<double *>(ymem->ptr) + yo;
-    yo += int64_t(k) * bj.n;
-    if (oz) {
-      auto ins = oidx.emplace(F->p, omats.size());
-      if (ins.second) omats.push_back(MatRef{F->p, k, kp, F->ld});
-      OzOperand uj = bj.uop, ui = bi.uop;
-      uj.p += int64_t(b.second + il * kp) * uj.ld;
-      ui.p += int64_t(a.second + il * k) * ui.ld;
-      p1oz.push_back(P1{ins.first->second, uj, kp, k, bj.n, Y});
-      p2oz[OpKey{ip, a.first, b.first}].push_back({ui, ymats.size()});
-      ymats.push_back(MatRef{Y, k, bj.n, bj.n});
-      continue;
+    pw.ymem = engine_alloc(e, ysz * sizeof(double) + 8);
+    int64_t yo = 0;
+    std::map<const double *, size_t> oidx;
+    for (auto &t : pend) {
+      const FBlock *F = std::get<0>(t);
+      const int ip = std::get<1>(t), ii = std::get<2>(t), iip = std::get<3>(t), bb = std::get<4>(t),
+                il = std::get<5>(t);
+      const int k = int(r->kept[ii]), kp = int(r->kept[iip]);
+      auto a = sub_of.at({ii, bb});
+      auto b = sub_of.at({iip, bb});
+      const DevBlock &bi = sd.blocks[sd.sectors[a.first].dev];
+      const DevBlock &bj = sd.blocks[sd.sectors[b.first].dev];
+      double *Y = static_cast<double *>(pw.ymem->ptr) + yo;
+      yo += int64_t(k) * bj.n;
+      if (oz) {
+        auto ins = oidx.emplace(F->p, omats.size());
+        if (ins.second) omats.push_back(MatRef{F->p, k, kp, F->ld});
+        OzOperand uj = bj.uop, ui = bi.uop;
+        uj.p += int64_t(b.second + il * kp) * uj.ld;
+        ui.p += int64_t(a.second + il * k) * ui.ld;
+        pw.p1oz.push_back(P1{ins.first->second, uj, kp, k, bj.n, Y});
+        pw.p2oz[OpKey{ip, a.first, b.first}].push_back({ui, ymats.size()});
+        ymats.push_back(MatRef{Y, k, bj.n, bj.n});
+        continue;
+      }
+      // pass 1: Y (k x n_j) = O[:k,:k'] U_j[rows (iip,bb,il), :]
+      p1.out(Y, bj.n, k, bj.n, false,
+             {gc(F->p, F->ld, bj.U + int64_t(b.second + il * kp) * bj.ld, bj.ld, kp, 0, 1.0)});
+      // pass 2: O_new(i,j) += U_i[rows (ii,bb,il), :]^T Y
+      pw.p2c[OpKey{ip, a.first, b.first}].push_back(
+          gc(bi.U + int64_t(a.second + il * k) * bi.ld, bi.ld, Y, bj.n, k, 1, 1.0));
     }
-    // pass 1: Y (k x n_j) = O[:k,:k'] U_j[rows (iip,bb,il), :]
-    p1.out(Y, bj.n, k, bj.n, false,
-           {gc(F->p, F->ld, bj.U + int64_t(b.second + il * kp) * bj.ld, bj.ld, kp, 0, 1.0)});
-    // pass 2: O_new(i,j) += U_i[rows (ii,bb,il), :]^T Y
-    p2c[OpKey{ip, a.first, b.first}].push_back(
-        gc(bi.U + int64_t(a.second + il * k) * bi.ld, bi.ld, Y, bj.n, k, 1, 1.0));
+    int64_t osz = 0;
+    for (auto &kv : outs) {
+      const DevBlock &bi = sd.blocks[sd.sectors[std::get<1>(kv.first)].dev];
+      const DevBlock &bj = sd.blocks[sd.sectors[std::get<2>(kv.first)].dev];
+      osz += int64_t(bi.n) * bj.n;
+    }
+    pw.omem = engine_alloc(e, osz * sizeof(double) + 8);
+    int64_t oo = 0;
+    for (auto &kv : outs) {
+      const DevBlock &bi = sd.blocks[sd.sectors[std::get<1>(kv.first)].dev];
+      const DevBlock &bj = sd.blocks[sd.sectors[std::get<2>(kv.first)].dev];
+      FBlock fb{static_cast<double *>(pw.omem->ptr) + oo, bi.n, bj.n, bj.n};
+      oo += int64_t(bi.n) * bj.n;
+      pw.nb_blocks[kv.first] = fb;
+      if (oz) continue;
+      auto it = pw.p2c.find(kv.first);
+      p2.out(fb.p, fb.ld, bi.n, bj.n, false, it == pw.p2c.end() ? std::vector<GemmContrib>{} : it->second);
+    }
   }
-  int64_t osz = 0;
-  for (auto &kv : outs) {
-    const DevBlock &bi = sd.blocks[sd.sectors[std::get<1>(kv.first)].dev];
-    const DevBlock &bj = sd.blocks[sd.sectors[std::get<2>(kv.first)].dev];
-    osz += int64_t(bi.n) * bj.n;
-  }
-  DevPtr omem = engine_alloc(e, osz * sizeof(double) + 8);
-  std::map<OpKey, FBlock> nb_blocks;
-  int64_t oo = 0;
-  for (auto &kv : outs) {
-    const DevBlock &bi = sd.blocks[sd.sectors[std::get<1>(kv.first)].dev];
-    const DevBlock &bj = sd.blocks[sd.sectors[std::get<2>(kv.first)].dev];
-    FBlock fb{static_cast<double *>(omem->ptr) + oo, bi.n, bj.n, bj.n};
-    oo += int64_t(bi.n) * bj.n;
-    nb_blocks[kv.first] = fb;
-    if (oz) continue;
-    auto it = p2c.find(kv.first);
-    p2.out(fb.p, fb.ld, bi.n, bj.n, false, it == p2c.end() ? std::vector<GemmContrib>{} : it->second);
-  }
-  if (oz) {
+  if (oz) {  // tensor-core variant (mixed path): digit planes of the O views and of Y
     std::vector<DevPtr> hold;
     PlaneBuf po = split_matrices(e, omats, hold);
     OzList l1;
-    for (auto &x : p1oz) l1.out(x.Y, x.nj, x.k, x.nj, false, {ozc(po.op(x.o), x.u, x.kp, 0)});
+    for (auto &pw : P)
+      for (auto &x : pw.p1oz) l1.out(x.Y, x.nj, x.k, x.nj, false, {ozc(po.op(x.o), x.u, x.kp, 0)});
     l1.launch(e, hold);
     PlaneBuf py = split_matrices(e, ymats, hold);
     OzList l2;
-    for (auto &kv : nb_blocks) {
-      std::vector<OzContrib> cs;
-      auto it = p2oz.find(kv.first);
-      if (it != p2oz.end())
-        for (auto &pr : it->second) cs.push_back(ozc(pr.first, py.op(pr.second), ymats[pr.second].rows, 1));
-      l2.out(kv.second.p, kv.second.ld, kv.second.rows, kv.second.cols, false, cs);
-    }
+    for (auto &pw : P)
+      for (auto &kv : pw.nb_blocks) {
+        std::vector<OzContrib> cs;
+        auto it = pw.p2oz.find(kv.first);
+        if (it != pw.p2oz.end())
+          for (auto &pr : it->second) cs.push_back(ozc(pr.first, py.op(pr.second), ymats[pr.second].rows, 1));
+        l2.out(kv.second.p, kv.second.ld, kv.second.rows, kv.second.cols, false, cs);
+      }
     l2.launch(e, hold);
   } else {
     p1.run(e);
     p2.run(e);
   }
-  o->blocks = std::move(nb_blocks);
-  o->mem = omem;
-  o->updated_this_site = true;
+  for (auto &pw : P) {
+    pw.o->blocks = std::move(pw.nb_blocks);
+    pw.o->mem = pw.omem;
+    pw.o->updated_this_site = true;
+  }
 }
+
+static void opset_update(nrg_opset *o) { opset_update_batch({o}); }
 
 // ------------------------------------------------------------- FDM (T = 0)
 // One backward-pass shell (fdmSpectrum::calcSpectrum, fdmSpectrum.hpp:55-63)
@@ -952,6 +965,19 @@ int nrg_opset_update(nrg_opset *o) {
   return guard([&] {
     if (!o) fail(NRG_E_ARG, "null opset");
     opset_update(o);
+  });
+}
+
+int nrg_opset_update_batch(nrg_opset *const *os, int n) {
+  return guard([&] {
+    if (n < 0 || (n > 0 && !os)) fail(NRG_E_ARG, "bad argument");
+    std::vector<nrg_opset *> v(os, os + n);
+    for (size_t a = 0; a < v.size(); ++a) {
+      if (!v[a]) fail(NRG_E_ARG, "null operator set");
+      for (size_t b = 0; b < a; ++b)
+        if (v[b] == v[a]) fail(NRG_E_ARG, "an operator set appears twice in one batch");
+    }
+    opset_update_batch(v);
   });
 }
 

@@ -1,6 +1,6 @@
-"""nrg_fdm_calc_batch: the backward passes of several runs in shared launches
-give the same spectral weights as one nrg_fdm_calc per run (to 1e-12
-relative: the binning adds with floating-point atomics)."""
+"""Batched calls across runs give the per-run results: nrg_opset_update_batch
+bit for bit (fixed-order GEMMs), nrg_fdm_calc_batch to 1e-12 relative (the
+binning adds with floating-point atomics)."""
 import math
 
 import numpy as np
@@ -15,7 +15,7 @@ NK, NS, LAM = 96, 14, 2.0
 PARAMS = [(-0.4, 0.8, 0.15), (-0.3, 0.6, 0.12), (-0.5, 1.0, 0.2)]
 
 
-def _forward(engine):
+def _forward(engine, batched_ops=False):
     runs, datas, ops, min_it = [], [], [], []
     for eps, U, V in PARAMS:
         imp, bath = workloads.build_models("siam", eps, U)
@@ -30,8 +30,12 @@ def _forward(engine):
     for it in range(NS):
         h = M.hopping(it, LAM)
         api.batch_add_site(runs, [[h, h]] * len(runs), [math.sqrt(LAM) if it > 0 else 1.0] * len(runs))
+        if batched_ops:
+            api.update_system_operator_batch(runs, ops)
+        else:
+            for k, r in enumerate(runs):
+                api.update_system_operator(r, ops[k])
         for k, r in enumerate(runs):
-            api.update_system_operator(r, ops[k])
             if r.checkHigherEnergyDiscarded():
                 datas[k].saveCurrentData(ops[k])
             else:
@@ -83,3 +87,25 @@ def test_batched_fdm_rejects_two_objects_of_one_run(mixed_engine):
     f1.close()
     f2.close()
     run.close()
+
+
+def test_batched_operator_update_equals_per_run(mixed_engine):
+    res = []
+    for batched in (False, True):
+        runs, datas, ops, _ = _forward(mixed_engine, batched_ops=batched)
+        nsec = len(runs[0].eigenvaluesQ)
+        blocks = {}
+        for k, o in enumerate(ops):
+            for ip in range(2):
+                for i in range(nsec):
+                    for j in range(nsec):
+                        b = o.block(ip, i, j)
+                        if b is not None:
+                            blocks[(k, ip, i, j)] = b
+        res.append(blocks)
+        for o, r in zip(ops, runs):
+            o.close()
+            r.close()
+    assert res[0].keys() == res[1].keys() and len(res[0]) > 0
+    for key in res[0]:
+        assert np.array_equal(res[0][key], res[1][key]), key

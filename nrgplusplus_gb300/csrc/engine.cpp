@@ -66,8 +66,7 @@ struct Arena {
   char *push(nrg_engine *e, DevPtr &hold) {
     hold = dalloc(e, buf.size());
     if (!buf.empty())
-      check_cuda(cudaMemcpyAsync(hold->ptr, buf.data(), buf.size(), cudaMemcpyHostToDevice, e->stream),
-                 "descriptor upload");
+      upload_async(e, hold->ptr, buf.data(), buf.size());
     return static_cast<char *>(hold->ptr);
   }
 };
@@ -75,6 +74,53 @@ struct Arena {
 template <class T> static T *at(char *base, size_t off) { return reinterpret_cast<T *>(base + off); }
 
 static void count_launch(nrg_engine *e, int n = 1) { e->launches += n; }
+
+void upload_async(nrg_engine *e, void *dst, const void *src, size_t bytes) {
+  if (bytes == 0) return;
+  const size_t need = (bytes + 255) & ~size_t(255);
+  if (need > e->ring_cap) {  // (re)allocate: wait for every pending copy first
+    check_cuda(cudaStreamSynchronize(e->stream), "upload ring");
+    release_uploads(e);
+    const size_t cap = std::max<size_t>(size_t(64) << 20, 2 * need);
+    check_cuda(cudaHostAlloc(reinterpret_cast<void **>(&e->ring), cap, cudaHostAllocDefault), "cudaHostAlloc");
+    e->ring_cap = cap;
+    e->ring_head = 0;
+  }
+  if (e->ring_head + need > e->ring_cap) {
+    // wrap: the stream runs in order, so once the newest copy is done every
+    // region of the ring is free again
+    if (!e->ring_busy.empty()) check_cuda(cudaEventSynchronize(e->ring_busy.back().ev), "upload ring wait");
+    for (auto &sp : e->ring_busy) e->ring_events.push_back(sp.ev);
+    e->ring_busy.clear();
+    e->ring_head = 0;
+  }
+  const size_t a = e->ring_head, b = a + need;
+  // within one lap no region is handed out twice; recycle finished events
+  while (!e->ring_busy.empty() && cudaEventQuery(e->ring_busy.front().ev) == cudaSuccess) {
+    e->ring_events.push_back(e->ring_busy.front().ev);
+    e->ring_busy.pop_front();
+  }
+  std::memcpy(e->ring + a, src, bytes);
+  check_cuda(cudaMemcpyAsync(dst, e->ring + a, bytes, cudaMemcpyHostToDevice, e->stream), "upload");
+  cudaEvent_t ev;
+  if (e->ring_events.empty()) {
+    check_cuda(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "event");
+  } else {
+    ev = e->ring_events.back();
+    e->ring_events.pop_back();
+  }
+  check_cuda(cudaEventRecord(ev, e->stream), "event");
+  e->ring_busy.push_back({a, b, ev});
+  e->ring_head = b;
+}
+
+void release_uploads(nrg_engine *e) {
+  for (auto &sp : e->ring_busy) e->ring_events.push_back(sp.ev);
+  e->ring_busy.clear();
+  if (e->ring) cudaFreeHost(e->ring);
+  e->ring = nullptr;
+  e->ring_cap = e->ring_head = 0;
+}
 
 void check_kernel_error(nrg_engine *e) {
   int h = 0;
@@ -620,8 +666,7 @@ static MixedStatus mixed_eigensolve(nrg_engine *e, std::vector<DevBlock *> &blks
     }
     g1.launch(e, hold);
     g2.launch(e, hold);
-    check_cuda(cudaMemcpyAsync(dp + orb, rb.data(), nb * sizeof(RefineBlock), cudaMemcpyHostToDevice, s),
-               "refine descriptors");
+    upload_async(e, dp + orb, rb.data(), nb * sizeof(RefineBlock));
     if (final) {
       Prof pf(e, "k_oa_final");
       launch_oa_final(at<RefineBlock>(dp, orb), int(nb), max_n, kClusterTau, at<int>(dp, ost), s);

@@ -50,8 +50,7 @@ struct Staged {  // descriptor tables of one launch phase
   }
   char *push(nrg_engine *e, DevPtr &hold) {
     hold = engine_alloc(e, buf.size());
-    check_cuda(cudaMemcpyAsync(hold->ptr, buf.data(), buf.size(), cudaMemcpyHostToDevice, e->stream),
-               "descriptor upload");
+    upload_async(e, hold->ptr, buf.data(), buf.size());
     return static_cast<char *>(hold->ptr);
   }
 };
@@ -595,6 +594,8 @@ int nrg_engine_destroy(nrg_engine *e) {
   return guard([&] {
     if (!e) return;
     cudaStreamSynchronize(e->stream);
+    release_uploads(e);
+    for (auto ev : e->ring_events) cudaEventDestroy(ev);
     if (e->d_kerr) cudaFree(e->d_kerr);
     for (auto &ev : e->ev) cudaEventDestroy(ev);
     cudaStreamDestroy(e->stream);

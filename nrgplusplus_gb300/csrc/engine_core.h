@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <deque>
 #include <map>
 #include <memory>
 #include <string>
@@ -140,6 +141,17 @@ struct nrg_engine {
   uint64_t launches = 0;
   int eig_smem_f64 = 0, eig_smem_f32 = 0;
   int *d_kerr = nullptr;  // set by kernels whose bounded waits ran out (k_gemm_oz)
+  // pinned ring for host -> device uploads (descriptor tables): a copy from
+  // pageable memory may wait for the stream to drain, one from pinned memory
+  // does not, so the host can build the next phase while the GPU runs
+  struct PinnedSpan {
+    size_t a, b;
+    cudaEvent_t ev;
+  };
+  char *ring = nullptr;
+  size_t ring_cap = 0, ring_head = 0;
+  std::deque<PinnedSpan> ring_busy;
+  std::vector<cudaEvent_t> ring_events;
   uint64_t fallback_blocks = 0;  // mixed path: blocks re-solved in FP64
   // mixed path: FP64-accurate GEMMs on the tensor cores, bit 0 for the
   // eigenvector refinement, bit 1 for the operator rotations
@@ -159,6 +171,11 @@ namespace nrg {
 // Fails with NRG_E_CUDA (and clears the word) when a kernel has reported a
 // timed-out wait; call after a stream synchronisation.
 void check_kernel_error(nrg_engine *e);
+// Stream-ordered host -> device copy of `bytes` through the engine's pinned
+// ring: returns at once; the host buffer may be reused immediately.
+void upload_async(nrg_engine *e, void *dst, const void *src, size_t bytes);
+// Releases the pinned ring (engine destruction, after a stream sync).
+void release_uploads(nrg_engine *e);
 // Records CUDA events around one kernel launch on the engine stream when
 // profiling is on; `work` is the launch's algorithmic flop count (byte count
 // for the memory-bound kernels k_split and k_oa_update).

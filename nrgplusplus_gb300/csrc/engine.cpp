@@ -12,6 +12,7 @@
 // Empty sectors (no kept states) stay in the API-level sector lists exactly as
 // the reference keeps them, but never reach the device.
 #include <algorithm>
+#include <unordered_map>
 #include <cmath>
 #include <cstring>
 #include <numeric>
@@ -287,21 +288,50 @@ static void build_basis(RunStep &st) {
   sd->pre_q = r->pre_q;
   sd->kept_prev = r->kept;
   const int nb = int(bath.q.size());
+  // new sectors in first-seen order over (previous sector, bath sector), as
+  // create_next_basis (nrgcore.hpp:238-261); the basis is never pruned, so
+  // this loop runs over every pair: sector keys are packed into 64 bits
+  // (up to 4 quantum numbers of 16 bits) for a hash lookup
+  const size_t nq = r->pre_q.empty() ? 0 : r->pre_q[0].size();
+  for (int j = 0; j < nb; ++j)
+    if (bath.q[j].size() != nq) fail(NRG_E_ARG, "quantum number count differs between impurity and bath");
+  bool packable = nq <= 4;
+  for (auto &q : r->pre_q)
+    for (int v : q) packable = packable && v > -16384 && v < 16384;
+  for (auto &q : bath.q)
+    for (int v : q) packable = packable && v > -16384 && v < 16384;
+  std::unordered_map<uint64_t, int> where_packed;
   std::map<std::vector<int>, int> where;
-  for (size_t i = 0; i < r->pre_q.size(); ++i)
+  if (packable) where_packed.reserve(r->pre_q.size() * 2 + 16);
+  int tmq[4];
+  std::vector<int> tm(nq);
+  for (size_t i = 0; i < r->pre_q.size(); ++i) {
+    const std::vector<int> &pq = r->pre_q[i];
+    if (pq.size() != nq) fail(NRG_E_ARG, "quantum number count differs between sectors");
     for (int j = 0; j < nb; ++j) {
-      std::vector<int> tm = r->pre_q[i];
-      if (tm.size() != bath.q[j].size()) fail(NRG_E_ARG, "quantum number count differs between impurity and bath");
-      for (size_t x = 0; x < tm.size(); ++x) tm[x] += bath.q[j][x];
-      auto it = where.find(tm);
-      if (it != where.end()) {
-        sd->coupled[it->second].push_back(uint64_t(i) * nb + j);
+      int idx;
+      bool fresh;
+      if (packable) {
+        uint64_t key = 0;
+        for (size_t x = 0; x < nq; ++x) {
+          tmq[x] = pq[x] + bath.q[j][x];
+          key = (key << 16) | uint64_t(uint16_t(tmq[x] + 32768));
+        }
+        auto ins = where_packed.emplace(key, int(sd->cur_q.size()));
+        idx = ins.first->second;
+        fresh = ins.second;
+        if (fresh) sd->cur_q.emplace_back(tmq, tmq + nq);
       } else {
-        where[tm] = int(sd->cur_q.size());
-        sd->cur_q.push_back(tm);
-        sd->coupled.push_back({uint64_t(i) * nb + j});
+        for (size_t x = 0; x < nq; ++x) tm[x] = pq[x] + bath.q[j][x];
+        auto ins = where.emplace(tm, int(sd->cur_q.size()));
+        idx = ins.first->second;
+        fresh = ins.second;
+        if (fresh) sd->cur_q.push_back(tm);
       }
+      if (fresh) sd->coupled.emplace_back();
+      sd->coupled[idx].push_back(uint64_t(i) * nb + j);
     }
+  }
   sd->sectors.resize(sd->cur_q.size());
   for (size_t s = 0; s < sd->cur_q.size(); ++s) {
     int off = 0;

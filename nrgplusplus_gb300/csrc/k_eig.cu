@@ -475,14 +475,18 @@ k_eig(const EigBlock *__restrict__ blocks, int max_n_smem, int *status, const in
 //   * Sturm-sequence bisection, one thread per eigenvalue (all in parallel);
 //   * inverse iteration, one thread per eigenvector (tridiagonal LU solve,
 //     vectors stored column-wise so every step is a coalesced row access);
-//   * near-degenerate clusters (gaps <= 1e-3 |T|) redone one warp per
+//   * near-degenerate clusters (gaps <= 1e-5 |T|) redone one warp per
 //     cluster, re-orthogonalising each new iterate against the cluster's
-//     earlier vectors (the classic inverse-iteration/Gram-Schmidt scheme);
+//     earlier vectors (the classic inverse-iteration/Gram-Schmidt scheme).
+//     Pairs further apart leave inverse iteration with an overlap of about
+//     eps32 |T| / gap <= 1e-2, which the FP64 refinement's orthonormalisation
+//     (pairs closer than 1e-4 |H|) or Newton step (the others) removes; a
+//     wider cluster gap only made the sequential cluster solves longer;
 //   * the back-transform X = Q V applies the reflectors to V in a separate
 //     multi-CTA kernel (k_reflect).
 // Accuracy is FP32 (~1e-6); the FP64-accurate refinement follows.
 
-constexpr float kClusterGap = 1e-3f;
+constexpr float kClusterGap = 1e-5f;
 constexpr int kInvIter = 3;
 
 __device__ __forceinline__ float block_minf(float v, float *red) {

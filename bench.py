@@ -236,7 +236,6 @@ def reference_arm(args):
 # nominal per-GPU peaks for the pipes MEASURED_PEAKS.json does not cover
 FP64_PEAK_TFLOPS = 1.25   # GB300 FP64 (vector and tensor) dense
 FP32_PEAK_TFLOPS = 80.5   # 152 SMs x 128 FP32 lanes x 2 flops x 2.07 GHz
-OZ_PAIRS = 36             # bf16 digit-plane products per FP64 product (p + q <= 7 of 8 x 8)
 
 
 def _measured(key, fallback):
@@ -261,8 +260,9 @@ def kernel_models():
                          "(4/3) n^3 per block (Householder reduction)"),
         "k_reflect": ("fp32", FP32_PEAK_TFLOPS, "TFLOP/s", 1e-12, "nominal GB300 FP32",
                       "2 n^3 per block (Householder reflectors applied to the tridiagonal eigenvectors)"),
-        "k_gemm_oz": ("tensor", bf16, "TFLOP/s", OZ_PAIRS * 1e-12, bf16_src,
-                      "36 bf16 digit-plane products x 2MNK per FP64-accurate GEMM contribution"),
+        "k_gemm_oz": ("tensor", bf16, "TFLOP/s", 1e-12, bf16_src,
+                      "bf16 tensor flops: 2MNK per digit-plane product (36 products per FP64-accurate "
+                      "product with 8 planes, 15 with the 5 planes of the first refinement step)"),
         "k_split": ("hbm", hbm, "GB/s", 1e-9, hbm_src,
                     "bytes: 8 (max pass) + 8 (digit pass) read + 16 written per element"),
         "k_oa_update": ("hbm", hbm, "GB/s", 1e-9, hbm_src, "bytes: S, G read + E written, 24 per element"),

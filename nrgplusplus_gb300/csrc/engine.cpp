@@ -507,23 +507,28 @@ static PlaneBuf split_blocks(nrg_engine *e, const double *base, const std::vecto
   return split_matrices(e, m, hold);
 }
 
-void OzList::out(double *C, int ldc, int M, int N, bool acc, const std::vector<OzContrib> &cs) {
+void OzList::out(double *C, int ldc, int M, int N, bool acc, const std::vector<OzContrib> &cs, bool upper) {
   OzGroup g{};
   g.C = C;
   g.ldc = ldc;
   g.M = M;
   g.N = N;
   g.accumulate = acc ? 1 : 0;
+  g.planes = planes;
   g.c0 = int(contribs.size());
+  const double pairs = 0.5 * planes * (planes + 1);
   for (auto &c : cs) {
     contribs.push_back(c);
-    flops += 2.0 * M * N * double(c.K);
+    flops += 2.0 * M * N * double(c.K) * pairs;
   }
   g.c1 = int(contribs.size());
   const int gi = int(groups.size());
   groups.push_back(g);
   for (int tm = 0; tm < (M + OZ_TILE_M - 1) / OZ_TILE_M; ++tm)
-    for (int tn = 0; tn < (N + OZ_TILE_N - 1) / OZ_TILE_N; ++tn) tiles.push_back({gi, tm, tn, 0});
+    for (int tn = 0; tn < (N + OZ_TILE_N - 1) / OZ_TILE_N; ++tn) {
+      if (upper && tm * OZ_TILE_M > tn * OZ_TILE_N + OZ_TILE_N - 1) continue;  // wholly below the diagonal
+      tiles.push_back({gi, tm, tn, 0});
+    }
 }
 
 void OzList::launch(nrg_engine *e, std::vector<DevPtr> &hold) {
@@ -552,6 +557,10 @@ OzContrib ozc(const OzOperand &A, const OzOperand &B, int K, int trans, double a
 
 constexpr int kRefineSteps = 3;
 constexpr double kClusterTau = 1e-4;  // relative gap below which levels form a cluster
+// The first Newton step starts from FP32 eigenvectors (errors >= 1e-7), so
+// its products need only 5 digit planes (35 bits, relative error ~3e-11,
+// 15 instead of 36 digit-plane products); the later steps use all 8.
+constexpr int kFirstStepPlanes = 5;
 
 // Mixed-precision eigensolve of every block of the batch: FP32 Householder +
 // QL (k_eig<float>), then kRefineSteps Ogita-Aishima Newton steps with
@@ -661,6 +670,7 @@ static MixedStatus mixed_eigensolve(nrg_engine *e, std::vector<DevBlock *> &blks
     if (oz) {
       splitv(pX, X[cur]);
       OzList y;
+      y.planes = step == 0 ? kFirstStepPlanes : kDigitPlanes;
       for (size_t b = 0; b < nb; ++b) {  // Y = H X
         const int n = blks[b]->n;
         y.out(P(my, off[b]), lds[b], n, n, false, {ozc(pH.op(b), pX.op(b), n, 0)});
@@ -668,10 +678,13 @@ static MixedStatus mixed_eigensolve(nrg_engine *e, std::vector<DevBlock *> &blks
       y.launch(e, hold);
       splitv(pY, P(my, 0));
       OzList sg;
+      sg.planes = y.planes;
       for (size_t b = 0; b < nb; ++b) {  // S = X^T Y, G = X^T X
         const int n = blks[b]->n;
-        sg.out(P(ms, off[b]), lds[b], n, n, false, {ozc(pX.op(b), pY.op(b), n, 1)});
-        sg.out(P(mg, off[b]), lds[b], n, n, false, {ozc(pX.op(b), pX.op(b), n, 1)});
+        // symmetric: only the tiles that meet the upper triangle (the refinement
+        // kernels read S and G there)
+        sg.out(P(ms, off[b]), lds[b], n, n, false, {ozc(pX.op(b), pY.op(b), n, 1)}, true);
+        sg.out(P(mg, off[b]), lds[b], n, n, false, {ozc(pX.op(b), pX.op(b), n, 1)}, true);
       }
       sg.launch(e, hold);
     }
@@ -717,6 +730,7 @@ static MixedStatus mixed_eigensolve(nrg_engine *e, std::vector<DevBlock *> &blks
     if (oz) {
       splitv(pE, P(me2, 0));
       OzList g3;
+      g3.planes = step == 0 ? kFirstStepPlanes : kDigitPlanes;
       for (size_t b = 0; b < nb; ++b) {
         const int n = blks[b]->n;
         g3.out(X[1 - cur] + off[b], lds[b], n, n, true, {ozc(pX.op(b), pE.op(b), n, 0)});

@@ -113,8 +113,11 @@ struct OzList {
   std::vector<OzGroup> groups;
   std::vector<OzContrib> contribs;
   std::vector<GemmTile> tiles;
-  double flops = 0;
-  void out(double *C, int ldc, int M, int N, bool acc, const std::vector<OzContrib> &cs);
+  double flops = 0;  // bf16 tensor flops: 2MNK per digit-plane product
+  int planes = kDigitPlanes;  // digit planes of the products (fewer: a cheaper, less exact product)
+  // upper: only the tiles that meet the upper triangle (symmetric outputs whose
+  // readers use the upper triangle)
+  void out(double *C, int ldc, int M, int N, bool acc, const std::vector<OzContrib> &cs, bool upper = false);
   void launch(nrg_engine *e, std::vector<DevPtr> &hold);
 };
 OzContrib ozc(const OzOperand &A, const OzOperand &B, int K, int trans, double alpha = 1.0);

@@ -193,10 +193,10 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
 // op(B) (64 x 16): 3072 rows of 16 bytes, 24 per producer thread (tp =
 // 0..127): per plane two A rows and one B row.
 __device__ __forceinline__ void stage_step(const OzContrib &q, int M, int N, int m0, int n0, int k0, int kend,
-                                           unsigned char *st, int tp) {
+                                           unsigned char *st, int tp, int P) {
   const bool ta = q.trans & 1, tb = (q.trans >> 1) & 1;
 #pragma unroll 2
-  for (int p = 0; p < kPlanes; ++p) {
+  for (int p = 0; p < P; ++p) {
     unsigned char *As = st + p * kATile;
     unsigned char *Bs = st + kPlanes * kATile + p * kBTile;
     const __nv_bfloat16 *a = q.A.p + int64_t(p) * q.A.pstride;
@@ -275,6 +275,7 @@ k_gemm_oz(const GemmTile *__restrict__ tiles, const OzGroup *__restrict__ groups
   const OzGroup g = groups[t.group];
   const int m0 = t.tm * TM, n0 = t.tn * TN;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int P = (g.planes >= 1 && g.planes <= kPlanes) ? g.planes : kPlanes;
 
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
@@ -309,7 +310,7 @@ k_gemm_oz(const GemmTile *__restrict__ tiles, const OzGroup *__restrict__ groups
       if (use > 0 && !mbar_wait(smem_u32(&empty[st]), uint32_t((use - 1) & 1))) abort_flag = 1;
       if (abort_flag) break;
       const OzContrib &q = contribs[it.c];
-      stage_step(q, g.M, g.N, m0, n0, it.k0, q.K, ring + st * kStageBytes, tp);
+      stage_step(q, g.M, g.N, m0, n0, it.k0, q.K, ring + st * kStageBytes, tp, P);
       cp_async_commit();
       it.next(g, contribs);
       if (s >= kLag) {  // the copies of step s - kLag have landed: hand it over
@@ -350,11 +351,17 @@ k_gemm_oz(const GemmTile *__restrict__ tiles, const OzGroup *__restrict__ groups
         for (int cc = 0; cc < TN; cc += 8) {
           uint32_t v[kPlanes][8];
 #pragma unroll
-          for (int d = 0; d < kPlanes; ++d)
-            asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-                         : "=r"(v[d][0]), "=r"(v[d][1]), "=r"(v[d][2]), "=r"(v[d][3]), "=r"(v[d][4]),
-                           "=r"(v[d][5]), "=r"(v[d][6]), "=r"(v[d][7])
-                         : "r"(tl + uint32_t(64 * d + cc)));
+          for (int d = 0; d < kPlanes; ++d) {
+            if (d < P) {
+              asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                           : "=r"(v[d][0]), "=r"(v[d][1]), "=r"(v[d][2]), "=r"(v[d][3]), "=r"(v[d][4]),
+                             "=r"(v[d][5]), "=r"(v[d][6]), "=r"(v[d][7])
+                           : "r"(tl + uint32_t(64 * d + cc)));
+            } else {  // groups beyond the planes used are not computed
+#pragma unroll
+              for (int j = 0; j < 8; ++j) v[d][j] = 0u;
+            }
+          }
           asm volatile("tcgen05.wait::ld.sync.aligned;");
           if (gm < g.M) {
 #pragma unroll
@@ -402,6 +409,7 @@ k_gemm_oz(const GemmTile *__restrict__ tiles, const OzGroup *__restrict__ groups
           for (int p = 0; p < kPlanes; ++p) {
 #pragma unroll
             for (int qd = 0; qd < kPlanes - p; ++qd) {
+              if (p + qd >= P) continue;  // uniform: fewer planes, fewer products
               const uint64_t ad = ds + uint64_t((p * kATile) >> 4);
               const uint64_t bd = ds + uint64_t((kPlanes * kATile + qd * kBTile) >> 4);
               const uint32_t acc = p > 0 ? 1u : first;  // the first pair of each group starts it

@@ -31,6 +31,12 @@ constexpr int kMaxJacobiSweeps = 30;
 // whose FP32 start was too poor for the fixed step count stays far above.
 constexpr double kConvTol = 1e-10;
 
+// S and G are symmetric; their lower triangle may not be written (the
+// tensor-core path computes only the tiles that meet the upper triangle)
+__device__ __forceinline__ double sym(const double *M, int ld, int i, int j) {
+  return i <= j ? M[int64_t(i) * ld + j] : M[int64_t(j) * ld + i];
+}
+
 __device__ double block_max(double v, double *red) {
   for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
   __syncthreads();
@@ -58,13 +64,13 @@ k_oa_update(const RefineBlock *__restrict__ blocks, double tau_rel) {
   const double tau = tau_rel * fmax(1.0, block_max(local, red));
   for (int64_t idx = threadIdx.x; idx < int64_t(n) * n; idx += kThreads) {
     const int i = int(idx / n), j = int(idx - int64_t(i) * n);
-    const double g = B.G[int64_t(i) * B.ld + j];
+    const double g = sym(B.G, B.ld, i, j);
     double e;
     if (i == j) {
       e = 0.5 * (1.0 - g);
     } else {
       const double d = lam[j] - lam[i];
-      e = (fabs(d) > tau) ? (B.S[int64_t(i) * B.ld + j] - lam[j] * g) / d : -0.5 * g;
+      e = (fabs(d) > tau) ? (sym(B.S, B.ld, i, j) - lam[j] * g) / d : -0.5 * g;
     }
     B.E2[int64_t(i) * B.ld + j] = e;
   }
@@ -103,13 +109,13 @@ k_oa_final(const RefineBlock *__restrict__ blocks, double tau_rel, int *status) 
   // part) must be below kConvTol, otherwise the block is re-solved in FP64
   for (int64_t idx = threadIdx.x; idx < int64_t(n) * n && bad == 0.0; idx += kThreads) {
     const int i = int(idx / n), j = int(idx - int64_t(i) * n);
-    const double g = B.G[int64_t(i) * B.ld + j];
+    const double g = sym(B.G, B.ld, i, j);
     double r;
     if (i == j) {
       r = 1.0 - g;
     } else {
       const double d = lam[j] - lam[i];
-      r = (fabs(d) > tau) ? (B.S[int64_t(i) * B.ld + j] - lam[j] * g) / d : g;
+      r = (fabs(d) > tau) ? (sym(B.S, B.ld, i, j) - lam[j] * g) / d : g;
     }
     if (!(fabs(r) <= kConvTol)) bad = 1.0;
   }
@@ -158,7 +164,7 @@ k_oa_final(const RefineBlock *__restrict__ blocks, double tau_rel, int *status) 
     }
     for (int idx = threadIdx.x; idx < c * c; idx += kThreads) {
       const int p = idx / c, s = idx - p * c;
-      Sc[idx] = B.S[int64_t(perm[a + p]) * B.ld + perm[a + s]];
+      Sc[idx] = sym(B.S, B.ld, perm[a + p], perm[a + s]);
       Qc[idx] = (p == s) ? 1.0 : 0.0;
     }
     __syncthreads();

@@ -141,6 +141,7 @@ struct OzGroup {
   double *C;
   int ldc, M, N, accumulate;
   int c0, c1;
+  int planes, pad;  // digit planes used (1..8): groups d < planes, pairs p + q < planes
 };
 void launch_split(const SplitTask *tasks, int ntasks, cudaStream_t s);
 // Grid-wide split: chunk0_max / chunk0_dig are per-task prefix counts of

@@ -82,6 +82,34 @@ def _dist():
     return ws, rank
 
 
+def max_over_ranks(values):
+    """Element-wise maximum of a list of floats over the ranks of the
+    initialised process group (the values unchanged without one)."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return [float(v) for v in values]
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return t.tolist()
+
+
+def _site_bytes(site):
+    """Host bytes of one site description as the C ABI receives it."""
+    n = 0
+    n += 4 * sum(len(q) for q in site.qnums) + 4 * len(site.energies)
+    n += 8 * sum(len(e) for e in site.energies) + 8 * len(site.chi)
+    for op in site.fdag:
+        for m in op.values():
+            n += 12 + 8 * m.size
+    return n
+
+
+def _ops_bytes(ops):
+    return sum(20 + 8 * m.size for op in ops for m in op.values())
+
+
 class ClockSampler:
     """nvidia-smi clock/throttle sampling during the timed region."""
 
@@ -133,7 +161,9 @@ def one_run(engine, e2e, batch=None):
     """One step: `batch` complete spectral runs stepped together (one launch
     per phase for all their blocks), then each run's backward passes.  With
     e2e the caller-visible results are copied to host buffers as a user of
-    the API would read them.  Returns the device-to-host bytes of the step."""
+    the API would read them.  Returns the host-to-device bytes of the inputs
+    (models, tracked operators, hoppings, temperatures) and the device-to-host
+    bytes of the results of the step."""
     import numpy as np
     from nrgplusplus_gb300 import api, workloads
     from nrgplusplus_gb300 import models as M
@@ -187,7 +217,10 @@ def one_run(engine, e2e, batch=None):
         ths[k].close()
         ops[k].close()
         run.close()
-    return d2h
+    imp, bath = M.spinhalf(w["eps"], w["U"]), M.spinhalf(0.0, 0.0)
+    h2d = B * (_site_bytes(imp) + _site_bytes(bath) + _ops_bytes(M.d_dag_chi())
+               + 8 * (w["nsites"] + 1) * 3 + 8 * len(workloads.temperature_grid()))
+    return h2d, d2h
 
 
 def time_oracle_run(max_sites):
@@ -358,16 +391,11 @@ def main():
             flush.zero_()
             barrier()
             t0 = time.perf_counter()
-            d2h = one_run(engine, e2e=True)
+            h2d, d2h = one_run(engine, e2e=True)
             engine.sync()
             barrier()
             e2e_times.append(time.perf_counter() - t0)
-    if ws > 1:
-        tt = torch.tensor([sum(times), sum(e2e_times)], device="cuda")
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        tsum, esum = tt[0].item(), tt[1].item()
-    else:
-        tsum, esum = sum(times), sum(e2e_times)
+    tsum, esum = max_over_ranks([sum(times), sum(e2e_times)])
     per = tsum / args.steps
     value = ws * BATCH / per
     e2e_v = ws * BATCH / (esum / args.steps)
@@ -408,7 +436,7 @@ def main():
                 "gpu_launches": launches,
                 "fp64_fallback_blocks": fallbacks,
                 "hbm_peak_bytes": hbm_peak,
-                "e2e": {"value": e2e_v, "unit": "runs/s", "h2d_bytes_per_step": 4096,
+                "e2e": {"value": e2e_v, "unit": "runs/s", "h2d_bytes_per_step": int(h2d),
                         "d2h_bytes_per_step": int(d2h)},
                 "serving": serving, "plain_fp64": plain, "roofline": rf,
                 "kernels_ms_per_step": {k: round(v[0], 3) for k, v in kt.items()},

@@ -302,6 +302,11 @@ def kernel_models():
     }
 
 
+# DRAM bytes (read + write) per launch measured with ncu on the full bench
+# step (mean over 1500 launches; summary and command under profiles/)
+MEASURED_TRAFFIC = {"k_gemm_oz": 449.2e6}
+
+
 def kernel_profile(engine):
     """One extra run with per-kernel CUDA events on the engine stream."""
     engine.set_profiling(True)
@@ -316,7 +321,9 @@ def _roofline(name, ms, work, n, models):
     bound, peak, unit, mult, src, per = models[name]
     achieved = work * mult / (ms * 1e-3) if ms > 0 else 0.0
     return {"bound": bound, "kernel": name, "achieved": achieved, "peak": peak, "unit": unit,
-            "frac": achieved / peak if peak else None, "traffic": None, "peak_source": src,
+            "frac": achieved / peak if peak else None, "traffic": MEASURED_TRAFFIC.get(name),
+            "traffic_unit": "bytes per launch (ncu dram__bytes_read.sum + dram__bytes_write.sum)",
+            "peak_source": src,
             "launches": n, "ms_total": ms, "per_launch": per}
 
 

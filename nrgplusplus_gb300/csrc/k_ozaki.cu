@@ -347,8 +347,10 @@ k_gemm_oz(const GemmTile *__restrict__ tiles, const OzGroup *__restrict__ groups
       }
       drain_phase ^= 1u;
       asm volatile("tcgen05.fence::after_thread_sync;");
-      if (__shfl_sync(0xffffffffu, abort_flag, 0) == 0) {
-        for (int cc = 0; cc < TN; cc += 8) {
+      // a warp whose 32 rows lie past M, and column chunks past N, have
+      // nothing to fold (warp-uniform conditions: tcgen05.ld is collective)
+      if (__shfl_sync(0xffffffffu, abort_flag, 0) == 0 && m0 + 32 * warp < g.M) {
+        for (int cc = 0; cc < TN && n0 + cc < g.N; cc += 8) {
           uint32_t v[kPlanes][8];
 #pragma unroll
           for (int d = 0; d < kPlanes; ++d) {

@@ -444,15 +444,17 @@ static GemmContrib contrib(const double *A, int lda, const double *B, int ldb, i
 PlaneBuf split_matrices(nrg_engine *e, const std::vector<MatRef> &mats, std::vector<DevPtr> &hold) {
   PlaneBuf pb;
   const size_t nm = mats.size();
-  std::vector<int64_t> poff(nm), cmax(nm + 1, 0), cdig(nm + 1, 0);
+  std::vector<int64_t> poff(nm), chunk0(nm + 1, 0);
   std::vector<int> ldp(nm);
   int64_t tot = 0;
+  const int64_t chunk = split_chunk_elements();
   for (size_t i = 0; i < nm; ++i) {
     ldp[i] = round_up(std::max(mats[i].cols, 1), 8);
     poff[i] = tot;
-    tot += int64_t(mats[i].rows) * ldp[i];
-    cmax[i + 1] = cmax[i] + (int64_t(mats[i].rows) * mats[i].cols + 1023) / 1024;
-    cdig[i + 1] = cdig[i] + (int64_t(mats[i].rows) * ldp[i] + 1023) / 1024;
+    const int64_t nel = int64_t(mats[i].rows) * ldp[i];
+    if (nel >= (int64_t(1) << 31)) fail(NRG_E_ARG, "matrix too large for the digit split");
+    tot += nel;
+    chunk0[i + 1] = chunk0[i] + (nel + chunk - 1) / chunk;
   }
   pb.mem = dalloc(e, tot * kDigitPlanes * 2 + 16);
   pb.exps = dalloc(e, nm * sizeof(int) + 16);
@@ -478,12 +480,11 @@ PlaneBuf split_matrices(nrg_engine *e, const std::vector<MatRef> &mats, std::vec
     pb.ops[i] = o;
   }
   if (nm == 0) return pb;
-  const int64_t nchunk_max = cmax[nm], nchunk_dig = cdig[nm];
-  cmax.pop_back();
-  cdig.pop_back();
+  const int64_t nchunks = chunk0[nm];
+  chunk0.pop_back();
   std::vector<unsigned long long> scratch(nm, 0);
   Arena a;
-  size_t ot = a.add(t), om = a.add(cmax), od = a.add(cdig), os = a.add(scratch);
+  size_t ot = a.add(t), oc = a.add(chunk0), os = a.add(scratch);
   DevPtr d;
   char *dp = a.push(e, d);
   hold.push_back(d);
@@ -491,8 +492,8 @@ PlaneBuf split_matrices(nrg_engine *e, const std::vector<MatRef> &mats, std::vec
   for (size_t i = 0; i < nm; ++i)
     bytes += 16.0 * mats[i].rows * mats[i].cols + 16.0 * mats[i].rows * ldp[i];
   Prof pf(e, "k_split", bytes);
-  launch_split_grid(at<SplitTask>(dp, ot), at<int64_t>(dp, om), at<int64_t>(dp, od), int(nm), nchunk_max,
-                    nchunk_dig, at<unsigned long long>(dp, os), e->stream);
+  launch_split_grid(at<SplitTask>(dp, ot), at<int64_t>(dp, oc), int(nm), nchunks, at<unsigned long long>(dp, os),
+                    e->stream);
   count_launch(e, 2);
   post_launch("split");
   return pb;
@@ -1309,25 +1310,10 @@ extern "C" int nrg_dgemm_tc(nrg_engine *e, int transA, int transB, int M, int N,
     check_cuda(cudaMemcpy2DAsync(db->ptr, bc * 8, B, ldb * 8, bc * 8, br, cudaMemcpyHostToDevice, s), "B");
     if (beta != 0.0)
       check_cuda(cudaMemcpy2DAsync(dc->ptr, N * 8, C, ldc * 8, N * 8, M, cudaMemcpyHostToDevice, s), "C");
-    const int lpa = round_up(ac, 8), lpb = round_up(bc, 8);
-    DevPtr pa = dalloc(e, int64_t(ar) * lpa * 8 * 2 + 16), pb = dalloc(e, int64_t(br) * lpb * 8 * 2 + 16),
-           ex = dalloc(e, 64);
-    std::vector<SplitTask> t(2);
-    t[0] = SplitTask{static_cast<double *>(da->ptr), ar, ac, ac, lpa, pa->ptr, int64_t(ar) * lpa,
-                     static_cast<int *>(ex->ptr)};
-    t[1] = SplitTask{static_cast<double *>(db->ptr), br, bc, bc, lpb, pb->ptr, int64_t(br) * lpb,
-                     static_cast<int *>(ex->ptr) + 1};
-    Arena a;
-    size_t o = a.add(t);
-    DevPtr dd;
-    char *dp = a.push(e, dd);
-    launch_split(at<SplitTask>(dp, o), 2, s);
-    count_launch(e);
-    post_launch("split");
-    OzOperand oa{static_cast<const __nv_bfloat16 *>(pa->ptr), int64_t(ar) * lpa, lpa, 0,
-                 static_cast<const int *>(ex->ptr)};
-    OzOperand ob{static_cast<const __nv_bfloat16 *>(pb->ptr), int64_t(br) * lpb, lpb, 0,
-                 static_cast<const int *>(ex->ptr) + 1};
+    const PlaneBuf pl = split_matrices(e, {MatRef{static_cast<const double *>(da->ptr), ar, ac, ac},
+                                           MatRef{static_cast<const double *>(db->ptr), br, bc, bc}},
+                                       hold);
+    const OzOperand oa = pl.op(0), ob = pl.op(1);
     OzList l;
     l.out(static_cast<double *>(dc->ptr), N, M, N, beta != 0.0,
           {ozc(oa, ob, K, (transA ? 1 : 0) | (transB ? 2 : 0), alpha)});

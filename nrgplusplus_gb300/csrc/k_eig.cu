@@ -791,11 +791,10 @@ template <typename T>
 void launch(const EigBlock *blocks, int nblocks, int max_n, int max_n_smem, int *status,
             cudaStream_t s, const int *gate = nullptr) {
   if (nblocks == 0) return;
-  static bool configured = false;
-  if (!configured) {
-    cudaFuncSetAttribute(k_eig<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
-    configured = true;
-  }
+  // once per process, thread-safe (engines may launch from several threads)
+  static const bool configured =
+      (cudaFuncSetAttribute(k_eig<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes), true);
+  (void)configured;
   // enough shared memory for the largest block of this launch
   size_t bytes = smem_bytes<T>(max_n, max_n <= max_n_smem);
   if (max_n > max_n_smem) bytes = std::max(bytes, smem_bytes<T>(max_n_smem, true));
@@ -826,11 +825,10 @@ void launch_eig_f64(const EigBlock *blocks, int nblocks, int max_n, int max_n_sm
 void launch_eig_bisect_f32(const EigBlock *blocks, int nblocks, int max_n, int max_n_smem,
                            cudaStream_t s) {
   if (nblocks == 0) return;
-  static bool configured = false;
-  if (!configured) {
-    cudaFuncSetAttribute(k_eig_bi, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
-    configured = true;
-  }
+  // once per process, thread-safe (engines may launch from several threads)
+  static const bool configured =
+      (cudaFuncSetAttribute(k_eig_bi, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes), true);
+  (void)configured;
   size_t bytes = smem_bytes<float>(max_n, max_n <= max_n_smem);
   if (max_n > max_n_smem) bytes = std::max(bytes, smem_bytes<float>(max_n_smem, true));
   if (bytes > size_t(kSmemBytes)) bytes = kSmemBytes;
@@ -857,11 +855,10 @@ int reflect_max_n() {
 
 template <int TW> static void reflect_launch(const EigBlock *blocks, const int2 *tiles, int ntiles, int panel,
                                              size_t bytes, cudaStream_t s) {
-  static bool cfg = false;
-  if (!cfg) {
-    cudaFuncSetAttribute(k_reflect<TW>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kReflectSmem));
-    cfg = true;
-  }
+  // once per process, thread-safe (engines may launch from several threads)
+  static const bool cfg =
+      (cudaFuncSetAttribute(k_reflect<TW>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kReflectSmem)), true);
+  (void)cfg;
   k_reflect<TW><<<ntiles, 256, bytes, s>>>(blocks, tiles, panel);
 }
 

@@ -40,11 +40,22 @@ __device__ __forceinline__ uint32_t smem_u32(const void *p) {
 }
 
 // ---------------------------------------------------------------- split
-// Two grid-wide passes over every element of every task (chunks of 1024
-// elements, task located by binary search on the chunk prefix):
+// Two grid-wide passes over the padded elements of every task (chunks of
+// kSplitChunk, task located by binary search on the chunk prefix):
 //   k_split_max:    per-task max |x| by atomicMax on the IEEE bits (for
 //                   non-negative doubles the bit order is the value order);
 //   k_split_digits: exponent from the max, then the 8 digits per element.
+// Both work on the IEEE-754 fields with integer instructions only: GB300's
+// FP64 pipe issues about 2 operations per clock per SM, 64 times fewer than
+// its integer pipes, and the split touches every element of every operand.
+// Each thread loads its 16 elements before it uses any of them (16
+// independent loads in flight per thread).
+constexpr int kSplitThreads = 256, kSplitPer = 16, kSplitChunk = kSplitThreads * kSplitPer;
+// block exponent of a task whose max is Inf or NaN: 2^(eA+eB-61) overflows,
+// so every product with it is NaN and the refinement's convergence check
+// sends the block to the FP64 solver
+constexpr int kNonFiniteExp = 4096;
+
 __device__ __forceinline__ int find_task(const int64_t *chunk0, int ntasks, int64_t chunk) {
   int lo = 0, hi = ntasks - 1;
   while (lo < hi) {
@@ -54,86 +65,115 @@ __device__ __forceinline__ int find_task(const int64_t *chunk0, int ntasks, int6
   return lo;
 }
 
-__global__ void __launch_bounds__(256)
+// e with max|x| < 2^e, i.e. ilogb(max) + 1 (0 for an all-zero task)
+__device__ __forceinline__ int split_exp(unsigned long long maxbits) {
+  if (maxbits == 0) return 0;
+  const int ef = int(maxbits >> 52);
+  if (ef == 0x7FF) return kNonFiniteExp;
+  if (ef == 0) return -1010 - __clzll(static_cast<long long>(maxbits));  // subnormal maximum
+  return ef - 1022;
+}
+
+// rint(x * 2^s), ties to even, from the fields of x = m 2^ex (m < 2^53):
+// shifts of m instead of an FP64 multiply and conversion.  The caller's s
+// keeps |x| 2^s < 2^55, so a left shift cannot overflow.
+__device__ __forceinline__ long long scale_round(unsigned long long b, int s) {
+  const int ef = int((b >> 52) & 0x7FF);
+  unsigned long long m = b & ((1ull << 52) - 1);
+  int ex = -1074;
+  if (ef) {
+    m |= 1ull << 52;
+    ex = ef - 1075;
+  }
+  const int sh = ex + s;
+  unsigned long long q;
+  if (sh >= 0) {
+    q = m << sh;
+  } else if (sh <= -55) {
+    q = 0;  // below half a unit
+  } else {
+    const int r = -sh;
+    q = m >> r;
+    const unsigned long long rem = m & ((1ull << r) - 1), half = 1ull << (r - 1);
+    q += (rem > half || (rem == half && (q & 1))) ? 1 : 0;
+  }
+  return (b >> 63) ? -static_cast<long long>(q) : static_cast<long long>(q);
+}
+
+// bf16 bits of a small integer (|a| <= 64): 1.5 2^23 + a is exact in FP32,
+// subtracting 1.5 2^23 leaves float(a), whose low 16 bits are zero
+__device__ __forceinline__ unsigned short small_int_bf16(int a) {
+  return static_cast<unsigned short>(__float_as_uint(__int_as_float(0x4B400000 + a) - 12582912.0f) >> 16);
+}
+
+// balanced base-128 digits of |X| <= 2^55, least significant first, in
+// 32-bit arithmetic: 4 digits from the low 28 bits, their carry into the
+// high part, 3 more digits; the most significant digit is the remainder
+// itself, which lies in [-64, 64] (the lower digits sum to less than
+// 0.504 * 128^7)
+__device__ __forceinline__ void store_digits(long long X, unsigned short *pl, int64_t pstride, int64_t i) {
+  int L = int(X & 0xFFFFFFF), H = int(X >> 28);
+#pragma unroll
+  for (int p = kPlanes - 1; p >= 4; --p) {
+    const int a = ((L + 64) & 127) - 64;
+    L = (L - a) >> 7;
+    pl[int64_t(p) * pstride + i] = small_int_bf16(a);
+  }
+  H += L;
+#pragma unroll
+  for (int p = 3; p >= 1; --p) {
+    const int a = ((H + 64) & 127) - 64;
+    H = (H - a) >> 7;
+    pl[int64_t(p) * pstride + i] = small_int_bf16(a);
+  }
+  pl[i] = small_int_bf16(H);
+}
+
+__global__ void __launch_bounds__(kSplitThreads)
 k_split_max(const SplitTask *__restrict__ tasks, const int64_t *__restrict__ chunk0, int ntasks,
             unsigned long long *__restrict__ maxbits) {
   const int t = find_task(chunk0, ntasks, blockIdx.x);
   const SplitTask T = tasks[t];
-  const int64_t base = (int64_t(blockIdx.x) - chunk0[t]) * 1024;
-  const int64_t nel = int64_t(T.rows) * T.cols;
-  double m = 0.0;
-  for (int u = 0; u < 4; ++u) {
-    const int64_t i = base + u * 256 + threadIdx.x;
-    if (i < nel) {
-      const int r = int(i / T.cols), c = int(i - int64_t(r) * T.cols);
-      m = fmax(m, fabs(T.src[int64_t(r) * T.ld + c]));
-    }
+  const int base = int(int64_t(blockIdx.x) - chunk0[t]) * kSplitChunk;
+  const int nel = T.rows * T.ldp;
+  const unsigned long long *src = reinterpret_cast<const unsigned long long *>(T.src);
+  unsigned long long v[kSplitPer];
+#pragma unroll
+  for (int u = 0; u < kSplitPer; ++u) {
+    const int i = base + u * kSplitThreads + int(threadIdx.x);
+    const int r = unsigned(i) / unsigned(T.ldp), c = i - r * T.ldp;
+    v[u] = (i < nel && c < T.cols) ? src[int64_t(r) * T.ld + c] : 0ull;
   }
-  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
-  if ((threadIdx.x & 31) == 0 && m > 0.0)
-    atomicMax(maxbits + t, static_cast<unsigned long long>(__double_as_longlong(m)));
+  unsigned long long m = 0;
+#pragma unroll
+  for (int u = 0; u < kSplitPer; ++u) m = max(m, v[u] & 0x7FFFFFFFFFFFFFFFull);
+  for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0 && m > 0) atomicMax(maxbits + t, m);
 }
 
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(kSplitThreads)
 k_split_digits(const SplitTask *__restrict__ tasks, const int64_t *__restrict__ chunk0, int ntasks,
                const unsigned long long *__restrict__ maxbits) {
   const int t = find_task(chunk0, ntasks, blockIdx.x);
   const SplitTask T = tasks[t];
-  const double mx = __longlong_as_double(static_cast<long long>(maxbits[t]));
-  const int e = (mx > 0.0 && isfinite(mx)) ? ilogb(mx) + 1 : 0;
+  const int e = split_exp(maxbits[t]);
   if (blockIdx.x == chunk0[t] && threadIdx.x == 0) *T.exp = e;
-  const int64_t base = (int64_t(blockIdx.x) - chunk0[t]) * 1024;
-  const int64_t nel = int64_t(T.rows) * T.ldp;
-  __nv_bfloat16 *pl = static_cast<__nv_bfloat16 *>(T.planes);
-  for (int u = 0; u < 4; ++u) {
-    const int64_t i = base + u * 256 + threadIdx.x;
-    if (i >= nel) break;
-    const int r = int(i / T.ldp), c = int(i - int64_t(r) * T.ldp);
-    long long X = 0;
-    if (c < T.cols) X = llrint(scalbn(T.src[int64_t(r) * T.ld + c], 55 - e));
-    // balanced base-128 digits, least significant first; the most
-    // significant digit is the remainder itself, which lies in [-64, 64]
+  const int base = int(int64_t(blockIdx.x) - chunk0[t]) * kSplitChunk;
+  const int nel = T.rows * T.ldp;
+  const unsigned long long *src = reinterpret_cast<const unsigned long long *>(T.src);
+  unsigned long long v[kSplitPer];
 #pragma unroll
-    for (int p = kPlanes - 1; p >= 1; --p) {
-      const long long a = ((X + 64) & 127) - 64;
-      X = (X - a) >> 7;
-      pl[int64_t(p) * T.pstride + i] = __float2bfloat16_rn(float(a));
-    }
-    pl[i] = __float2bfloat16_rn(float(X));
+  for (int u = 0; u < kSplitPer; ++u) {
+    const int i = base + u * kSplitThreads + int(threadIdx.x);
+    const int r = unsigned(i) / unsigned(T.ldp), c = i - r * T.ldp;
+    v[u] = (i < nel && c < T.cols) ? src[int64_t(r) * T.ld + c] : 0ull;
   }
-}
-
-__global__ void __launch_bounds__(256) k_split(const SplitTask *__restrict__ tasks) {
-  __shared__ double red[8];
-  const SplitTask T = tasks[blockIdx.x];
-  const int64_t nel = int64_t(T.rows) * T.cols;
-  double m = 0.0;
-  for (int64_t i = threadIdx.x; i < nel; i += blockDim.x) {
-    const int r = int(i / T.cols), c = int(i - int64_t(r) * T.cols);
-    m = fmax(m, fabs(T.src[int64_t(r) * T.ld + c]));
-  }
-  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
-  __syncthreads();
-  double mx = red[0];
-  for (int w = 1; w < int(blockDim.x >> 5); ++w) mx = fmax(mx, red[w]);
-  const int e = (mx > 0.0 && isfinite(mx)) ? ilogb(mx) + 1 : 0;
-  if (threadIdx.x == 0) *T.exp = e;
-  for (int64_t i = threadIdx.x; i < int64_t(T.rows) * T.ldp; i += blockDim.x) {
-    const int r = int(i / T.ldp), c = int(i - int64_t(r) * T.ldp);
-    long long X = 0;
-    if (c < T.cols) X = llrint(scalbn(T.src[int64_t(r) * T.ld + c], 55 - e));
-    // balanced base-128 digits, least significant first; the most
-    // significant digit is the remainder itself, which lies in [-64, 64]
-    // (|X| <= 2^55 and the lower digits sum to less than 0.504 * 128^7)
-    __nv_bfloat16 *pl = static_cast<__nv_bfloat16 *>(T.planes);
+  unsigned short *pl = static_cast<unsigned short *>(T.planes);
+  const bool finite = e != kNonFiniteExp;
 #pragma unroll
-    for (int p = kPlanes - 1; p >= 1; --p) {
-      const long long a = ((X + 64) & 127) - 64;
-      X = (X - a) >> 7;
-      pl[int64_t(p) * T.pstride + i] = __float2bfloat16_rn(float(a));
-    }
-    pl[i] = __float2bfloat16_rn(float(X));
+  for (int u = 0; u < kSplitPer; ++u) {
+    const int i = base + u * kSplitThreads + int(threadIdx.x);
+    if (i < nel) store_digits(finite ? scale_round(v[u], 55 - e) : 0ll, pl, T.pstride, i);
   }
 }
 
@@ -450,28 +490,23 @@ constexpr size_t kGemmSmem = size_t(kStages) * kStageBytes;
 
 }  // namespace
 
-void launch_split(const SplitTask *tasks, int ntasks, cudaStream_t s) {
-  if (ntasks == 0) return;
-  k_split<<<ntasks, 256, 0, s>>>(tasks);
-}
+int split_chunk_elements() { return kSplitChunk; }
 
-void launch_split_grid(const SplitTask *tasks, const int64_t *chunk0_max, const int64_t *chunk0_dig,
-                       int ntasks, int64_t nchunk_max, int64_t nchunk_dig, unsigned long long *maxbits,
-                       cudaStream_t s) {
-  if (ntasks == 0) return;
+void launch_split_grid(const SplitTask *tasks, const int64_t *chunk0, int ntasks, int64_t nchunks,
+                       unsigned long long *maxbits, cudaStream_t s) {
+  if (ntasks == 0 || nchunks == 0) return;
   cudaMemsetAsync(maxbits, 0, sizeof(unsigned long long) * ntasks, s);
-  if (nchunk_max > 0) k_split_max<<<unsigned(nchunk_max), 256, 0, s>>>(tasks, chunk0_max, ntasks, maxbits);
-  k_split_digits<<<unsigned(nchunk_dig), 256, 0, s>>>(tasks, chunk0_dig, ntasks, maxbits);
+  k_split_max<<<unsigned(nchunks), kSplitThreads, 0, s>>>(tasks, chunk0, ntasks, maxbits);
+  k_split_digits<<<unsigned(nchunks), kSplitThreads, 0, s>>>(tasks, chunk0, ntasks, maxbits);
 }
 
 void launch_gemm_oz(const GemmTile *tiles, int ntiles, const OzGroup *groups, const OzContrib *contribs,
                     int *err, cudaStream_t s) {
   if (ntiles == 0) return;
-  static bool cfg = false;
-  if (!cfg) {
-    cudaFuncSetAttribute(k_gemm_oz, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kGemmSmem));
-    cfg = true;
-  }
+  // once per process, thread-safe (engines may launch from several threads)
+  static const bool cfg =
+      (cudaFuncSetAttribute(k_gemm_oz, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kGemmSmem)), true);
+  (void)cfg;
   k_gemm_oz<<<ntiles, kTcThreads, kGemmSmem, s>>>(tiles, groups, contribs, err);
 }
 

@@ -143,13 +143,12 @@ struct OzGroup {
   int c0, c1;
   int planes, pad;  // digit planes used (1..8): groups d < planes, pairs p + q < planes
 };
-void launch_split(const SplitTask *tasks, int ntasks, cudaStream_t s);
-// Grid-wide split: chunk0_max / chunk0_dig are per-task prefix counts of
-// 1024-element chunks over rows*cols (max pass) and rows*ldp (digit pass);
+// Grid-wide split: chunk0 holds per-task prefix counts of chunks of
+// split_chunk_elements() padded elements (rows * ldp, below 2^31 per task);
 // maxbits: ntasks of scratch.
-void launch_split_grid(const SplitTask *tasks, const int64_t *chunk0_max, const int64_t *chunk0_dig,
-                       int ntasks, int64_t nchunk_max, int64_t nchunk_dig, unsigned long long *maxbits,
-                       cudaStream_t s);
+int split_chunk_elements();
+void launch_split_grid(const SplitTask *tasks, const int64_t *chunk0, int ntasks, int64_t nchunks,
+                       unsigned long long *maxbits, cudaStream_t s);
 // tiles: (group, 128-row tile, 64-column tile); *err is set when a bounded
 // wait inside the kernel runs out (the launch then leaves its tile unfinished)
 constexpr int OZ_TILE_M = 128, OZ_TILE_N = 64;

@@ -1,11 +1,14 @@
 """Benchmark: complete SIAM FDM runs per second on one GB300.
 
-One step = one full run of the spectral workload (eps_d=-0.4, U=0.8, V=0.15,
-Lambda=2, Nkeep=1024, 50 Wilson sites): forward NRG with the d-dagger-chi
-operators tracked and device-resident snapshots, the T=0 FDM backward pass
-(binning into 1e5 log bins), log-Gaussian broadening (b=0.6, 100 points per
-decade over |w| in [1e-8, 1]) and entropy / specific heat on the 200-point
-temperature grid.  The reference publishes no number for this metric.
+One run = the spectral workload (eps_d=-0.4, U=0.8, V=0.15, Lambda=2,
+Nkeep=1024, 50 Wilson sites): forward NRG with the d-dagger-chi operators
+tracked and device-resident snapshots, the T=0 FDM backward pass (binning
+into 1e5 log bins), log-Gaussian broadening (b=0.6, 100 points per decade
+over |w| in [1e-8, 1]) and entropy / specific heat on the 200-point
+temperature grid.  One step = ENGINES engines, each driven by its own host
+thread, each stepping RUNS_PER_ENGINE runs together (batched launches); the
+engines' streams overlap one engine's host work with another's kernels.
+The reference publishes no number for this metric.
 
   value : runs/s through the engine, results left on the device
   e2e   : runs/s through the public C-ABI calls a user makes, with the
@@ -32,18 +35,21 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 WORK = dict(kind="siam", nkeep=1024, nsites=50, lam=2.0, eps=-0.4, U=0.8, V=0.15)
-BATCH = int(os.environ.get("NRG_BENCH_BATCH", "16"))  # runs stepped together per step
+BATCH = int(os.environ.get("NRG_BENCH_BATCH", "8"))  # runs stepped together per engine
+ENGINES = int(os.environ.get("NRG_BENCH_ENGINES", "4"))  # engines (host threads) per step
 CONFIG = {"workload": "siam_fdm_spectral_c2", "impurity": "spinhalf(eps_d=-0.4,U=0.8)",
           "V": 0.15, "Lambda": 2.0, "Nkeep": 1024, "sites": 50, "T": 1e-6,
           "spectral": "T=0 FDM, b=0.6, 801 points |w| in [1e-8,1]",
           "thermo": "entropy + C on 200-point T grid",
-          "l2": "flushed (256 MiB write) between steps", "runs_per_step": BATCH}
+          "l2": "flushed (256 MiB write) between steps", "runs_per_step": ENGINES * BATCH,
+          "engines": ENGINES, "runs_per_engine": BATCH}
 METRIC = "SIAM runs/s (full FDM spectral run, Nkeep=1024, 50 sites)"
 
 
-def serving_run(engine, rate, n, seed=2024, max_active=16):
+def serving_run(engine, rate, n, seed=2024, max_active=BATCH, workers=ENGINES):
     """Seeded Poisson stream of n workload requests at `rate` per second into
-    the serving loop; latency = submission to completed results."""
+    the serving loop (`workers` engines, up to `max_active` runs each);
+    latency = submission to completed results."""
     import threading
     import numpy as np
     from nrgplusplus_gb300 import api, workloads
@@ -51,7 +57,7 @@ def serving_run(engine, rate, n, seed=2024, max_active=16):
     req = workloads.siam_request(w["nkeep"], w["nsites"], w["lam"], w["V"], eps=w["eps"], U=w["U"],
                                  fdm=True, thermo=True, keep_eigs=False)
     gaps = np.random.default_rng(seed).exponential(1.0 / rate, size=n)
-    srv = api.Server(engine, max_active=max_active)
+    srv = api.Server(engine, max_active=max_active, workers=workers)
     ids = []
 
     def arrivals():
@@ -69,7 +75,8 @@ def serving_run(engine, rate, n, seed=2024, max_active=16):
     wall = time.perf_counter() - t0
     st = srv.stats()
     srv.close()
-    return {"requests": n, "arrival_rate_per_s": rate, "seed": seed, "max_active": max_active,
+    return {"requests": n, "arrival_rate_per_s": rate, "seed": seed, "max_active_per_worker": max_active,
+            "workers": workers,
             "runs_per_s": st["completed"] / wall, "p50_latency_s": st["p50_latency_s"],
             "p99_latency_s": st["p99_latency_s"], "mean_latency_s": st["mean_latency_s"],
             "max_active_seen": int(st["max_active_seen"]), "failed": int(st["failed"]),
@@ -223,6 +230,29 @@ def one_run(engine, e2e, batch=None):
     return h2d, d2h
 
 
+def step(engines, e2e, batch=None):
+    """One bench step: every engine runs one_run in its own host thread
+    (ctypes releases the GIL inside each C-ABI call).  Returns the summed
+    (h2d, d2h) bytes; re-raises the first error of any thread."""
+    import threading
+    res, errs = [None] * len(engines), []
+
+    def drive(k):
+        try:
+            res[k] = one_run(engines[k], e2e, batch)
+        except BaseException as x:  # noqa: BLE001 - re-raised below
+            errs.append(x)
+
+    ths = [threading.Thread(target=drive, args=(k,)) for k in range(len(engines))]
+    for t in ths:
+        t.start()
+    for t in ths:
+        t.join()
+    if errs:
+        raise errs[0]
+    return sum(r[0] for r in res), sum(r[1] for r in res)
+
+
 def time_oracle_run(max_sites):
     """The oracle port on this host's cores: the same workload, forward sites
     capped at max_sites (bounded sample)."""
@@ -350,7 +380,7 @@ def main():
                     help="forward sites of the bounded CPU-baseline sample")
     ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 comparator")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving-loop measurement")
-    ap.add_argument("--serving-requests", type=int, default=32)
+    ap.add_argument("--serving-requests", type=int, default=64)
     ap.add_argument("--sites", type=int, default=50,
                     help="Wilson sites per run (50 = the workload; fewer only for profiling captures)")
     args = ap.parse_args()
@@ -370,7 +400,8 @@ def main():
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     torch.cuda.set_device(local)
     build(verbose=False)
-    engine = api.Engine(api.PREC_MIXED, device=local)
+    engines = [api.Engine(api.PREC_MIXED, device=local) for _ in range(ENGINES)]
+    engine = engines[0]
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
 
     def barrier():
@@ -379,54 +410,62 @@ def main():
         torch.cuda.synchronize()
 
     for _ in range(args.warmup):
-        one_run(engine, e2e=False)
+        step(engines, e2e=False)
     times, d2h = [], 0
-    l0 = engine.launch_count()
+    launch_total = lambda: sum(e.launch_count() for e in engines)  # noqa: E731
+    l0 = launch_total()
     os.makedirs(os.path.join(ROOT, "gpurun_out"), exist_ok=True)
     with ClockSampler(os.path.join(ROOT, "gpurun_out", "bench_clocks.csv")) as clk:
         for _ in range(args.steps):
             flush.zero_()
             barrier()
             t0 = time.perf_counter()
-            one_run(engine, e2e=False)
-            engine.sync()
+            step(engines, e2e=False)
+            for e in engines:
+                e.sync()
             barrier()
             times.append(time.perf_counter() - t0)
-        launches = (engine.launch_count() - l0) // args.steps
+        launches = (launch_total() - l0) // args.steps
         e2e_times = []
         for _ in range(args.steps):
             flush.zero_()
             barrier()
             t0 = time.perf_counter()
-            h2d, d2h = one_run(engine, e2e=True)
-            engine.sync()
+            h2d, d2h = step(engines, e2e=True)
+            for e in engines:
+                e.sync()
             barrier()
             e2e_times.append(time.perf_counter() - t0)
+    runs = ENGINES * BATCH
     tsum, esum = max_over_ranks([sum(times), sum(e2e_times)])
     per = tsum / args.steps
-    value = ws * BATCH / per
-    e2e_v = ws * BATCH / (esum / args.steps)
+    value = ws * runs / per
+    e2e_v = ws * runs / (esum / args.steps)
     kt = kernel_profile(engine)
     rf = roofline_from(kt)
-    fallbacks = engine.fallback_count()
-    hbm_peak = engine.memory()[1]
+    fallbacks = sum(e.fallback_count() for e in engines)
+    hbm_peak = sum(e.memory()[1] for e in engines)
+    for e in engines[1:]:
+        e.close()
     serving = None
     if not args.no_serving:
-        serving = serving_run(engine, 0.8 * BATCH / per, args.serving_requests)
+        serving = serving_run(engine, 0.8 * runs / per, args.serving_requests)
     engine.close()
     plain = None
     if not args.no_fp64:
-        e64 = api.Engine(api.PREC_FP64, device=local)
+        e64s = [api.Engine(api.PREC_FP64, device=local) for _ in range(ENGINES)]
         flush.zero_()
         barrier()
         t0 = time.perf_counter()
-        one_run(e64, e2e=False)
-        e64.sync()
+        step(e64s, e2e=False)
+        for e in e64s:
+            e.sync()
         barrier()
         t64 = time.perf_counter() - t0
-        e64.close()
-        plain = {"value": ws * BATCH / t64, "unit": "runs/s", "ms_per_step": t64 * 1e3,
-                 "speedup_mixed_over_fp64": value / (ws * BATCH / t64)}
+        for e in e64s:
+            e.close()
+        plain = {"value": ws * runs / t64, "unit": "runs/s", "ms_per_step": t64 * 1e3,
+                 "speedup_mixed_over_fp64": value / (ws * runs / t64)}
     cpu = None
     if rank == 0 and ws == 1:
         sites = max(1, min(args.cpu_sites, WORK["nsites"]))
@@ -446,7 +485,9 @@ def main():
                 "e2e": {"value": e2e_v, "unit": "runs/s", "h2d_bytes_per_step": int(h2d),
                         "d2h_bytes_per_step": int(d2h)},
                 "serving": serving, "plain_fp64": plain, "roofline": rf,
-                "kernels_ms_per_step": {k: round(v[0], 3) for k, v in kt.items()},
+                "kernels_ms_per_engine_batch": {k: round(v[0], 3) for k, v in kt.items()},
+                "kernels_profiled": "one engine's %d-run batch alone, per-kernel CUDA events on its stream"
+                                    % BATCH,
                 "cpu_baseline": cpu, "clocks": clk.summary()}
         print(json.dumps(line))
     if ws > 1:

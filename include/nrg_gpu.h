@@ -101,6 +101,8 @@ int nrg_engine_destroy(nrg_engine *eng);
  * out[0] assemble, out[1] eigensolve, out[2] truncate, out[3] rotate,
  * out[4] operators; n = entries written. */
 int nrg_engine_phase_times(nrg_engine *eng, double *out, int cap, int *n);
+/* The options the engine was created with. */
+int nrg_engine_get_opts(nrg_engine *eng, nrg_engine_opts *out);
 /* Number of kernel launches issued by the engine so far. */
 int nrg_engine_launch_count(nrg_engine *eng, uint64_t *out);
 /* Mixed precision: number of blocks whose refinement did not converge and
@@ -253,19 +255,25 @@ int nrg_batch_update_state(nrg_run *const *runs, int nruns);
 
 /* ---- serving loop: continuous batching of whole runs ------------------- */
 /* No counterpart in the reference (its drivers run one nrgcore at a time).
- * A server owns a worker thread that drives one engine: requests submitted
- * from any thread queue up, are admitted while fewer than max_active runs
- * are active and their estimated device footprint fits hbm_budget_bytes
- * (0 = no budget; an idle server admits one request regardless), and every
- * tick advances all active runs by one Wilson site in shared launches
+ * A server owns worker threads, each driving one engine (the first worker the
+ * engine given to nrg_server_create, every further worker an engine the
+ * server creates with the same options and destroys with the server):
+ * requests submitted from any thread queue up, are admitted by the workers
+ * while a worker has fewer than max_active runs (and no more than its even
+ * share of the active and queued runs) and their estimated device footprint
+ * fits hbm_budget_bytes next to the reservations of every active run (0 = no
+ * budget; an idle server admits one request regardless), and every tick of a
+ * worker advances its active runs by one Wilson site in shared launches
  * (nrg_batch_add_site per hopping count), then runs the backward passes
- * (FDM spectrum, thermodynamics) of the runs that finished.  Results are
- * kept until nrg_server_release.  The engine must not be used by other
- * threads while a server drives it. */
+ * (FDM spectrum, thermodynamics) of its runs that finished.  Several workers
+ * overlap the host work of one engine's tick with the GPU work of another's.
+ * Results are kept until nrg_server_release.  The given engine must not be
+ * used by other threads while a server drives it. */
 typedef struct nrg_server nrg_server;
 typedef struct {
-  int max_active;             /* runs stepped together (>= 1) */
-  uint64_t hbm_budget_bytes;  /* admission budget, 0 = none */
+  int max_active;             /* runs stepped together per worker (>= 1) */
+  uint64_t hbm_budget_bytes;  /* admission budget over all workers, 0 = none */
+  int workers;                /* worker threads / engines, 0 or 1 = one */
 } nrg_server_opts;
 typedef struct {
   const nrg_site_desc *impurity, *bath;

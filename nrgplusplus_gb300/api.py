@@ -58,7 +58,7 @@ class RunInfo(C.Structure):
 
 EXPORTS = [
     "nrg_last_error", "nrg_engine_create", "nrg_engine_destroy", "nrg_engine_phase_times",
-    "nrg_engine_launch_count", "nrg_engine_fallback_count", "nrg_engine_memory", "nrg_engine_set_profiling",
+    "nrg_engine_launch_count", "nrg_engine_get_opts", "nrg_engine_fallback_count", "nrg_engine_memory", "nrg_engine_set_profiling",
     "nrg_engine_kernel_times",
     "nrg_engine_sync", "nrg_run_create", "nrg_run_destroy",
     "nrg_run_set_parameters", "nrg_run_set_bath", "nrg_run_add_site", "nrg_run_update_state",
@@ -570,7 +570,7 @@ def batch_update_state(runs):
 
 # ---------------------------------------------------------------- serving loop
 class _ServerOpts(C.Structure):
-    _fields_ = [("max_active", C.c_int), ("hbm_budget_bytes", C.c_uint64)]
+    _fields_ = [("max_active", C.c_int), ("hbm_budget_bytes", C.c_uint64), ("workers", C.c_int)]
 
 
 class _Request(C.Structure):
@@ -596,15 +596,18 @@ class _ServerStats(C.Structure):
 
 
 class Server:
-    """Continuous-batching serving loop over one engine (nrg_server_*): whole
-    NRG runs are submitted from any thread, admitted by count and HBM budget,
-    stepped together one Wilson site per tick, and their backward passes run
-    when they finish.  The engine must not be used elsewhere while it serves."""
+    """Continuous-batching serving loop (nrg_server_*): whole NRG runs are
+    submitted from any thread, admitted by count and HBM budget, stepped
+    together one Wilson site per tick, and their backward passes run when
+    they finish.  `workers` worker threads each drive one engine (the given
+    one and workers - 1 the server creates with its options), so the host
+    work of one tick overlaps the GPU work of another.  The given engine must
+    not be used elsewhere while it serves."""
 
-    def __init__(self, engine, max_active=16, hbm_budget_bytes=0):
+    def __init__(self, engine, max_active=16, hbm_budget_bytes=0, workers=1):
         self.engine = engine
         self.h = C.c_void_p()
-        opts = _ServerOpts(max_active, hbm_budget_bytes)
+        opts = _ServerOpts(max_active, hbm_budget_bytes, workers)
         _call(lib().nrg_server_create, engine.h, C.byref(opts), C.byref(self.h))
 
     def submit(self, impurity, bath, nkeep, t, rescale, ops=None, fdm=False, temps=None, shell_scale=None,

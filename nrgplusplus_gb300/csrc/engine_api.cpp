@@ -661,6 +661,17 @@ int nrg_engine_kernel_times(nrg_engine *e, char *names, uint64_t names_cap, doub
   });
 }
 
+int nrg_engine_get_opts(nrg_engine *e, nrg_engine_opts *out) {
+  return guard([&] {
+    if (!e || !out) fail(NRG_E_ARG, "null argument");
+    *out = nrg_engine_opts{};
+    out->device = e->device;
+    out->precision = e->precision;
+    out->hbm_budget_bytes = e->budget;
+    out->verbose = e->verbose;
+  });
+}
+
 int nrg_engine_launch_count(nrg_engine *e, uint64_t *out) {
   return guard([&] {
     if (!e || !out) fail(NRG_E_ARG, "null argument");

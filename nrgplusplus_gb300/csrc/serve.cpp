@@ -1,21 +1,27 @@
-// Serving loop: continuous batching of complete NRG runs on one engine.
+// Serving loop: continuous batching of complete NRG runs.
 //
 // Requests (a whole run: models, hoppings, tracked operators, FDM spectrum
 // and thermodynamics) arrive from any host thread through nrg_server_submit
-// and wait in a FIFO queue.  One worker thread owns the engine and repeats a
-// tick:
-//   1. admit queued requests while the active count is below max_active and
-//      their estimated device footprint fits the HBM budget next to the
-//      reservations of the active runs (an idle server admits one request
+// and wait in a FIFO queue.  Each worker thread owns one engine (its own
+// CUDA stream) and repeats a tick:
+//   1. admit queued requests while its active count is below max_active and
+//      below its even share of all active and queued runs, and while their
+//      estimated device footprint fits the HBM budget next to the
+//      reservations of every active run (an idle server admits one request
 //      regardless, so a request larger than the budget still runs alone);
 //   2. advance every active run in its forward phase by one Wilson site:
-//      one nrg_batch_add_site / nrg_batch_update_state per hopping count,
-//      so the blocks of runs at different sites share every launch, with the
-//      tracked-operator update and the snapshot of each run in between
-//      (update_system_operator and saveCurrentData, in the reference's order);
+//      one nrg_batch_add_site / nrg_opset_update_batch /
+//      nrg_batch_update_state per hopping count, so the blocks of runs at
+//      different sites share every launch, with the snapshot of each run in
+//      between (update_system_operator and saveCurrentData, in the
+//      reference's order);
 //   3. run the backward passes (FDM spectrum, thermodynamics) of the runs
-//      that finished their last site, collect their results and free them.
+//      that finished their last site, shell by shell from the last, the FDM
+//      shells of all of them in one nrg_fdm_calc_batch per step; collect
+//      their results and free them.
 // Requests that arrive while a tick is on the GPU join at the next tick.
+// While one worker's host thread prepares its next launches, the kernels of
+// the other workers' ticks keep the GPU busy.
 // The footprint estimate is coef * nsites * (bath states * nkeep)^2 bytes;
 // coef starts at 2 and is raised to 1.1x the largest ratio a finished run
 // has shown (its peak device bytes over the same product).
@@ -159,6 +165,7 @@ struct Job {
   std::vector<uint64_t> eig_counts;
   std::vector<double> energy_points, positive, negative, entropy, cv;
   Clock::time_point t_submit, t_admit, t_finish;
+  bool admitted = false;  // counted in the server's active runs and reservation
 
   void release_device() {
     if (opset) nrg_opset_destroy(opset);
@@ -174,8 +181,14 @@ void check(int rc, const char *what) {
 
 }  // namespace
 
-struct nrg_server {
+struct Worker {
   nrg_engine *eng = nullptr;
+  bool owns_engine = false;
+  std::thread th;
+  std::vector<std::shared_ptr<Job>> active;  // touched by this worker's thread only
+};
+
+struct nrg_server {
   int device = 0;  // CUDA device current when the server was created
   int max_active = 16;
   uint64_t budget = 0;
@@ -184,10 +197,11 @@ struct nrg_server {
   std::condition_variable cv_work, cv_done;
   std::deque<std::shared_ptr<Job>> queue;
   std::map<uint64_t, std::shared_ptr<Job>> jobs;  // every job not yet released
-  std::vector<std::shared_ptr<Job>> active;       // owned by the worker
+  std::vector<std::unique_ptr<Worker>> workers;
+  uint64_t n_active = 0;  // admitted, not finished (all workers)
+  double reserved = 0;    // footprint estimates of those runs
   uint64_t next_id = 1;
   bool stop = false;
-  std::thread worker;
   // statistics
   uint64_t submitted = 0, completed = 0, failed = 0, max_active_seen = 0, ticks = 0;
   double busy_s = 0;
@@ -197,14 +211,20 @@ struct nrg_server {
     const double s = double(j.bath.states) * double(j.nkeep);
     return coef * double(j.nsites) * s * s;
   }
-  void loop();
+  void loop(Worker &w);
   void tick(std::vector<std::shared_ptr<Job>> &act);
+  void backward(std::vector<Job *> &fin);
   void finish(Job &j, int status, const std::string &msg);
 };
 
 void nrg_server::finish(Job &j, int status, const std::string &msg) {
   j.release_device();
   std::lock_guard<std::mutex> lk(mu);
+  if (j.admitted) {
+    j.admitted = false;
+    --n_active;
+    reserved -= j.estimate;
+  }
   j.status = status;
   j.message = msg;
   j.t_finish = Clock::now();
@@ -221,8 +241,10 @@ void nrg_server::finish(Job &j, int status, const std::string &msg) {
   cv_done.notify_all();
 }
 
-void nrg_server::loop() {
+void nrg_server::loop(Worker &w) {
   cudaSetDevice(device);  // the runtime's current device is per host thread
+  std::vector<std::shared_ptr<Job>> &active = w.active;
+  const uint64_t nworkers = workers.size();
   for (;;) {
     std::vector<std::shared_ptr<Job>> admitted;
     {
@@ -232,31 +254,31 @@ void nrg_server::loop() {
         cv_work.wait_for(lk, std::chrono::milliseconds(50));
         continue;
       }
-      double reserved = 0;
-      for (auto &a : active) reserved += a->estimate;
-      while (!queue.empty() && int(active.size() + admitted.size()) < max_active) {
+      // even share of the active and queued runs over the workers
+      const uint64_t share = (n_active + queue.size() + nworkers - 1) / nworkers;
+      const uint64_t cap = std::min<uint64_t>(uint64_t(max_active), std::max<uint64_t>(share, 1));
+      while (!queue.empty() && active.size() + admitted.size() < cap) {
         auto &q = queue.front();
         const double est = estimate(*q);
-        const bool idle = active.empty() && admitted.empty();
+        const bool idle = n_active == 0;
         if (budget && !idle && reserved + est > double(budget)) break;
         q->estimate = est;
         q->t_admit = Clock::now();
+        q->admitted = true;
         reserved += est;
+        ++n_active;
         admitted.push_back(q);
         queue.pop_front();
       }
+      max_active_seen = std::max<uint64_t>(max_active_seen, n_active);
     }
     for (auto &j : admitted) {
       try {
-        check(nrg_run_create(eng, &j->imp.desc, &j->bath.desc, j->nkeep, &j->run), "run create");
+        check(nrg_run_create(w.eng, &j->imp.desc, &j->bath.desc, j->nkeep, &j->run), "run create");
         active.push_back(j);
       } catch (const ServeError &x) {
         finish(*j, x.code, x.msg);
       }
-    }
-    {
-      std::lock_guard<std::mutex> lk(mu);
-      max_active_seen = std::max<uint64_t>(max_active_seen, active.size());
     }
     if (active.empty()) continue;
     const auto t0 = Clock::now();
@@ -266,16 +288,20 @@ void nrg_server::loop() {
     busy_s += seconds(t0, t1);
     ++ticks;
   }
-  // stopped: fail what is still queued or running
+  // stopped: fail what this worker still runs; the queue is failed by the
+  // server once every worker has stopped
   for (auto &j : active)
     if (!j->done) finish(*j, NRG_E_STATE, "server stopped");
+}
+
+static void fail_queue(nrg_server *s) {
   std::vector<std::shared_ptr<Job>> rest;
   {
-    std::lock_guard<std::mutex> lk(mu);
-    rest.assign(queue.begin(), queue.end());
-    queue.clear();
+    std::lock_guard<std::mutex> lk(s->mu);
+    rest.assign(s->queue.begin(), s->queue.end());
+    s->queue.clear();
   }
-  for (auto &j : rest) finish(*j, NRG_E_STATE, "server stopped");
+  for (auto &j : rest) s->finish(*j, NRG_E_STATE, "server stopped");
 }
 
 void nrg_server::tick(std::vector<std::shared_ptr<Job>> &act) {
@@ -306,11 +332,30 @@ void nrg_server::tick(std::vector<std::shared_ptr<Job>> &act) {
       runs.clear();
       for (Job *j : js) runs.push_back(j->run);
     }
-    std::vector<Job *> stepped;
+    // tracked operators of all runs of the group in one batched update
+    std::vector<Job *> with_ops;
     for (Job *j : js) {
       try {
         if (j->has_ops && j->site == 0) check(nrg_opset_create(j->run, &j->ops.desc, &j->opset), "opset");
-        if (j->opset) check(nrg_opset_update(j->opset), "opset update");
+        if (j->opset) with_ops.push_back(j);
+      } catch (const ServeError &x) {
+        finish(*j, x.code, x.msg);
+      }
+    }
+    if (!with_ops.empty()) {
+      std::vector<nrg_opset *> os;
+      for (Job *j : with_ops) os.push_back(j->opset);
+      if (nrg_opset_update_batch(os.data(), int(os.size())) != NRG_OK) {
+        for (Job *j : with_ops) {  // isolate the failing run(s)
+          const int r1 = nrg_opset_update(j->opset);
+          if (r1 != NRG_OK) finish(*j, r1, std::string("opset update: ") + nrg_last_error());
+        }
+      }
+    }
+    std::vector<Job *> stepped;
+    for (Job *j : js) {
+      if (j->done) continue;
+      try {
         if ((j->fdm || !j->temps.empty()) && j->site >= j->first_shell_site) {
           int disc = 0;
           check(nrg_run_check_discarded(j->run, &disc), "check discarded");
@@ -356,48 +401,112 @@ void nrg_server::tick(std::vector<std::shared_ptr<Job>> &act) {
     }
   }
   // ---- backward passes of the runs that finished their last site
-  for (auto &jp : act) {
-    Job &j = *jp;
-    if (j.done || j.site < j.nsites) continue;
+  std::vector<Job *> fin;
+  for (auto &jp : act)
+    if (!jp->done && jp->site >= jp->nsites) fin.push_back(jp.get());
+  if (!fin.empty()) backward(fin);
+  act.erase(std::remove_if(act.begin(), act.end(), [](const std::shared_ptr<Job> &j) { return j->done; }),
+            act.end());
+}
+
+// Backward passes of the runs in `fin`, shell by shell from each run's last
+// shell: step r loads the r-th last snapshot of every run that has one and
+// bins the FDM shells of all of them in one nrg_fdm_calc_batch (a run's
+// shells stay in the reference's order; the runs only share launches).
+void nrg_server::backward(std::vector<Job *> &fin) {
+  struct Pass {
+    Job *j;
     nrg_fdm *f = nullptr;
     nrg_thermo *th = nullptr;
+  };
+  std::vector<Pass> ps;
+  for (Job *j : fin) {
+    Pass p{j};
+    try {
+      const int nops = j->has_ops ? j->ops.desc.nops : 0;
+      if (j->fdm) check(nrg_fdm_create(j->run, nops, &p.f), "fdm create");
+      if (!j->temps.empty())
+        check(nrg_thermo_create(j->run, j->temps.data(), int(j->temps.size()), &p.th), "thermo create");
+      ps.push_back(p);
+    } catch (const ServeError &x) {
+      if (p.f) nrg_fdm_destroy(p.f);
+      if (p.th) nrg_thermo_destroy(p.th);
+      finish(*j, x.code, x.msg);
+    }
+  }
+  auto fail = [&](Pass &p, const ServeError &x) {
+    if (p.f) nrg_fdm_destroy(p.f);
+    if (p.th) nrg_thermo_destroy(p.th);
+    p.f = nullptr;
+    p.th = nullptr;
+    finish(*p.j, x.code, x.msg);
+  };
+  size_t depth = 0;
+  for (auto &p : ps) depth = std::max(depth, p.j->shells.size());
+  for (size_t r = 0; r < depth; ++r) {
+    std::vector<Pass *> step;
+    for (auto &p : ps) {
+      if (p.j->done || r >= p.j->shells.size()) continue;
+      try {
+        check(nrg_run_load_snapshot(p.j->run, p.j->shells[p.j->shells.size() - 1 - r].iteration), "load snapshot");
+        step.push_back(&p);
+      } catch (const ServeError &x) {
+        fail(p, x);
+      }
+    }
+    std::vector<nrg_fdm *> fs;
+    std::vector<double> sc;
+    for (Pass *p : step) {
+      if (!p->f) continue;
+      fs.push_back(p->f);
+      sc.push_back(p->j->shell_scale[p->j->shells[p->j->shells.size() - 1 - r].site]);
+    }
+    if (!fs.empty() && nrg_fdm_calc_batch(fs.data(), int(fs.size()), sc.data()) != NRG_OK) {
+      for (Pass *p : step) {  // isolate the failing run(s)
+        if (!p->f) continue;
+        const int r1 = nrg_fdm_calc(p->f, p->j->shell_scale[p->j->shells[p->j->shells.size() - 1 - r].site]);
+        if (r1 != NRG_OK) fail(*p, ServeError{r1, std::string("fdm calc: ") + nrg_last_error()});
+      }
+    }
+    for (Pass *p : step) {
+      if (p->j->done || !p->th) continue;
+      try {
+        check(nrg_thermo_calc(p->th, p->j->shell_scale[p->j->shells[p->j->shells.size() - 1 - r].site]),
+              "thermo calc");
+      } catch (const ServeError &x) {
+        fail(*p, x);
+      }
+    }
+  }
+  for (auto &p : ps) {
+    Job &j = *p.j;
+    if (j.done) continue;
     try {
       const int nops = j.has_ops ? j.ops.desc.nops : 0;
-      if (j.fdm) check(nrg_fdm_create(j.run, nops, &f), "fdm create");
-      if (!j.temps.empty())
-        check(nrg_thermo_create(j.run, j.temps.data(), int(j.temps.size()), &th), "thermo create");
-      for (auto it = j.shells.rbegin(); it != j.shells.rend(); ++it) {
-        check(nrg_run_load_snapshot(j.run, it->iteration), "load snapshot");
-        const double scale = j.shell_scale[it->site];
-        if (f) check(nrg_fdm_calc(f, scale), "fdm calc");
-        if (th) check(nrg_thermo_calc(th, scale), "thermo calc");
-      }
-      if (f) {
+      if (p.f) {
         j.energy_points.assign(kFdmPoints, 0.0);
         j.positive.assign(size_t(nops) * kFdmPoints, 0.0);
         j.negative.assign(size_t(nops) * kFdmPoints, 0.0);
-        check(nrg_fdm_get(f, j.energy_points.data(), j.positive.data(), j.negative.data(), kFdmPoints),
+        check(nrg_fdm_get(p.f, j.energy_points.data(), j.positive.data(), j.negative.data(), kFdmPoints),
               "fdm get");
       }
-      if (th) {
+      if (p.th) {
         j.entropy.assign(j.temps.size(), 0.0);
         j.cv.assign(j.temps.size(), 0.0);
-        check(nrg_thermo_final(th, j.entropy.data(), j.cv.data()), "thermo final");
+        check(nrg_thermo_final(p.th, j.entropy.data(), j.cv.data()), "thermo final");
       }
       nrg_run_info info{};
       check(nrg_run_get_info(j.run, &info), "info");
       j.peak_bytes = std::max<int64_t>(j.peak_bytes, info.device_bytes);
-      if (f) nrg_fdm_destroy(f);
-      if (th) nrg_thermo_destroy(th);
+      if (p.f) nrg_fdm_destroy(p.f);
+      if (p.th) nrg_thermo_destroy(p.th);
+      p.f = nullptr;
+      p.th = nullptr;
       finish(j, NRG_OK, "");
     } catch (const ServeError &x) {
-      if (f) nrg_fdm_destroy(f);
-      if (th) nrg_thermo_destroy(th);
-      finish(j, x.code, x.msg);
+      fail(p, x);
     }
   }
-  act.erase(std::remove_if(act.begin(), act.end(), [](const std::shared_ptr<Job> &j) { return j->done; }),
-            act.end());
 }
 
 namespace {
@@ -427,15 +536,37 @@ int nrg_server_create(nrg_engine *eng, const nrg_server_opts *opts, nrg_server *
   return sguard([&] {
     if (!eng || !out) throw ServeError{NRG_E_ARG, "null argument"};
     auto s = std::make_unique<nrg_server>();
-    s->eng = eng;
     if (cudaGetDevice(&s->device) != cudaSuccess) throw ServeError{NRG_E_NOCUDA, "no current CUDA device"};
+    int nworkers = 1;
     if (opts) {
       if (opts->max_active < 1) throw ServeError{NRG_E_ARG, "max_active must be >= 1"};
+      if (opts->workers < 0 || opts->workers > 64) throw ServeError{NRG_E_ARG, "workers must be in [0, 64]"};
       s->max_active = opts->max_active;
       s->budget = opts->hbm_budget_bytes;
+      nworkers = std::max(1, opts->workers);
+    }
+    nrg_engine_opts eo{};
+    check(nrg_engine_get_opts(eng, &eo), "engine options");
+    for (int k = 0; k < nworkers; ++k) {
+      auto w = std::make_unique<Worker>();
+      w->eng = eng;
+      if (k > 0) {
+        const int rc = nrg_engine_create(&eo, &w->eng);
+        if (rc != NRG_OK) {
+          const std::string msg = nrg_last_error();
+          for (auto &o : s->workers)
+            if (o->owns_engine) nrg_engine_destroy(o->eng);
+          throw ServeError{rc, "worker engine: " + msg};
+        }
+        w->owns_engine = true;
+      }
+      s->workers.push_back(std::move(w));
     }
     nrg_server *raw = s.get();
-    s->worker = std::thread([raw] { raw->loop(); });
+    for (auto &w : s->workers) {
+      Worker *wp = w.get();
+      w->th = std::thread([raw, wp] { raw->loop(*wp); });
+    }
     *out = s.release();
   });
 }
@@ -448,7 +579,11 @@ int nrg_server_destroy(nrg_server *s) {
       s->stop = true;
     }
     s->cv_work.notify_all();
-    if (s->worker.joinable()) s->worker.join();
+    for (auto &w : s->workers)
+      if (w->th.joinable()) w->th.join();
+    fail_queue(s);
+    for (auto &w : s->workers)
+      if (w->owns_engine) nrg_engine_destroy(w->eng);
     delete s;
   });
 }

@@ -156,3 +156,28 @@ def test_bad_requests_fail_alone():
     assert math.isfinite(srv.result(good)["entropy"][0])
     srv.close()
     eng.close()
+
+
+def test_workers_give_the_same_results():
+    """Three workers (three engines and host threads) serving a burst: every
+    run equals the same run served alone, whichever engine stepped it."""
+    eng = api.Engine(api.PREC_MIXED)
+    srv = api.Server(eng, max_active=1)
+    rid = srv.submit(**_req())
+    assert srv.wait(rid)
+    alone = srv.result(rid)
+    srv.close()
+
+    srv = api.Server(eng, max_active=2, workers=3)
+    ids = [srv.submit(**_req()) for _ in range(5)]
+    ids += [srv.submit(**_req(eps=-0.3, U=0.6, nsites=10))]
+    for i in ids[:5]:
+        assert srv.wait(i)
+        _same(srv.result(i), alone)
+    assert srv.wait(ids[5])
+    assert np.isfinite(srv.result(ids[5])["entropy"]).all()
+    st = srv.stats()
+    srv.close()
+    eng.close()
+    assert st["completed"] == 6 and st["failed"] == 0
+    assert st["max_active_seen"] > 2  # more runs active than one worker may hold

@@ -189,12 +189,9 @@ __device__ __forceinline__ void cp_async16(void *dst, const void *src, bool vali
 __device__ __forceinline__ void cp_async16_k(void *dst, const void *src, int nvalid) {
   const uint32_t d = smem_u32(dst);
   const int sz = nvalid <= 0 ? 0 : (nvalid >= 8 ? 16 : 2 * nvalid);
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 16, %2;\n" ::"r"(d), "l"(src), "r"(sz));
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(d), "l"(src), "r"(sz));
 }
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
-template <int N> __device__ __forceinline__ void cp_async_wait() {
-  asm volatile("cp.async.wait_group %0;\n" ::"n"(N));
-}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
 constexpr int TM = 128, TN = 64, TK = 16;  // output tile, k-step (one MMA)
 constexpr int kStages = 4;
@@ -203,7 +200,6 @@ constexpr int kATile = TM * TK * 2, kBTile = TN * TK * 2;  // bytes per plane
 constexpr int kStageBytes = kPlanes * (kATile + kBTile);   // 48 KB
 constexpr uint32_t kLBO = 128, kSBO = 256;                 // core-matrix strides (K = 16)
 constexpr int kWaitLimit = 1 << 24;                        // bounded mbarrier polls
-constexpr int kLag = 1;            // producer copy groups in flight before a hand-over
 
 // byte offset of the 16-byte core-matrix row holding element (r, k) of an
 // R x 16 operand tile: K-major rows are 8 consecutive k, MN-major rows are
@@ -286,9 +282,6 @@ struct StepIt {
   }
 };
 
-__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
-  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
-}
 __device__ __forceinline__ void mma_commit(uint32_t bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
 }
@@ -351,18 +344,12 @@ k_gemm_oz(const GemmTile *__restrict__ tiles, const OzGroup *__restrict__ groups
       if (abort_flag) break;
       const OzContrib &q = contribs[it.c];
       stage_step(q, g.M, g.N, m0, n0, it.k0, q.K, ring + st * kStageBytes, tp, P);
-      cp_async_commit();
+      // full[st] receives this thread's arrival when its copies so far have
+      // landed; the producer moves on to the next stage without waiting
+      asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(smem_u32(&full[st])) : "memory");
       it.next(g, contribs);
-      if (s >= kLag) {  // the copies of step s - kLag have landed: hand it over
-        cp_async_wait<kLag>();
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        mbar_arrive(smem_u32(&full[(s - kLag) % kStages]));
-      }
     }
-    cp_async_wait<0>();
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    if (!abort_flag)
-      for (int s = (nsteps > kLag ? nsteps - kLag : 0); s < nsteps; ++s) mbar_arrive(smem_u32(&full[s % kStages]));
+    cp_async_wait_all();
   } else {
     // ------------------------------------------------ MMA issue and folds
     StepIt it{g.c0, 0};
@@ -430,9 +417,14 @@ k_gemm_oz(const GemmTile *__restrict__ tiles, const OzGroup *__restrict__ groups
       first_fold = false;
     };
 
+    int scale_c = -1;  // contribution whose scale is in `scale`
+    double scale = 0.0;
     for (int s = 0; s < nsteps; ++s) {
       const OzContrib &q = contribs[it.c];
-      const double scale = fabs(q.alpha) * scalbn(1.0, *q.A.exp + *q.B.exp - 61);
+      if (it.c != scale_c) {
+        scale = fabs(q.alpha) * scalbn(1.0, *q.A.exp + *q.B.exp - 61);
+        scale_c = it.c;
+      }
       if (kacc > 0 && (scale != acc_scale || kacc + TK > kChunkK)) fold();
       acc_scale = scale;
       if (tid == 0 && !abort_flag) {
@@ -440,6 +432,9 @@ k_gemm_oz(const GemmTile *__restrict__ tiles, const OzGroup *__restrict__ groups
         if (!mbar_wait(smem_u32(&full[st]), uint32_t((s / kStages) & 1))) {
           abort_flag = 1;
         } else {
+          // the stage's cp.async writes (generic proxy) are visible to this
+          // thread; order them before the MMAs' async-proxy reads
+          asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
           asm volatile("tcgen05.fence::after_thread_sync;");
           const bool ta = q.trans & 1, tb = (q.trans >> 1) & 1;
           const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | (uint32_t(q.alpha < 0.0) << 13) |

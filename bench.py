@@ -332,9 +332,9 @@ def kernel_models():
     }
 
 
-# DRAM bytes (read + write) per launch measured with ncu on the full bench
-# step (mean over 1500 launches; summary and command under profiles/)
-MEASURED_TRAFFIC = {"k_gemm_oz": 449.2e6}
+# DRAM bytes (read + write) per launch measured with ncu on one engine's full
+# 8-run step (mean over its 869 launches; summary and command under profiles/)
+MEASURED_TRAFFIC = {"k_gemm_oz": 220.3e6}
 
 
 def kernel_profile(engine):

@@ -12,6 +12,8 @@
 // Empty sectors (no kept states) stay in the API-level sector lists exactly as
 // the reference keeps them, but never reach the device.
 #include <algorithm>
+#include <map>
+#include <tuple>
 #include <unordered_map>
 #include <cmath>
 #include <cstring>
@@ -534,14 +536,38 @@ void OzList::out(double *C, int ldc, int M, int N, bool acc, const std::vector<O
 
 void OzList::launch(nrg_engine *e, std::vector<DevPtr> &hold) {
   if (tiles.empty()) return;
+  // one TMA tensor map per distinct operand view (a view is shared by the
+  // products of many groups: the same U block, the same X)
+  std::vector<OzTensorMap> maps;
+  std::map<std::tuple<const void *, int, int, int, int64_t, int>, int> seen;
+  auto map_of = [&](const OzOperand &o, int inner, int outer, int box_outer) {
+    const auto key = std::make_tuple(static_cast<const void *>(o.p), inner, outer, o.ld, o.pstride, box_outer);
+    auto it = seen.find(key);
+    if (it != seen.end()) return it->second;
+    OzTensorMap m;
+    if (!encode_oz_map(&m, o, inner, outer, planes, box_outer))
+      fail(NRG_E_CUDA, "TMA tensor map of a digit-plane operand rejected");
+    maps.push_back(m);
+    seen.emplace(key, int(maps.size()) - 1);
+    return int(maps.size()) - 1;
+  };
+  for (const OzGroup &g : groups)
+    for (int c = g.c0; c < g.c1; ++c) {
+      OzContrib &q = contribs[c];
+      q.tmA = q.tmB = -1;
+      if (q.K <= 0) continue;
+      const bool ta = q.trans & 1, tb = (q.trans >> 1) & 1;
+      q.tmA = ta ? map_of(q.A, g.M, q.K, 16) : map_of(q.A, q.K, g.M, OZ_TILE_M);
+      q.tmB = tb ? map_of(q.B, q.K, g.N, OZ_TILE_N) : map_of(q.B, g.N, q.K, 16);
+    }
   Arena a;
-  size_t ot = a.add(tiles), og = a.add(groups), oc = a.add(contribs);
+  size_t ot = a.add(tiles), og = a.add(groups), oc = a.add(contribs), om = a.add(maps);
   DevPtr d;
   char *p = a.push(e, d);
   hold.push_back(d);
   Prof pf(e, "k_gemm_oz", flops);
-  launch_gemm_oz(at<GemmTile>(p, ot), int(tiles.size()), at<OzGroup>(p, og), at<OzContrib>(p, oc), e->d_kerr,
-                 e->stream);
+  launch_gemm_oz(at<GemmTile>(p, ot), int(tiles.size()), at<OzGroup>(p, og), at<OzContrib>(p, oc),
+                 at<OzTensorMap>(p, om), e->d_kerr, e->stream);
   count_launch(e);
   post_launch("ozaki gemm");
 }

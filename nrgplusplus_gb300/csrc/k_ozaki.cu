@@ -16,16 +16,19 @@
 // one CTA owns a 128 x 64 output tile, the eight group sums live in tensor
 // memory (TMEM: 8 accumulators x 64 FP32 columns = all 512 columns, lane =
 // output row), and one thread issues tcgen05.mma (kind::f16, bf16 inputs,
-// FP32 accumulation, M = 128, N = 64, K = 16) on operand tiles that all
-// threads stage in shared memory with 16-byte cp.async copies in the
-// canonical no-swizzle core-matrix layouts (K-major or MN-major per operand,
-// so transposed operands need no transpose).  A four-stage ring overlaps the
-// copies of later k-steps with the MMAs of the current one; tcgen05.commit
-// arrives on one mbarrier per stage when its MMAs are done.  The group sums
+// FP32 accumulation, M = 128, N = 64, K = 16) on operand tiles that one
+// producer thread stages in shared memory with TMA tensor copies
+// (cp.async.bulk.tensor, one tensor map per operand view, encoded on the
+// host) whose boxes land directly in the canonical no-swizzle core-matrix
+// layouts (K-major or MN-major per operand, so transposed operands need no
+// transpose).  A four-stage ring overlaps the copies of later k-steps with
+// the MMAs of the current one; tcgen05.commit arrives on one mbarrier per
+// stage when its MMAs are done.  The group sums
 // are folded into the FP64 output once per run of contributions that share a
 // scale (at most 512 deep): tcgen05.ld to registers, integer Horner over the
 // groups, one FP64 fma per element.  Every mbarrier wait is bounded; a wait
 // that runs out sets *err, and the kernel drains and releases TMEM.
+#include <cuda.h>
 #include <cuda_bf16.h>
 
 #include "nrg_internal.h"
@@ -178,39 +181,38 @@ k_split_digits(const SplitTask *__restrict__ tasks, const int64_t *__restrict__ 
 }
 
 // ----------------------------------------------------------------- GEMM
-__device__ __forceinline__ void cp_async16(void *dst, const void *src, bool valid) {
-  const uint32_t d = smem_u32(dst);
-  const int sz = valid ? 16 : 0;  // 0: no bytes read, 16 zero bytes written
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(d), "l"(src), "r"(sz));
-}
-// 8-element vector along k whose tail may run past kend (sub-matrix views
-// whose rows continue with real data): copy the first `nvalid` elements,
-// zero the rest.  cp.async src-size is in bytes (2 per element).
-__device__ __forceinline__ void cp_async16_k(void *dst, const void *src, int nvalid) {
-  const uint32_t d = smem_u32(dst);
-  const int sz = nvalid <= 0 ? 0 : (nvalid >= 8 ? 16 : 2 * nvalid);
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(d), "l"(src), "r"(sz));
-}
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
-
 constexpr int TM = 128, TN = 64, TK = 16;  // output tile, k-step (one MMA)
 constexpr int kStages = 4;
-constexpr int kTcThreads = 384;  // 4 consumer warps + 8 producer warps
+constexpr int kTcThreads = 160;  // 4 consumer warps + 1 producer warp (one issuing thread)
 constexpr int kATile = TM * TK * 2, kBTile = TN * TK * 2;  // bytes per plane
+constexpr int kAStage = kPlanes * kATile;                  // 32 KB
 constexpr int kStageBytes = kPlanes * (kATile + kBTile);   // 48 KB
-constexpr uint32_t kLBO = 128, kSBO = 256;                 // core-matrix strides (K = 16)
+constexpr int kOctetBox = kPlanes * TK * 16;               // 2 KB: 8 planes x 16 k x 8 elements
 constexpr int kWaitLimit = 1 << 24;                        // bounded mbarrier polls
 
-// byte offset of the 16-byte core-matrix row holding element (r, k) of an
-// R x 16 operand tile: K-major rows are 8 consecutive k, MN-major rows are
-// 8 consecutive r (r, k multiples of 8 at the row start)
-__device__ __forceinline__ uint32_t tile_off(int r, int k, bool kmajor) {
-  return uint32_t(r >> 3) * kSBO + uint32_t(k >> 3) * kLBO + (kmajor ? uint32_t(r & 7) * 16 : uint32_t(k & 7) * 16);
+// Stage layouts.  Every operand tile of a stage is written by TMA boxes (no
+// swizzle) straight into canonical core-matrix layouts (8 rows of 16 bytes
+// each, contiguous):
+//   K-major (rows of k):  two boxes {8 k, R rows, 8 planes}, one per k-half:
+//     [k-half][plane][row][8 k]; plane p at p * R * 16, row groups 128 bytes
+//     apart (SBO), k-halves R * 16 * 8 bytes apart (LBO);
+//   MN-major (rows of m or n): R / 8 boxes {8 m, 16 k, 8 planes}, one per
+//     m-octet: [octet][plane][k][8 m]; plane p at p * 256, k-groups 128
+//     bytes apart (LBO), octets 2 KB apart (SBO).
+// The boxes of a stage always total kStageBytes (rows, k and planes beyond
+// the operand view are zero-filled by the TMA unit), which the producer
+// announces with one expect_tx on the stage's full barrier.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+  return uint64_t((addr >> 4) & 0x3FFF) | (uint64_t((lbo >> 4) & 0x3FFF) << 16) |
+         (uint64_t((sbo >> 4) & 0x3FFF) << 32) | (uint64_t(1) << 46);  // version 1; no swizzle
 }
 
-__device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
-  return uint64_t((addr >> 4) & 0x3FFF) | (uint64_t(kLBO >> 4) << 16) | (uint64_t(kSBO >> 4) << 32) |
-         (uint64_t(1) << 46);  // descriptor version; base offset 0; no swizzle
+__device__ __forceinline__ void tma_load_3d(uint32_t dst, const OzTensorMap *map, int x, int y, int z, uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(bar)
+      : "memory");
 }
 
 __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
@@ -225,46 +227,26 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
   return false;
 }
 
-// Stage the k-step [k0, k0 + 16) of all 8 planes of op(A) (128 x 16) and
-// op(B) (64 x 16): 3072 rows of 16 bytes over 256 producer threads (tp =
-// 0..255): per plane one A row each, one B row for tp < 128.  (Eight
-// producer warps issue the copies about 8 % faster than four; twelve are
-// slower again.)
-__device__ __forceinline__ void stage_step(const OzContrib &q, int M, int N, int m0, int n0, int k0, int kend,
-                                           unsigned char *st, int tp, int P) {
+// The boxes of the k-step [k0, k0 + 16) of all 8 planes of op(A) (128 x 16)
+// and op(B) (64 x 16) into stage `st` (shared address), completing on `bar`.
+// x coordinates (k0, k0 + 8, m0 + 8 o, n0 + 8 o) are multiples of 8
+// elements: 16-byte aligned, as TMA requires.
+__device__ __forceinline__ void stage_tma(const OzContrib &q, const OzTensorMap *maps, int m0, int n0, int k0,
+                                          uint32_t st, uint32_t bar) {
   const bool ta = q.trans & 1, tb = (q.trans >> 1) & 1;
-#pragma unroll 2
-  for (int p = 0; p < P; ++p) {
-    unsigned char *As = st + p * kATile;
-    unsigned char *Bs = st + kPlanes * kATile + p * kBTile;
-    const __nv_bfloat16 *a = q.A.p + int64_t(p) * q.A.pstride;
-    const __nv_bfloat16 *b = q.B.p + int64_t(p) * q.B.pstride;
-    {  // A: 256 rows
-      const int r = tp;
-      if (!ta) {  // stored [m][k]: 128 m x 2 k-halves
-        const int m = r >> 1, kh = (r & 1) * 8;
-        const int gm = m0 + m, gk = k0 + kh;
-        const bool ok = gm < M && gk < kend;
-        cp_async16_k(As + tile_off(m, kh, true), ok ? a + int64_t(gm) * q.A.ld + gk : a, ok ? kend - gk : 0);
-      } else {    // stored [k][m]: 16 k x 16 m-octets
-        const int k = r >> 4, mo = (r & 15) * 8;
-        const int gk = k0 + k, gm = m0 + mo;
-        const bool ok = gk < kend && gm < M;
-        cp_async16(As + tile_off(mo, k, false), ok ? a + int64_t(gk) * q.A.ld + gm : a, ok);
-      }
-    }
-    if (tp >= 128) continue;
-    if (tb) {   // B stored [n][k]: 64 n x 2 k-halves
-      const int n = tp >> 1, kh = (tp & 1) * 8;
-      const int gn = n0 + n, gk = k0 + kh;
-      const bool ok = gn < N && gk < kend;
-      cp_async16_k(Bs + tile_off(n, kh, true), ok ? b + int64_t(gn) * q.B.ld + gk : b, ok ? kend - gk : 0);
-    } else {    // stored [k][n]: 16 k x 8 n-octets
-      const int k = tp >> 3, no = (tp & 7) * 8;
-      const int gk = k0 + k, gn = n0 + no;
-      const bool ok = gk < kend && gn < N;
-      cp_async16(Bs + tile_off(no, k, false), ok ? b + int64_t(gk) * q.B.ld + gn : b, ok);
-    }
+  const OzTensorMap *ma = maps + q.tmA, *mb = maps + q.tmB;
+  if (!ta) {
+    tma_load_3d(st, ma, k0, m0, 0, bar);
+    tma_load_3d(st + kAStage / 2, ma, k0 + 8, m0, 0, bar);
+  } else {
+    for (int o = 0; o < TM / 8; ++o) tma_load_3d(st + o * kOctetBox, ma, m0 + 8 * o, k0, 0, bar);
+  }
+  const uint32_t sb = st + kAStage;
+  if (tb) {
+    tma_load_3d(sb, mb, k0, n0, 0, bar);
+    tma_load_3d(sb + (kStageBytes - kAStage) / 2, mb, k0 + 8, n0, 0, bar);
+  } else {
+    for (int o = 0; o < TN / 8; ++o) tma_load_3d(sb + o * kOctetBox, mb, n0 + 8 * o, k0, 0, bar);
   }
 }
 
@@ -291,16 +273,16 @@ __device__ __forceinline__ void consumer_sync() {  // warps 0-3 only
   asm volatile("bar.sync 1, 128;" ::: "memory");
 }
 
-// Warp roles: warps 4-11 stage k-steps into a ring of kStages buffers (a
-// stage is released by the tcgen05.commit of its MMAs on empty[stage] and
-// handed over on full[stage] once its copies have landed); warp 0 lane 0
-// issues the 36 MMAs of each step; warps 0-3 (the 128 TMEM lanes) fold the
+// Warp roles: warp 4 lane 0 stages k-steps into a ring of kStages buffers
+// with TMA boxes (a stage is released by the tcgen05.commit of its MMAs on
+// empty[stage] and completes on full[stage] when its bytes have landed);
+// warp 0 lane 0 issues the 36 MMAs of each step; warps 0-3 (the 128 TMEM lanes) fold the
 // group sums whenever the scale changes, 512 k-terms are used up, or the
 // list ends (after a drain commit on `drain`).  No CTA-wide barrier sits in
 // the k-loop.
 __global__ void __launch_bounds__(kTcThreads, 1)
 k_gemm_oz(const GemmTile *__restrict__ tiles, const OzGroup *__restrict__ groups,
-          const OzContrib *__restrict__ contribs, int *err) {
+          const OzContrib *__restrict__ contribs, const OzTensorMap *__restrict__ maps, int *err) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   __shared__ __align__(8) uint64_t full[kStages], empty[kStages], drain;
   __shared__ uint32_t tmem_slot;
@@ -319,7 +301,7 @@ k_gemm_oz(const GemmTile *__restrict__ tiles, const OzGroup *__restrict__ groups
   }
   if (tid == 0) {
     for (int i = 0; i < kStages; ++i) {
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], 256;" ::"r"(smem_u32(&full[i])));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&full[i])));
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&empty[i])));
     }
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&drain)));
@@ -336,22 +318,34 @@ k_gemm_oz(const GemmTile *__restrict__ tiles, const OzGroup *__restrict__ groups
     if (contribs[c].K > 0) nsteps += (contribs[c].K + TK - 1) / TK;
 
   if (warp >= 4) {
-    // ------------------------------------------------------------ producers
-    const int tp = tid - 128;
-    StepIt it{g.c0, 0};
-    it.skip_empty(g, contribs);
-    for (int s = 0; s < nsteps; ++s) {
-      const int st = s % kStages, use = s / kStages;
-      if (use > 0 && !mbar_wait(smem_u32(&empty[st]), uint32_t((use - 1) & 1))) abort_flag = 1;
-      if (abort_flag) break;
-      const OzContrib &q = contribs[it.c];
-      stage_step(q, g.M, g.N, m0, n0, it.k0, q.K, ring + st * kStageBytes, tp, P);
-      // full[st] receives this thread's arrival when its copies so far have
-      // landed; the producer moves on to the next stage without waiting
-      asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(smem_u32(&full[st])) : "memory");
-      it.next(g, contribs);
+    // ------------------------------------------------------------- producer
+    if (warp == 4 && lane == 0) {
+      StepIt it{g.c0, 0};
+      it.skip_empty(g, contribs);
+      int issued = 0, cur = -1;
+      const uint32_t ring0 = smem_u32(ring);
+      for (int s = 0; s < nsteps; ++s) {
+        const int st = s % kStages, use = s / kStages;
+        if (use > 0 && !mbar_wait(smem_u32(&empty[st]), uint32_t((use - 1) & 1))) abort_flag = 1;
+        if (abort_flag) break;
+        const OzContrib &q = contribs[it.c];
+        if (it.c != cur) {  // the tensor maps were written by a copy before the launch
+          asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(maps + q.tmA) : "memory");
+          asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(maps + q.tmB) : "memory");
+          cur = it.c;
+        }
+        const uint32_t fb = smem_u32(&full[st]);
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(fb), "r"(kStageBytes)
+                     : "memory");
+        stage_tma(q, maps, m0, n0, it.k0, ring0 + uint32_t(st * kStageBytes), fb);
+        ++issued;
+        it.next(g, contribs);
+      }
+      // no TMA write may be in flight when the CTA ends (after an abort the
+      // consumer stops waiting for the stages)
+      for (int s = (issued > kStages ? issued - kStages : 0); s < issued; ++s)
+        mbar_wait(smem_u32(&full[s % kStages]), uint32_t((s / kStages) & 1));
     }
-    cp_async_wait_all();
   } else {
     // ------------------------------------------------ MMA issue and folds
     StepIt it{g.c0, 0};
@@ -360,7 +354,7 @@ k_gemm_oz(const GemmTile *__restrict__ tiles, const OzGroup *__restrict__ groups
     double acc_scale = 0;
     bool first_fold = true;
     uint32_t drain_phase = 0;
-    const uint64_t d0 = smem_desc(smem_u32(ring));
+    const uint32_t ring0 = smem_u32(ring);
     const uint32_t tl = tmem + (uint32_t(32 * warp) << 16);
     const int gm = m0 + 32 * warp + lane;
 
@@ -434,23 +428,25 @@ k_gemm_oz(const GemmTile *__restrict__ tiles, const OzGroup *__restrict__ groups
         if (!mbar_wait(smem_u32(&full[st]), uint32_t((s / kStages) & 1))) {
           abort_flag = 1;
         } else {
-          // the stage's cp.async writes (generic proxy) are visible to this
-          // thread; order them before the MMAs' async-proxy reads
-          asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
           asm volatile("tcgen05.fence::after_thread_sync;");
           const bool ta = q.trans & 1, tb = (q.trans >> 1) & 1;
           const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | (uint32_t(q.alpha < 0.0) << 13) |
                                  (uint32_t(ta) << 15) | (uint32_t(!tb) << 16) | (uint32_t(TN >> 3) << 17) |
                                  (uint32_t(TM >> 4) << 24);
-          const uint64_t ds = d0 + uint64_t((st * kStageBytes) >> 4);
+          const uint32_t sa = ring0 + uint32_t(st * kStageBytes), sb = sa + kAStage;
+          // plane p of A at a0 + p * astep, plane q of B at b0 + q * bstep
+          // (the stage layouts above)
+          const uint64_t a0 = ta ? smem_desc(sa, 128, kOctetBox) : smem_desc(sa, kAStage / 2, 128);
+          const uint64_t b0 = tb ? smem_desc(sb, (kStageBytes - kAStage) / 2, 128) : smem_desc(sb, 128, kOctetBox);
+          const uint32_t astep = ta ? 256 : TM * 16, bstep = tb ? TN * 16 : 256;
           const uint32_t first = kacc == 0 ? 0u : 1u;
 #pragma unroll
           for (int p = 0; p < kPlanes; ++p) {
 #pragma unroll
             for (int qd = 0; qd < kPlanes - p; ++qd) {
               if (p + qd >= P) continue;  // uniform: fewer planes, fewer products
-              const uint64_t ad = ds + uint64_t((p * kATile) >> 4);
-              const uint64_t bd = ds + uint64_t((kPlanes * kATile + qd * kBTile) >> 4);
+              const uint64_t ad = a0 + uint64_t((p * astep) >> 4);
+              const uint64_t bd = b0 + uint64_t((qd * bstep) >> 4);
               const uint32_t acc = p > 0 ? 1u : first;  // the first pair of each group starts it
               asm volatile(
                   "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
@@ -498,13 +494,43 @@ void launch_split_grid(const SplitTask *tasks, const int64_t *chunk0, int ntasks
 }
 
 void launch_gemm_oz(const GemmTile *tiles, int ntiles, const OzGroup *groups, const OzContrib *contribs,
-                    int *err, cudaStream_t s) {
+                    const OzTensorMap *maps, int *err, cudaStream_t s) {
   if (ntiles == 0) return;
   // once per process, thread-safe (engines may launch from several threads)
   static const bool cfg =
       (cudaFuncSetAttribute(k_gemm_oz, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kGemmSmem)), true);
   (void)cfg;
-  k_gemm_oz<<<ntiles, kTcThreads, kGemmSmem, s>>>(tiles, groups, contribs, err);
+  k_gemm_oz<<<ntiles, kTcThreads, kGemmSmem, s>>>(tiles, groups, contribs, maps, err);
+}
+
+bool encode_oz_map(OzTensorMap *out, const OzOperand &o, int inner, int outer, int planes, int box_outer) {
+  using Encode = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                              const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                              CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+  // the driver's encoder, looked up once (the library links the runtime only)
+  static const Encode enc = [] {
+    void *f = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      f = nullptr;
+    return reinterpret_cast<Encode>(f);
+  }();
+  static_assert(sizeof(CUtensorMap) == sizeof(OzTensorMap), "tensor map size");
+  if (!enc || inner <= 0 || outer <= 0 || planes <= 0 || planes > kPlanes) return false;
+  const cuuint64_t strides[2] = {cuuint64_t(o.ld) * 2, cuuint64_t(o.pstride) * 2};
+  const cuuint32_t box[3] = {8, cuuint32_t(box_outer), cuuint32_t(kPlanes)}, es[3] = {1, 1, 1};
+  // planes beyond `planes` are zero-filled (no bytes read) when the driver
+  // takes a box deeper than the tensor; otherwise all 8 (always allocated)
+  for (const int np : {planes, kPlanes}) {
+    const cuuint64_t dims[3] = {cuuint64_t(inner), cuuint64_t(outer), cuuint64_t(np)};
+    if (enc(reinterpret_cast<CUtensorMap *>(out), CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3,
+            const_cast<__nv_bfloat16 *>(o.p), dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+            CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS)
+      return true;
+  }
+  return false;
 }
 
 }  // namespace nrg

@@ -136,7 +136,20 @@ struct OzContrib {
   OzOperand A, B;
   int K, trans;            // trans bit0: A stored K x M; bit1: B stored N x K
   double alpha;
+  int tmA, tmB;            // TMA tensor maps of op(A), op(B) in the launch's map array
+  int pad0, pad1;
 };
+// One TMA tensor map (CUtensorMap: 128 bytes, 64-byte aligned).
+struct alignas(64) OzTensorMap {
+  unsigned char bytes[128];
+};
+// Tensor map of one operand view for k_gemm_oz's stage boxes: a 3-D tensor
+// (inner: the contiguous dimension, `inner` elements; outer: `outer` rows of
+// o.ld elements; planes: `planes` of o.pstride elements), box 8 x box_outer x 8.
+// K-major operands: inner = K, box_outer = 128 (A) or 64 (B); MN-major ones:
+// inner = M or N, outer = K, box_outer = 16.  Returns false if the driver
+// rejects the description.
+bool encode_oz_map(OzTensorMap *out, const OzOperand &o, int inner, int outer, int planes, int box_outer);
 struct OzGroup {
   double *C;
   int ldc, M, N, accumulate;
@@ -153,7 +166,7 @@ void launch_split_grid(const SplitTask *tasks, const int64_t *chunk0, int ntasks
 // wait inside the kernel runs out (the launch then leaves its tile unfinished)
 constexpr int OZ_TILE_M = 128, OZ_TILE_N = 64;
 void launch_gemm_oz(const GemmTile *tiles, int ntiles, const OzGroup *groups, const OzContrib *contribs,
-                    int *err, cudaStream_t s);
+                    const OzTensorMap *maps, int *err, cudaStream_t s);
 
 // ------------------------------------------------------------- truncation
 struct TruncRun {

@@ -1174,11 +1174,11 @@ int nrg_thermo_final(nrg_thermo *t, double *entropy, double *cv) {
     const int nt = int(t->temps.size());
     Staged st;
     size_t of = st.add(flat), oo = st.add(off), og = st.add(gs), ot = st.add(t->temps);
-    std::vector<double> scratch(size_t(2) * nsh * nt + 2 * nt, 0.0);
+    std::vector<double> scratch(size_t(3) * nsh * nt + 2 * nt, 0.0);
     size_t os = st.add(scratch);
     DevPtr hold;
     char *d = st.push(e, hold);
-    double *ent = at<double>(d, os) + size_t(2) * nsh * nt;
+    double *ent = at<double>(d, os) + size_t(3) * nsh * nt;
     launch_thermo(at<double>(d, of), at<int64_t>(d, oo), at<double>(d, og), nsh, at<double>(d, ot), nt,
                   t->bathdim, at<double>(d, os), ent, ent + nt, e->stream);
     engine_count_launch(e, 1);

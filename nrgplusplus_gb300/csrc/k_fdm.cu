@@ -113,58 +113,59 @@ __device__ __forceinline__ double regulate_exp(double x) {  // fdmThermodynamics
   return exp(x);
 }
 
-__device__ double cta_sum(double v, double *red) {
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  __syncthreads();
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
-  __syncthreads();
-  double t = 0.0;
-  for (int i = 0; i < int(blockDim.x >> 5); ++i) t += red[i];
-  __syncthreads();
-  return t;
-}
-
-// One CTA per temperature: partition function, entropy and specific heat from
-// the discarded energies of every shell (fdmThermodynamics::saveFinalData,
+// Partition function, entropy and specific heat from the discarded energies
+// of every shell (fdmThermodynamics::saveFinalData,
 // fdmThermodynamics.hpp:154-226).  disc holds per shell the discarded
 // energies already shifted by the shell minimum; gs the corrected shell
 // ground energies.
+// One CTA per temperature; warp w takes shells w, w + 8, ... and sums, over
+// the shell's discarded states with x = E - E_gs(shell) and
+// e = regulate_exp(-x / kT), the three moments Z_i = sum e, M1_i = sum x e,
+// M2_i = sum x^2 e in one pass (each Boltzmann factor once).  With the
+// reference's shell weights w_i = Z_i d^i / sum_j Z_j d^j and per-shell
+// probabilities e / Z_i (fdmThermodynamics.hpp:42-236):
+//   <E> = sum_i d^i M1_i / L,  <E^2> = sum_i d^i M2_i / L,  L = sum_i d^i Z_i,
+//   S = ln L + <E> / kT,  C = (<E^2> - <E>^2) / kT^2.
+// sums: 3 * nshell doubles of scratch per temperature.
 __global__ void k_thermo(const double *__restrict__ disc, const int64_t *__restrict__ disc_off,
                          const double *__restrict__ gs, int nshell, const double *__restrict__ temps,
-                         double bathdim, double *__restrict__ wm_buf, double *__restrict__ entropy,
+                         double bathdim, double *__restrict__ sums, double *__restrict__ entropy,
                          double *__restrict__ cv) {
-  __shared__ double red[32];
-  const double kbt = temps[blockIdx.x];
-  double *wm = wm_buf + int64_t(blockIdx.x) * 2 * nshell;
-  double *zp = wm + nshell;
-  for (int i = 0; i < nshell; ++i) {
-    double z = 0.0;
-    for (int64_t a = disc_off[i] + threadIdx.x; a < disc_off[i + 1]; a += blockDim.x)
-      z += regulate_exp((gs[i] - disc[a]) / kbt);
-    z = cta_sum(z, red);
-    if (threadIdx.x == 0) {
-      wm[i] = z * pow(bathdim, double(i));
-      zp[i] = z;
+  const double kbt = temps[blockIdx.x], inv = 1.0 / kbt;
+  double *z = sums + int64_t(blockIdx.x) * 3 * nshell, *m1 = z + nshell, *m2 = m1 + nshell;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  for (int i = warp; i < nshell; i += nw) {
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+    const double g = gs[i];
+    for (int64_t a = disc_off[i] + lane; a < disc_off[i + 1]; a += 32) {
+      const double x = disc[a] - g;
+      const double w = regulate_exp(-x * inv);
+      s0 += w;
+      s1 += x * w;
+      s2 += x * x * w;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      s0 += __shfl_xor_sync(0xffffffffu, s0, o);
+      s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+      s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+    }
+    if (lane == 0) {
+      z[i] = s0;
+      m1[i] = s1;
+      m2[i] = s2;
     }
   }
   __syncthreads();
-  double lpart = 0.0;
-  for (int i = 0; i < nshell; ++i) lpart += wm[i];
-  double eav = 0.0, esq = 0.0;
-  for (int i = 0; i < nshell; ++i) {
-    const double wi = wm[i] / lpart;
-    double s1 = 0.0, s2 = 0.0;
-    for (int64_t a = disc_off[i] + threadIdx.x; a < disc_off[i + 1]; a += blockDim.x) {
-      const double blm = regulate_exp((gs[i] - disc[a]) / kbt) / zp[i];
-      const double x = disc[a] - gs[i];
-      s1 += x * wi * blm;
-      s2 += x * x * wi * blm;
-    }
-    eav += cta_sum(s1, red);
-    esq += cta_sum(s2, red);
-  }
   if (threadIdx.x == 0) {
-    entropy[blockIdx.x] = log(lpart) + (eav / kbt);
+    double lpart = 0.0, e1 = 0.0, e2 = 0.0;
+    for (int i = 0; i < nshell; ++i) {
+      const double d = pow(bathdim, double(i));
+      lpart += z[i] * d;
+      e1 += m1[i] * d;
+      e2 += m2[i] * d;
+    }
+    const double eav = e1 / lpart, esq = e2 / lpart;
+    entropy[blockIdx.x] = log(lpart) + eav / kbt;
     cv[blockIdx.x] = (esq - eav * eav) / (kbt * kbt);
   }
 }
@@ -196,10 +197,10 @@ void launch_broaden(const double *e, const double *w, int64_t nbins, const doubl
 }
 
 void launch_thermo(const double *disc, const int64_t *disc_off, const double *gs, int nshell,
-                   const double *temps, int nt, double bathdim, double *wm_buf, double *entropy,
+                   const double *temps, int nt, double bathdim, double *sums, double *entropy,
                    double *cv, cudaStream_t s) {
   if (nt == 0) return;
-  k_thermo<<<nt, 256, 0, s>>>(disc, disc_off, gs, nshell, temps, bathdim, wm_buf, entropy, cv);
+  k_thermo<<<nt, 256, 0, s>>>(disc, disc_off, gs, nshell, temps, bathdim, sums, entropy, cv);
 }
 
 }  // namespace nrg

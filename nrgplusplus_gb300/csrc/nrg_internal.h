@@ -222,9 +222,9 @@ void launch_partial_trace(const TraceTask *tasks, int ntask, const TraceIn *ins,
                           cudaStream_t s);
 void launch_broaden(const double *e, const double *w, int64_t nbins, const double *omegas,
                     int64_t nomega, double b, double *out, cudaStream_t s);
-// wm_buf: 2 * nshell * nt doubles of scratch
+// sums: 3 * nshell * nt doubles of scratch
 void launch_thermo(const double *disc, const int64_t *disc_off, const double *gs, int nshell,
-                   const double *temps, int nt, double bathdim, double *wm_buf, double *entropy,
+                   const double *temps, int nt, double bathdim, double *sums, double *entropy,
                    double *cv, cudaStream_t s);
 
 }  // namespace nrg

@@ -334,7 +334,7 @@ def kernel_models():
 
 # DRAM bytes (read + write) per launch measured with ncu on one engine's full
 # 8-run step (mean over its 869 launches; summary and command under profiles/)
-MEASURED_TRAFFIC = {"k_gemm_oz": 220.3e6}
+MEASURED_TRAFFIC = {"k_gemm_oz": 221.0e6}
 
 
 def kernel_profile(engine):

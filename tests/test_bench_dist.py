@@ -42,3 +42,33 @@ def test_max_over_ranks_two_gloo_ranks():
 def test_max_over_ranks_without_process_group():
     import bench
     assert bench.max_over_ranks([1.5, 2.5]) == [1.5, 2.5]
+
+
+def test_step_runs_every_engine_on_its_own_thread(monkeypatch):
+    """bench.step drives each engine from its own host thread, sums the
+    per-engine input / output byte counts and re-raises a failure."""
+    import sys
+    import threading
+    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    import bench
+    seen = {}
+    together = threading.Barrier(3, timeout=30)  # passes only if all three run at once
+
+    def fake_one_run(engine, e2e, batch=None):
+        together.wait()
+        seen[engine] = (threading.current_thread() is not threading.main_thread(), e2e, batch)
+        return 10 * engine, engine
+
+    monkeypatch.setattr(bench, "one_run", fake_one_run)
+    assert bench.step([1, 2, 3], True, 8) == (60, 6)
+    assert sorted(seen) == [1, 2, 3]
+    assert all(v == (True, True, 8) for v in seen.values())
+
+    def failing(engine, e2e, batch=None):
+        if engine == 2:
+            raise RuntimeError("engine 2 failed")
+        return 0, 0
+
+    monkeypatch.setattr(bench, "one_run", failing)
+    with pytest.raises(RuntimeError, match="engine 2 failed"):
+        bench.step([1, 2, 3], False)

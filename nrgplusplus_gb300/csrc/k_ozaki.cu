@@ -183,7 +183,8 @@ k_split_digits(const SplitTask *__restrict__ tasks, const int64_t *__restrict__ 
 // ----------------------------------------------------------------- GEMM
 constexpr int TM = 128, TN = 64, TK = 16;  // output tile, k-step (one MMA)
 constexpr int kStages = 4;
-constexpr int kTcThreads = 160;  // 4 consumer warps + 1 producer warp (one issuing thread)
+constexpr int kTcThreads = 288;  // 8 consumer warps + 1 producer warp (one issuing thread)
+constexpr int kConsumers = 256;
 constexpr int kATile = TM * TK * 2, kBTile = TN * TK * 2;  // bytes per plane
 constexpr int kAStage = kPlanes * kATile;                  // 32 KB
 constexpr int kStageBytes = kPlanes * (kATile + kBTile);   // 48 KB
@@ -269,17 +270,19 @@ struct StepIt {
 __device__ __forceinline__ void mma_commit(uint32_t bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
 }
-__device__ __forceinline__ void consumer_sync() {  // warps 0-3 only
-  asm volatile("bar.sync 1, 128;" ::: "memory");
+__device__ __forceinline__ void consumer_sync() {  // warps 0-7 only
+  asm volatile("bar.sync 1, 256;" ::: "memory");
 }
 
-// Warp roles: warp 4 lane 0 stages k-steps into a ring of kStages buffers
+// Warp roles: warp 8 lane 0 stages k-steps into a ring of kStages buffers
 // with TMA boxes (a stage is released by the tcgen05.commit of its MMAs on
 // empty[stage] and completes on full[stage] when its bytes have landed);
-// warp 0 lane 0 issues the 36 MMAs of each step; warps 0-3 (the 128 TMEM lanes) fold the
-// group sums whenever the scale changes, 512 k-terms are used up, or the
-// list ends (after a drain commit on `drain`).  No CTA-wide barrier sits in
-// the k-loop.
+// warp 0 lane 0 issues the 36 MMAs of each step; warps 0-7 fold the group
+// sums whenever the scale changes, 512 k-terms are used up, or the list ends
+// (after a drain commit on `drain`): warp w reads TMEM lanes 32 (w mod 4) ..
+// + 31 (the lane quadrant its id gives it access to) and columns
+// 32 (w div 4) .. + 31 of each accumulator, so two warps share each
+// quadrant's rows.  No CTA-wide barrier sits in the k-loop.
 __global__ void __launch_bounds__(kTcThreads, 1)
 k_gemm_oz(const GemmTile *__restrict__ tiles, const OzGroup *__restrict__ groups,
           const OzContrib *__restrict__ contribs, const OzTensorMap *__restrict__ maps, int *err) {
@@ -317,9 +320,9 @@ k_gemm_oz(const GemmTile *__restrict__ tiles, const OzGroup *__restrict__ groups
   for (int c = g.c0; c < g.c1; ++c)
     if (contribs[c].K > 0) nsteps += (contribs[c].K + TK - 1) / TK;
 
-  if (warp >= 4) {
+  if (warp >= 8) {
     // ------------------------------------------------------------- producer
-    if (warp == 4 && lane == 0) {
+    if (warp == 8 && lane == 0) {
       StepIt it{g.c0, 0};
       it.skip_empty(g, contribs);
       int issued = 0, cur = -1;
@@ -355,12 +358,13 @@ k_gemm_oz(const GemmTile *__restrict__ tiles, const OzGroup *__restrict__ groups
     bool first_fold = true;
     uint32_t drain_phase = 0;
     const uint32_t ring0 = smem_u32(ring);
-    const uint32_t tl = tmem + (uint32_t(32 * warp) << 16);
-    const int gm = m0 + 32 * warp + lane;
+    const int quad = warp & 3, half = warp >> 2;  // TMEM lane quadrant, column half
+    const uint32_t tl = tmem + (uint32_t(32 * quad) << 16);
+    const int gm = m0 + 32 * quad + lane;
 
     // Every consumer thread makes the same fold() calls (the fold points
     // depend only on the contribution list), so the named barrier at its end
-    // is always reached by all 128; after an abort the waits and TMEM reads
+    // is always reached by all 256; after an abort the waits and TMEM reads
     // are skipped (decided per warp, as tcgen05.ld is warp-collective).
     auto fold = [&]() {
       // drain: every MMA issued so far has completed
@@ -372,8 +376,8 @@ k_gemm_oz(const GemmTile *__restrict__ tiles, const OzGroup *__restrict__ groups
       asm volatile("tcgen05.fence::after_thread_sync;");
       // a warp whose 32 rows lie past M, and column chunks past N, have
       // nothing to fold (warp-uniform conditions: tcgen05.ld is collective)
-      if (__shfl_sync(0xffffffffu, abort_flag, 0) == 0 && m0 + 32 * warp < g.M) {
-        for (int cc = 0; cc < TN && n0 + cc < g.N; cc += 8) {
+      if (__shfl_sync(0xffffffffu, abort_flag, 0) == 0 && m0 + 32 * quad < g.M) {
+        for (int cc = 32 * half; cc < 32 * half + 32 && n0 + cc < g.N; cc += 8) {
           uint32_t v[kPlanes][8];
 #pragma unroll
           for (int d = 0; d < kPlanes; ++d) {
@@ -463,7 +467,7 @@ k_gemm_oz(const GemmTile *__restrict__ tiles, const OzGroup *__restrict__ groups
     }
     if (nsteps > 0) fold();
     if (nsteps == 0 && !g.accumulate) {  // empty contribution list: C = 0
-      for (int i = tid; i < TM * TN; i += 128) {
+      for (int i = tid; i < TM * TN; i += kConsumers) {
         const int r = i / TN, c = i - r * TN;
         if (m0 + r < g.M && n0 + c < g.N) g.C[int64_t(m0 + r) * g.ldc + n0 + c] = 0.0;
       }

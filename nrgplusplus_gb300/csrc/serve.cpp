@@ -224,6 +224,7 @@ void nrg_server::finish(Job &j, int status, const std::string &msg) {
     j.admitted = false;
     --n_active;
     reserved -= j.estimate;
+    cv_work.notify_all();  // budget and a share slot freed: waiting workers may admit
   }
   j.status = status;
   j.message = msg;
@@ -271,6 +272,12 @@ void nrg_server::loop(Worker &w) {
         queue.pop_front();
       }
       max_active_seen = std::max<uint64_t>(max_active_seen, n_active);
+      if (active.empty() && admitted.empty()) {
+        // queued work this worker may not take yet (the budget is held by
+        // other workers' runs): wait for a finish or a submission
+        cv_work.wait_for(lk, std::chrono::milliseconds(50));
+        continue;
+      }
     }
     for (auto &j : admitted) {
       try {

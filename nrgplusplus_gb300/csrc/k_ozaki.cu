@@ -23,10 +23,10 @@
 // layouts (K-major or MN-major per operand, so transposed operands need no
 // transpose).  A four-stage ring overlaps the copies of later k-steps with
 // the MMAs of the current one; tcgen05.commit arrives on one mbarrier per
-// stage when its MMAs are done.  The group sums
-// are folded into the FP64 output once per run of contributions that share a
-// scale (at most 512 deep): tcgen05.ld to registers, integer Horner over the
-// groups, one FP64 fma per element.  Every mbarrier wait is bounded; a wait
+// stage when its MMAs are done.  The group sums are folded into the FP64
+// output once per run of contributions that share a scale (at most 512
+// deep) by eight warps, two per TMEM lane quadrant: tcgen05.ld to registers,
+// integer Horner over the groups, one FP64 fma per element.  Every mbarrier wait is bounded; a wait
 // that runs out sets *err, and the kernel drains and releases TMEM.
 #include <cuda.h>
 #include <cuda_bf16.h>

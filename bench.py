@@ -1,26 +1,43 @@
-"""Benchmark: complete SIAM FDM runs per second on one GB300.
+"""Benchmark: complete SIAM spectral runs per second on one GB300, the mixed-
+precision batched engine against the plain FP64 GPU path.
 
-One run = the spectral workload (eps_d=-0.4, U=0.8, V=0.15, Lambda=2,
-Nkeep=1024, 50 Wilson sites): forward NRG with the d-dagger-chi operators
-tracked and device-resident snapshots, the T=0 FDM backward pass (binning
-into 1e5 log bins), log-Gaussian broadening (b=0.6, 100 points per decade
-over |w| in [1e-8, 1]) and entropy / specific heat on the 200-point
+Workload (``--workload``, default ``siam_fdm_nk2048``): the impurity spectral
+run eps_d=-0.4, U=0.8, V=0.15, Lambda=2 at Nkeep=2048 over 40 Wilson sites
+(``siam_fdm_nk1024``: Nkeep=1024, 50 sites) -- forward NRG with the
+d-dagger-chi operators tracked and device-resident snapshots, the T=0 FDM
+backward pass (1e5 log bins), log-Gaussian broadening (b=0.6, 100 points per
+decade over |w| in [1e-8, 1]) and entropy / specific heat on the 200-point
 temperature grid.  One step = ENGINES engines, each driven by its own host
-thread, each stepping RUNS_PER_ENGINE runs together (batched launches); the
-engines' streams overlap one engine's host work with another's kernels.
-The reference publishes no number for this metric.
+thread, each stepping BATCH runs together (one launch per phase for all
+their blocks).  The reference publishes no number for this metric.
 
-  value : runs/s through the engine, results left on the device
-  e2e   : runs/s through the public C-ABI calls a user makes, with the
-          per-site all_eigenvalue and the final spectra / thermodynamics
-          copied to host buffers inside the timed region
+  value      : runs/s through the engine, mixed precision, results left on
+               the device (every site's eigenvalues still come back to the
+               host, as the truncation bookkeeping needs them)
+  e2e        : runs/s through the public C-ABI calls a user makes, with the
+               per-site all_eigenvalue and the final spectra /
+               thermodynamics copied to host buffers inside the timed region
+  plain_fp64 : the same steps on the plain FP64 GPU path (warm-up step, then
+               timed steps), with its own roofline against a measured FP64
+               peak (cuBLAS DGEMM through torch, CUDA events)
+  error      : every eigenvalue of every site, the spectral function and
+               the thermodynamics of both paths against the reference's own
+               outputs for this workload (tests/golden fixtures) and against
+               each other
+  sweep      : runs/s of a chunk of the seeded 512-instance SIAM sweep
+               (mixed Lambda, Nkeep, lengths; RG flows) on both paths
+  serving    : the workload's runs as requests to the continuous-batching
+               server, seeded Poisson arrivals at 80 % of the batch
+               throughput: p50 / p99 latency and served runs/s
+  roofline   : the dominant kernel, useful work only (an FP64-accurate
+               tensor-core product counts 2MNK, not its digit-plane
+               products), plus the path-level (F_eig + F_rot) / t
   --impl reference : the reference's CPU algorithm (the numpy port of the
-          oracle) timed on this host's cores on the same workload
-  serving : the same runs as requests to the continuous-batching server
-          (nrg_server_*), seeded Poisson arrivals at 80 % of the measured
-          batch throughput: p50 / p99 request latency and served runs/s
+               oracle) on this host's cores, the better of one run on all
+               threads and one single-threaded run per core
 
 usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                       [--workload siam_fdm_nk2048|siam_fdm_nk1024]
 """
 import argparse
 import json
@@ -29,30 +46,60 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-WORK = dict(kind="siam", nkeep=1024, nsites=50, lam=2.0, eps=-0.4, U=0.8, V=0.15)
-BATCH = int(os.environ.get("NRG_BENCH_BATCH", "8"))  # runs stepped together per engine
-ENGINES = int(os.environ.get("NRG_BENCH_ENGINES", "4"))  # engines (host threads) per step
-CONFIG = {"workload": "siam_fdm_spectral_c2", "impurity": "spinhalf(eps_d=-0.4,U=0.8)",
-          "V": 0.15, "Lambda": 2.0, "Nkeep": 1024, "sites": 50, "T": 1e-6,
-          "spectral": "T=0 FDM, b=0.6, 801 points |w| in [1e-8,1]",
-          "thermo": "entropy + C on 200-point T grid",
-          "l2": "flushed (256 MiB write) between steps", "runs_per_step": ENGINES * BATCH,
-          "engines": ENGINES, "runs_per_engine": BATCH}
-METRIC = "SIAM runs/s (full FDM spectral run, Nkeep=1024, 50 sites)"
+WORKLOADS = {
+    "siam_fdm_nk2048": dict(kind="siam", nkeep=2048, nsites=40, lam=2.0, eps=-0.4, U=0.8, V=0.15,
+                            fixture="ref_siam_fdm_nk2048", thermo_fixture="ref_siam_thermo_nk2048",
+                            engines=4, batch=4),
+    "siam_fdm_nk1024": dict(kind="siam", nkeep=1024, nsites=50, lam=2.0, eps=-0.4, U=0.8, V=0.15,
+                            fixture="ref_c2_siam_fdm_nk1024", thermo_fixture="ref_c2_siam_thermo_nk1024",
+                            engines=4, batch=8),
+}
+WORK = dict(WORKLOADS["siam_fdm_nk2048"])
+NAME = "siam_fdm_nk2048"
+BATCH = int(os.environ.get("NRG_BENCH_BATCH", "0")) or WORK["batch"]      # runs stepped together per engine
+ENGINES = int(os.environ.get("NRG_BENCH_ENGINES", "0")) or WORK["engines"]  # engines (host threads) per step
 
 
-def serving_run(engine, rate, n, seed=2024, max_active=BATCH, workers=ENGINES):
+def select_workload(name):
+    global WORK, NAME, BATCH, ENGINES
+    if name not in WORKLOADS:
+        raise SystemExit("unknown workload %r (one of %s)" % (name, ", ".join(WORKLOADS)))
+    NAME = name
+    WORK = dict(WORKLOADS[name])
+    BATCH = int(os.environ.get("NRG_BENCH_BATCH", "0")) or WORK["batch"]
+    ENGINES = int(os.environ.get("NRG_BENCH_ENGINES", "0")) or WORK["engines"]
+
+
+def config():
+    w = WORK
+    return {"workload": NAME, "impurity": "spinhalf(eps_d=%g,U=%g)" % (w["eps"], w["U"]),
+            "V": w["V"], "Lambda": w["lam"], "Nkeep": w["nkeep"], "sites": w["nsites"],
+            "spectral": "T=0 FDM (the reference's fdmSpectrum is T=0 only), b=0.6, 801 points |w| in [1e-8,1]",
+            "thermo": "entropy + C on 200-point T grid",
+            "l2": "flushed (256 MiB write) between steps", "runs_per_step": ENGINES * BATCH,
+            "engines": ENGINES, "runs_per_engine": BATCH}
+
+
+def metric():
+    return "SIAM runs/s (full FDM spectral run, Nkeep=%d, %d sites), mixed precision" % (
+        WORK["nkeep"], WORK["nsites"])
+
+
+def serving_run(engine, rate, n, seed=2024, max_active=None, workers=None):
     """Seeded Poisson stream of n workload requests at `rate` per second into
     the serving loop (`workers` engines, up to `max_active` runs each);
     latency = submission to completed results."""
     import threading
     import numpy as np
     from nrgplusplus_gb300 import api, workloads
+    max_active = BATCH if max_active is None else max_active
+    workers = ENGINES if workers is None else workers
     w = WORK
     req = workloads.siam_request(w["nkeep"], w["nsites"], w["lam"], w["V"], eps=w["eps"], U=w["U"],
                                  fdm=True, thermo=True, keep_eigs=False)
@@ -118,18 +165,20 @@ def _ops_bytes(ops):
 
 
 class ClockSampler:
-    """nvidia-smi clock/throttle sampling during the timed region."""
+    """nvidia-smi clock/throttle sampling during the timed region (samples in
+    a temporary file, summarised into the result line)."""
 
-    def __init__(self, path):
-        self.path = path
+    def __init__(self):
         self.p = None
+        self.path = None
 
     def __enter__(self):
         q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        fd, self.path = tempfile.mkstemp(prefix="nrg_bench_clocks_", suffix=".csv")
+        self.f = os.fdopen(fd, "w")
         try:
-            self.f = open(self.path, "w")
             self.p = subprocess.Popen(["nvidia-smi", "--query-gpu=" + q, "--format=csv,noheader,nounits",
                                        "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
         except Exception:
@@ -140,7 +189,7 @@ class ClockSampler:
         if self.p:
             self.p.terminate()
             self.p.wait()
-            self.f.close()
+        self.f.close()
 
     def summary(self):
         sm, mx, reasons = [], 0.0, set()
@@ -160,17 +209,24 @@ class ClockSampler:
                         reasons.add(name)
         except OSError:
             pass
+        finally:
+            try:
+                os.remove(self.path)
+            except OSError:
+                pass
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx or None,
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def one_run(engine, e2e, batch=None):
-    """One step: `batch` complete spectral runs stepped together (one launch
-    per phase for all their blocks), then each run's backward passes.  With
-    e2e the caller-visible results are copied to host buffers as a user of
-    the API would read them.  Returns the host-to-device bytes of the inputs
-    (models, tracked operators, hoppings, temperatures) and the device-to-host
-    bytes of the results of the step."""
+def one_run(engine, e2e, batch=None, collect=False):
+    """One engine's share of a step: `batch` complete spectral runs stepped
+    together (one launch per phase for all their blocks), then their backward
+    passes shell by shell (the FDM of every run in one batched call per
+    shell).  With e2e the caller-visible results are copied to host buffers as
+    a user of the API would read them.  Returns (host-to-device bytes of the
+    inputs, device-to-host bytes of the results, outputs of run 0 when
+    `collect`: every site's all_eigenvalue, the histograms, the broadened
+    spectral functions, entropy and specific heat)."""
     import numpy as np
     from nrgplusplus_gb300 import api, workloads
     from nrgplusplus_gb300 import models as M
@@ -187,6 +243,7 @@ def one_run(engine, e2e, batch=None):
     api.batch_update_state(runs)
     d2h = 0
     min_it = [0] * B
+    got = {"eig": []} if collect else None
     for it in range(w["nsites"]):
         api.batch_add_site(runs, [[M.hopping(it, lam)] * 2] * B, [math.sqrt(lam) if it > 0 else 1.0] * B)
         api.update_system_operator_batch(runs, ops)
@@ -198,9 +255,9 @@ def one_run(engine, e2e, batch=None):
         api.batch_update_state(runs)
         if e2e:
             d2h += sum(r.all_eigenvalue.nbytes for r in runs)
+        if collect:
+            got["eig"].append(runs[0].all_eigenvalue)
     om = np.logspace(-8, 0, 801)
-    # backward passes of all runs shell by shell, the FDM of every run in one
-    # batched call per shell (the thermodynamics are host sums)
     fs = [api.FdmSpectrum(r, 2) for r in runs]
     ths = [api.FdmThermodynamics(r, workloads.temperature_grid()) for r in runs]
     cnt = [r.nrg_iterations_cnt for r in runs]
@@ -220,6 +277,9 @@ def one_run(engine, e2e, batch=None):
         tdat = ths[k].saveFinalData()
         d2h += spec["GreenFnPositiveWeight"].nbytes * 2 + sum(a.nbytes for a in A)
         d2h += tdat["entropy"].nbytes * 2
+        if collect and k == 0:
+            got.update(spectra=A, energies=spec["GreenFnEnergyPoints"], entropy=tdat["entropy"],
+                       cv=tdat["specificHeat"], omegas=om)
         fs[k].close()
         ths[k].close()
         ops[k].close()
@@ -227,19 +287,20 @@ def one_run(engine, e2e, batch=None):
     imp, bath = M.spinhalf(w["eps"], w["U"]), M.spinhalf(0.0, 0.0)
     h2d = B * (_site_bytes(imp) + _site_bytes(bath) + _ops_bytes(M.d_dag_chi())
                + 8 * (w["nsites"] + 1) * 3 + 8 * len(workloads.temperature_grid()))
-    return h2d, d2h
+    return h2d, d2h, got
 
 
-def step(engines, e2e, batch=None):
+def step(engines, e2e, batch=None, collect=False):
     """One bench step: every engine runs one_run in its own host thread
     (ctypes releases the GIL inside each C-ABI call).  Returns the summed
-    (h2d, d2h) bytes; re-raises the first error of any thread."""
+    (h2d, d2h) bytes and engine 0's collected outputs; re-raises the first
+    error of any thread."""
     import threading
     res, errs = [None] * len(engines), []
 
     def drive(k):
         try:
-            res[k] = one_run(engines[k], e2e, batch)
+            res[k] = one_run(engines[k], e2e, batch, collect and k == 0)
         except BaseException as x:  # noqa: BLE001 - re-raised below
             errs.append(x)
 
@@ -250,19 +311,88 @@ def step(engines, e2e, batch=None):
         t.join()
     if errs:
         raise errs[0]
-    return sum(r[0] for r in res), sum(r[1] for r in res)
+    return sum(r[0] for r in res), sum(r[1] for r in res), res[0][2]
 
 
-def time_oracle_run(max_sites):
-    """The oracle port on this host's cores: the same workload, forward sites
-    capped at max_sites (bounded sample)."""
+# ------------------------------------------------------------ CPU baseline
+def _cpu_sample(work, sites):
+    """One bounded sample of the workload on the numpy port of the oracle:
+    the V site, `sites` Wilson sites with d-dagger-chi tracked, then the FDM
+    and thermodynamics backward passes over the shells it produced.
+    Returns its wall time in seconds."""
     from oracle.nrg_oracle import siam_run
     from nrgplusplus_gb300 import models as M
-    w = WORK
     t0 = time.perf_counter()
-    siam_run(M.spinhalf(w["eps"], w["U"]), M.spinhalf(0, 0), w["nkeep"], max_sites, w["lam"],
-             V=w["V"], track_ops=M.d_dag_chi(), fdm=True, thermo=False, full_fdag=True)
+    siam_run(M.spinhalf(work["eps"], work["U"]), M.spinhalf(0, 0), work["nkeep"], sites, work["lam"],
+             V=work["V"], track_ops=M.d_dag_chi(), fdm=True, thermo=True, full_fdag=False)
     return time.perf_counter() - t0
+
+
+class CpuBaseline:
+    """The reference's algorithm on this host's cores, in the two modes of a
+    throughput baseline: one run at a time on all BLAS threads ("one"), and
+    one single-threaded run per core at once ("per_core", a spawn-started
+    process pool, so it may start after the GPU is in use).  A sample runs
+    the first `sites` of the workload's Wilson sites and its backward passes;
+    runs/s counts it as sites/nsites of a run (per-site cost is flat once the
+    truncation starts and lower before, so the extrapolation favours the
+    CPU)."""
+
+    def __init__(self, sites):
+        self.sites = max(1, min(sites, WORK["nsites"]))
+        self.cores = cpu_cores()
+        self.pool = None
+
+    def _pool(self):
+        if self.pool is None:
+            import multiprocessing as mp
+            keys = ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS")
+            old = {k: os.environ.get(k) for k in keys}
+            for k in keys:
+                os.environ[k] = "1"
+            try:
+                self.pool = mp.get_context("spawn").Pool(self.cores)
+                self.pool.map(_cpu_sample, [(dict(WORK, nkeep=16), 1)] * self.cores)  # imports done
+            finally:
+                for k, v in old.items():
+                    if v is None:
+                        os.environ.pop(k, None)
+                    else:
+                        os.environ[k] = v
+        return self.pool
+
+    def measure(self, mode):
+        """(runs/s, wall seconds) of one sample in `mode`."""
+        frac = self.sites / WORK["nsites"]
+        t0 = time.perf_counter()
+        if mode == "one":
+            _cpu_sample(WORK, self.sites)
+            n = 1
+        else:
+            self._pool().starmap(_cpu_sample, [(WORK, self.sites)] * self.cores)
+            n = self.cores
+        wall = time.perf_counter() - t0
+        return n * frac / wall, wall
+
+    def best(self):
+        """Both modes once; the better one's line."""
+        r1, w1 = self.measure("one")
+        r2, w2 = self.measure("per_core")
+        mode, v, w = ("one", r1, w1) if r1 >= r2 else ("per_core", r2, w2)
+        return {"value": v, "unit": "runs/s", "cores": self.cores,
+                "kind": "port", "mode": mode,
+                "modes": {"one_run_all_threads": r1, "one_run_per_core": r2},
+                "sample": "numpy port of the reference (LAPACK syevd + BLAS dgemm), the workload's "
+                          "first %d of %d Wilson sites with operator tracking, FDM and thermodynamics "
+                          "backward passes, counted as %d/%d of a run; better of one run on all threads "
+                          "(%.2f runs/s) and %d single-threaded runs at once (%.2f runs/s); %.1f s"
+                          % (self.sites, WORK["nsites"], self.sites, WORK["nsites"], r1, self.cores, r2, w)}
+
+    def close(self):
+        if self.pool is not None:
+            self.pool.terminate()
+            self.pool.join()
+            self.pool = None
 
 
 def cpu_cores():
@@ -273,32 +403,45 @@ def cpu_cores():
 
 
 def reference_arm(args):
+    """--impl reference: the CPU algorithm on this host, steps of one bounded
+    sample each, in whichever mode the warm-up found faster."""
     ws, rank = _dist()
     if rank != 0:
         return 0
-    times = []
-    sites = WORK["nsites"]
-    for _ in range(args.warmup if args.warmup < 1 else 1):
-        time_oracle_run(4)
-    for _ in range(args.steps):
-        times.append(time_oracle_run(sites))
-    t = sum(times) / len(times)
-    v = 1.0 / t
-    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "runs/s", "n_gpus": args.gpus,
+    cb = CpuBaseline(args.cpu_sites)
+    try:
+        r = {"one": cb.measure("one")[0], "per_core": cb.measure("per_core")[0]}
+        mode = max(r, key=r.get)
+        for _ in range(max(0, args.warmup - 2)):
+            cb.measure(mode)
+        walls, vals = [], []
+        for _ in range(args.steps):
+            v, w = cb.measure(mode)
+            vals.append(v)
+            walls.append(w)
+    finally:
+        cb.close()
+    t = sum(walls) / len(walls)
+    v = sum(vals) / len(vals)
+    sample = ("numpy port of the reference (LAPACK syevd + BLAS dgemm): per step %s, each the first %d of %d "
+              "Wilson sites of the workload with operator tracking, FDM and thermodynamics backward passes, "
+              "counted as %d/%d of a run; mode chosen by the warm-up (one run on all threads %.3f runs/s, "
+              "%d single-threaded runs at once %.3f runs/s)"
+              % ("one run on all host threads" if mode == "one" else "%d single-threaded runs at once" % cb.cores,
+                 cb.sites, WORK["nsites"], cb.sites, WORK["nsites"], r["one"], cb.cores, r["per_core"]))
+    line = {"impl": "reference", "metric": metric(), "value": v, "unit": "runs/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic (model parameters only)", "config": CONFIG,
-            "cpu_baseline": {"value": v, "unit": "runs/s", "cores": cpu_cores(), "kind": "port",
-                             "sample": "full workload per step (numpy restatement of the reference, "
-                                       "LAPACK syevd + BLAS dgemm, all host threads)"},
+            "data": "synthetic (model parameters only)", "config": config(),
+            "cpu_baseline": {"value": v, "unit": "runs/s", "cores": cb.cores, "threads_mode": mode,
+                             "kind": "port", "sample": sample},
             "e2e": {"value": v, "unit": "runs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
     return 0
 
 
-# nominal per-GPU peaks for the pipes MEASURED_PEAKS.json does not cover
-FP64_PEAK_TFLOPS = 1.25   # GB300 FP64 (vector and tensor) dense
-FP32_PEAK_TFLOPS = 80.5   # 152 SMs x 128 FP32 lanes x 2 flops x 2.07 GHz
+# ---------------------------------------------------------------- rooflines
+FP32_PEAK_TFLOPS = 80.5   # nominal: 152 SMs x 128 FP32 lanes x 2 flops x 2.07 GHz
 
 
 def _measured(key, fallback):
@@ -309,42 +452,68 @@ def _measured(key, fallback):
         return fallback, "of fallback (%s)" % key
 
 
-def kernel_models():
+def measure_fp64_peak():
+    """FP64 peak of this GPU: cuBLAS DGEMM 8192^3 through torch.matmul, best
+    of 5 after 2 warm-ups, CUDA events on torch's stream (2 N^3 flops)."""
+    import torch
+    n = 8192
+    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    c = torch.empty_like(a)
+    for _ in range(2):
+        torch.matmul(a, b, out=c)
+    best = float("inf")
+    for _ in range(5):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b, out=c)
+        e1.record()
+        e1.synchronize()
+        best = min(best, e0.elapsed_time(e1))
+    del a, b, c
+    torch.cuda.empty_cache()
+    return 2.0 * n ** 3 / (best * 1e-3) / 1e12
+
+
+def kernel_models(fp64_peak):
     """Per kernel: (bound, peak, unit, multiplier from the recorded work to the
     unit's numerator, peak source, per-launch work definition)."""
     bf16, bf16_src = _measured("bf16_tflops_sustained", 1700.0)
     hbm, hbm_src = _measured("hbm_gbs", 6800.0)
-    fp64 = ("fp64", FP64_PEAK_TFLOPS, "TFLOP/s", 1e-12, "nominal GB300 FP64",
+    fp64 = ("fp64", fp64_peak, "TFLOP/s", 1e-12, "of measured (cuBLAS DGEMM 8192^3 in this run)",
             "2MNK per GEMM contribution / (10/3) n^3 per eigensolved block")
     return {
         "k_gemm_f64": fp64,
         "k_eig_f64": fp64,
-        "k_eig_bi_f32": ("fp32", FP32_PEAK_TFLOPS, "TFLOP/s", 1e-12, "nominal GB300 FP32",
+        "k_eig_bi_f32": ("fp32", FP32_PEAK_TFLOPS, "TFLOP/s", 1e-12, "of nominal GB300 FP32",
                          "(4/3) n^3 per block (Householder reduction)"),
-        "k_reflect": ("fp32", FP32_PEAK_TFLOPS, "TFLOP/s", 1e-12, "nominal GB300 FP32",
+        "k_reflect": ("fp32", FP32_PEAK_TFLOPS, "TFLOP/s", 1e-12, "of nominal GB300 FP32",
                       "2 n^3 per block (Householder reflectors applied to the tridiagonal eigenvectors)"),
         "k_gemm_oz": ("tensor", bf16, "TFLOP/s", 1e-12, bf16_src,
-                      "bf16 tensor flops: 2MNK per digit-plane product (36 products per FP64-accurate "
-                      "product with 8 planes, 15 with the 5 planes of the first refinement step)"),
+                      "useful work: 2MNK per FP64-accurate product; the bf16 digit-plane products it "
+                      "takes are reported apart (tensor_pipe)"),
         "k_split": ("hbm", hbm, "GB/s", 1e-9, hbm_src,
                     "bytes: 8 (max pass) + 8 (digit pass) read + 16 written per element"),
         "k_oa_update": ("hbm", hbm, "GB/s", 1e-9, hbm_src, "bytes: S, G read + E written, 24 per element"),
     }
 
 
-# DRAM bytes (read + write) per launch measured with ncu on one engine's full
-# 8-run step (mean over its 869 launches; summary and command under profiles/)
+# DRAM bytes (read + write) per launch measured with ncu on one engine's
+# batch (mean over its launches; summary and command under profiles/)
 MEASURED_TRAFFIC = {"k_gemm_oz": 221.0e6}
 
 
 def kernel_profile(engine):
-    """One extra run with per-kernel CUDA events on the engine stream."""
+    """One extra engine batch with per-kernel CUDA events on the engine
+    stream; returns ({kernel: (ms, work, launches)}, work counters)."""
     engine.set_profiling(True)
     engine.kernel_times()
+    engine.work_counters(reset=True)
     one_run(engine, e2e=False)
     kt = engine.kernel_times()
+    wc = engine.work_counters(reset=True)
     engine.set_profiling(False)
-    return kt
+    return kt, wc
 
 
 def _roofline(name, ms, work, n, models):
@@ -353,21 +522,157 @@ def _roofline(name, ms, work, n, models):
     return {"bound": bound, "kernel": name, "achieved": achieved, "peak": peak, "unit": unit,
             "frac": achieved / peak if peak else None, "traffic": MEASURED_TRAFFIC.get(name),
             "traffic_unit": "bytes per launch (ncu dram__bytes_read.sum + dram__bytes_write.sum)",
-            "peak_source": src,
-            "launches": n, "ms_total": ms, "per_launch": per}
+            "peak_source": src, "launches": n, "ms_total": ms, "per_launch": per}
 
 
-def roofline_from(kt):
-    """Roofline of the kernel with the largest share of the step, plus every
-    modelled kernel's own line."""
-    models = kernel_models()
+def roofline_from(kt, wc, fp64_peak):
+    """Roofline of the kernel with the largest share of the batch, every
+    modelled kernel's own line, and the tensor-pipe view of k_gemm_oz."""
+    models = kernel_models(fp64_peak)
     known = {k: v for k, v in kt.items() if k in models}
     top = max(known.items(), key=lambda kv: kv[1][0])
     rf = _roofline(top[0], *top[1], models)
-    rf["all"] = {k: {"achieved": round(r["achieved"], 2), "unit": r["unit"], "frac": round(r["frac"], 4),
+    rf["all"] = {k: {"achieved": round(r["achieved"], 3), "unit": r["unit"], "frac": round(r["frac"], 5),
                      "bound": r["bound"], "ms": round(v[0], 3)}
                  for k, v in known.items() for r in [_roofline(k, *v, models)]}
+    if "k_gemm_oz" in kt and kt["k_gemm_oz"][0] > 0 and wc.get("tc_useful"):
+        ms = kt["k_gemm_oz"][0]
+        bf16 = models["k_gemm_oz"][1]
+        pipe = wc["tc_bf16"] / (ms * 1e-3) / 1e12
+        rf["tensor_pipe"] = {"kernel": "k_gemm_oz", "bf16_tflops": pipe, "frac_of_bf16_peak": pipe / bf16,
+                             "digit_plane_products_per_useful": wc["tc_bf16"] / wc["tc_useful"],
+                             "note": "bf16 tensor-pipe work the FP64-accurate products took; not useful work"}
     return rf
+
+
+# ------------------------------------------------------------------ errors
+def _eig_tol(N, lam):
+    """Eigenvalue tolerance of the parity tests (tests/parity.py eig_tol):
+    1e-10 absolute in iteration units until the reference's own FP64 noise,
+    which grows like Lambda^(N/2) along the flow, exceeds it."""
+    return max(1e-10, 1e-14 * lam ** (N / 2.0))
+
+
+def _compare(got, ref_eigs, ref_spectra, ref_entropy, ref_cv, T):
+    import numpy as np
+    lam = WORK["lam"]
+    eabs, eover, emax_site = 0.0, 0.0, 0
+    for i, (a, b) in enumerate(zip(got["eig"], ref_eigs)):
+        if a.size != b.size:
+            return {"eig_count_mismatch_at_site": i}
+        d = float(np.abs(a - b).max()) if a.size else 0.0
+        if d > eabs:
+            eabs, emax_site = d, i
+        eover = max(eover, d / _eig_tol(i, lam))
+    spec = 0.0
+    for a, b in zip(got["spectra"], ref_spectra):
+        spec = max(spec, float(np.abs(a - b).max() / np.abs(b).max()))
+    m = T >= 2.6e-7
+    return {"eig_max_abs": eabs, "eig_max_abs_site": emax_site, "eig_max_over_tol": eover,
+            "eig_values_compared": int(sum(a.size for a in got["eig"])),
+            "spectral_max_rel": spec,
+            "entropy_max_abs": float(np.abs(got["entropy"] - ref_entropy).max()),
+            "cv_max_rel_T_ge_2.6e-7": float(np.max(np.abs(got["cv"][m] - ref_cv[m]) / np.abs(ref_cv[m])))}
+
+
+def output_errors(engine, got_mixed, got_fp64):
+    """Both paths' outputs of one run against the reference's outputs for the
+    same workload (tests/golden fixtures, generated from the reference
+    compiled from its own sources) and against each other."""
+    import numpy as np
+    from nrgplusplus_gb300 import workloads
+    gold = os.path.join(ROOT, "tests", "golden")
+    fx = np.load(os.path.join(gold, WORK["fixture"] + ".npz"))
+    th = np.load(os.path.join(gold, WORK["thermo_fixture"] + ".npz"))
+    T = workloads.temperature_grid()
+    eigs = [fx["eig%d" % i] for i in range(WORK["nsites"])]
+    e = got_mixed["energies"]
+    om = got_mixed["omegas"]
+    spectra = []
+    for key in ("Positive", "Negative"):
+        for ip in range(2):
+            h = np.zeros(100000)
+            h[fx["GreenFn%sWeight%d_idx" % (key, ip)]] = fx["GreenFn%sWeight%d_val" % (key, ip)]
+            spectra.append(engine.broaden(e, h, om, 0.6))
+    out = {"vs_reference": {}, "tolerances": {
+        "eig": "|dE| <= max(1e-10, 1e-14 Lambda^(N/2)) per site N (the reference's own FP64 noise); "
+               "north-star target 1e-9", "spectral": "1e-6 of the maximum", "entropy": "1e-8"}}
+    for name, got in (("mixed", got_mixed), ("fp64", got_fp64)):
+        if got:
+            out["vs_reference"][name] = _compare(got, eigs, spectra, th["entropy"], th["specificHeat"], T)
+    if got_mixed and got_fp64:
+        out["mixed_vs_fp64"] = _compare(got_mixed, got_fp64["eig"], got_fp64["spectra"], got_fp64["entropy"],
+                                        got_fp64["cv"], T)
+    return out
+
+
+# ------------------------------------------------------------------- sweep
+def sweep_pass(engines, count):
+    """The first `count` instances of the seeded 512-instance sweep, spread
+    over the engines (greedy by Nkeep^2 x sites), each engine stepping its
+    share as one heterogeneous batch in its own host thread.  Returns the
+    wall time in seconds."""
+    import threading
+    from nrgplusplus_gb300 import workloads
+    inst = workloads.sweep_instances()[:count]
+    order = sorted(range(len(inst)), key=lambda k: -inst[k]["nkeep"] ** 2 * inst[k]["nsites"])
+    load, share = [0.0] * len(engines), [[] for _ in engines]
+    for k in order:
+        j = min(range(len(engines)), key=lambda x: load[x])
+        share[j].append(inst[k])
+        load[j] += inst[k]["nkeep"] ** 2 * inst[k]["nsites"]
+    errs = []
+
+    def drive(j):
+        try:
+            if share[j]:
+                workloads.run_flow_batch(engines[j], share[j], keep_eigs=True)
+        except BaseException as x:  # noqa: BLE001 - re-raised below
+            errs.append(x)
+
+    t0 = time.perf_counter()
+    ths = [threading.Thread(target=drive, args=(j,)) for j in range(len(engines))]
+    for t in ths:
+        t.start()
+    for t in ths:
+        t.join()
+    for e in engines:
+        e.sync()
+    wall = time.perf_counter() - t0
+    if errs:
+        raise errs[0]
+    return wall
+
+
+# -------------------------------------------------------------------- main
+def timed_steps(engines, k, e2e, barrier, flush):
+    """k timed steps (L2 flushed before each, barrier + sync on both sides);
+    returns (seconds per step list, h2d, d2h, algorithmic work of the steps)."""
+    times, h2d, d2h = [], 0, 0
+    for e in engines:
+        e.work_counters(reset=True)
+    for _ in range(k):
+        flush.zero_()
+        barrier()
+        t0 = time.perf_counter()
+        h2d, d2h, _ = step(engines, e2e=e2e)
+        for e in engines:
+            e.sync()
+        barrier()
+        times.append(time.perf_counter() - t0)
+    work = {"F_eig": 0.0, "F_rot": 0.0}
+    for e in engines:
+        wc = e.work_counters(reset=True)
+        work["F_eig"] += wc["F_eig"]
+        work["F_rot"] += wc["F_rot"]
+    return times, h2d, d2h, work
+
+
+def path_roofline(work, seconds, peak, peak_src, pipe):
+    """Path level: (F_eig + F_rot) / t over the timed steps."""
+    a = (work["F_eig"] + work["F_rot"]) / seconds / 1e12
+    return {"achieved": a, "unit": "TFLOP/s", "peak": peak, "frac": a / peak, "peak_source": peak_src,
+            "pipe": pipe, "F_eig_per_run": None, "F_rot_per_run": None}
 
 
 def main():
@@ -376,18 +681,26 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours")
-    ap.add_argument("--cpu-sites", type=int, default=50,
-                    help="forward sites of the bounded CPU-baseline sample")
+    ap.add_argument("--workload", default="siam_fdm_nk2048", choices=sorted(WORKLOADS))
+    ap.add_argument("--cpu-sites", type=int, default=0,
+                    help="Wilson sites of one bounded CPU-baseline sample (default: per workload)")
+    ap.add_argument("--e2e-steps", type=int, default=3, help="timed steps of the e2e measurement")
+    ap.add_argument("--fp64-steps", type=int, default=3, help="timed steps of the plain FP64 comparator")
+    ap.add_argument("--sweep-runs", type=int, default=48,
+                    help="instances of the seeded sweep timed on both paths (0: skip)")
     ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 comparator")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving-loop measurement")
-    ap.add_argument("--serving-requests", type=int, default=64)
-    ap.add_argument("--sites", type=int, default=50,
-                    help="Wilson sites per run (50 = the workload; fewer only for profiling captures)")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    ap.add_argument("--serving-requests", type=int, default=48)
+    ap.add_argument("--sites", type=int, default=0,
+                    help="Wilson sites per run (default: the workload's; fewer only for profiling captures)")
     args = ap.parse_args()
-    if args.sites != WORK["nsites"]:
+    select_workload(args.workload)
+    if not args.cpu_sites:
+        args.cpu_sites = 12 if WORK["nkeep"] >= 2048 else 20
+    reduced = bool(args.sites) and args.sites != WORK["nsites"]
+    if reduced:
         WORK["nsites"] = args.sites
-        CONFIG["sites"] = args.sites
-        CONFIG["workload"] += "_reduced_for_profiling"
     if args.impl == "reference":
         return reference_arm(args)
     import torch
@@ -400,6 +713,7 @@ def main():
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     torch.cuda.set_device(local)
     build(verbose=False)
+    fp64_peak = measure_fp64_peak()
     engines = [api.Engine(api.PREC_MIXED, device=local) for _ in range(ENGINES)]
     engine = engines[0]
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
@@ -409,86 +723,100 @@ def main():
             torch.distributed.barrier()
         torch.cuda.synchronize()
 
-    for _ in range(args.warmup):
-        step(engines, e2e=False)
-    times, d2h = [], 0
+    got_mixed = None
+    for w in range(max(1, args.warmup)):
+        _, _, got = step(engines, e2e=False, collect=(w == 0 and not reduced))
+        got_mixed = got_mixed or got
     launch_total = lambda: sum(e.launch_count() for e in engines)  # noqa: E731
     l0 = launch_total()
-    os.makedirs(os.path.join(ROOT, "gpurun_out"), exist_ok=True)
-    with ClockSampler(os.path.join(ROOT, "gpurun_out", "bench_clocks.csv")) as clk:
-        for _ in range(args.steps):
-            flush.zero_()
-            barrier()
-            t0 = time.perf_counter()
-            step(engines, e2e=False)
-            for e in engines:
-                e.sync()
-            barrier()
-            times.append(time.perf_counter() - t0)
+    with ClockSampler() as clk:
+        times, _, _, work = timed_steps(engines, args.steps, False, barrier, flush)
         launches = (launch_total() - l0) // args.steps
-        e2e_times = []
-        for _ in range(args.steps):
-            flush.zero_()
-            barrier()
-            t0 = time.perf_counter()
-            h2d, d2h = step(engines, e2e=True)
-            for e in engines:
-                e.sync()
-            barrier()
-            e2e_times.append(time.perf_counter() - t0)
+        e2e_times, h2d, d2h, _ = timed_steps(engines, max(1, args.e2e_steps), True, barrier, flush)
+    clocks = clk.summary()
     runs = ENGINES * BATCH
     tsum, esum = max_over_ranks([sum(times), sum(e2e_times)])
     per = tsum / args.steps
     value = ws * runs / per
-    e2e_v = ws * runs / (esum / args.steps)
-    kt = kernel_profile(engine)
-    rf = roofline_from(kt)
+    e2e_v = ws * runs / (esum / len(e2e_times))
+    bf16, bf16_src = _measured("bf16_tflops_sustained", 1700.0)
+    path = path_roofline(work, tsum, bf16, bf16_src + "; the pipe that carries the bulk of the mixed path",
+                         "bf16 tensor")
+    path["F_eig_per_run"] = work["F_eig"] / (runs * args.steps)
+    path["F_rot_per_run"] = work["F_rot"] / (runs * args.steps)
+    path["frac_of_fp64_peak"] = path["achieved"] / fp64_peak
+    kt, wc = kernel_profile(engine)
+    rf = roofline_from(kt, wc, fp64_peak)
+    rf["path"] = path
     fallbacks = sum(e.fallback_count() for e in engines)
     hbm_peak = sum(e.memory()[1] for e in engines)
+    sweep = None
+    if args.sweep_runs > 0 and not reduced:
+        sweep = {"instances": args.sweep_runs, "of": 512, "seed": "workloads.SWEEP_SEED",
+                 "what": "RG flows (all eigenvalues per site) of the first instances of the seeded sweep, "
+                         "one heterogeneous batch per engine, one pass after the workload warmed the engines"}
+        t = sweep_pass(engines, args.sweep_runs)
+        sweep["mixed_runs_per_s"] = args.sweep_runs / t
     for e in engines[1:]:
         e.close()
     serving = None
-    if not args.no_serving:
+    if not args.no_serving and not reduced:
         serving = serving_run(engine, 0.8 * runs / per, args.serving_requests)
     engine.close()
-    plain = None
+    plain, got_fp64 = None, None
     if not args.no_fp64:
         e64s = [api.Engine(api.PREC_FP64, device=local) for _ in range(ENGINES)]
-        flush.zero_()
-        barrier()
-        t0 = time.perf_counter()
-        step(e64s, e2e=False)
-        for e in e64s:
-            e.sync()
-        barrier()
-        t64 = time.perf_counter() - t0
+        _, _, got_fp64 = step(e64s, e2e=False, collect=not reduced)  # warm-up
+        t64s, _, _, work64 = timed_steps(e64s, max(1, args.fp64_steps), False, barrier, flush)
+        t64 = max_over_ranks([sum(t64s)])[0] / len(t64s)
+        kt64, wc64 = kernel_profile(e64s[0])
+        rf64 = roofline_from(kt64, wc64, fp64_peak)
+        p64 = path_roofline(work64, sum(t64s), fp64_peak, "of measured (cuBLAS DGEMM 8192^3 in this run)",
+                            "fp64")
+        p64["F_eig_per_run"] = work64["F_eig"] / (runs * len(t64s))
+        p64["F_rot_per_run"] = work64["F_rot"] / (runs * len(t64s))
+        rf64["path"] = p64
+        if sweep is not None:
+            sweep["fp64_runs_per_s"] = args.sweep_runs / sweep_pass(e64s, args.sweep_runs)
+            sweep["speedup_mixed_over_fp64"] = sweep["mixed_runs_per_s"] / sweep["fp64_runs_per_s"]
         for e in e64s:
             e.close()
         plain = {"value": ws * runs / t64, "unit": "runs/s", "ms_per_step": t64 * 1e3,
-                 "speedup_mixed_over_fp64": value / (ws * runs / t64)}
+                 "steps": len(t64s), "warmup": 1, "speedup_mixed_over_fp64": value / (ws * runs / t64),
+                 "fp64_peak_tflops": fp64_peak, "fp64_peak_source": "cuBLAS DGEMM 8192^3 via torch.matmul, "
+                 "best of 5, CUDA events (this run)", "roofline": rf64,
+                 "kernels_ms_per_engine_batch": {k: round(v[0], 3) for k, v in kt64.items()}}
+    errors = None
+    if got_mixed is not None:
+        e0 = api.Engine(api.PREC_FP64, device=local)
+        errors = output_errors(e0, got_mixed, got_fp64)
+        e0.close()
     cpu = None
-    if rank == 0 and ws == 1:
-        sites = max(1, min(args.cpu_sites, WORK["nsites"]))
-        tc = time_oracle_run(sites)
-        cpu = {"value": 1.0 / tc, "unit": "runs/s (of the sample)", "cores": cpu_cores(), "kind": "port",
-               "sample": "numpy oracle, same model, forward %d of 50 sites + FDM backward "
-                         "(%.1f s); runs/s of that truncated run" % (sites, tc)}
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        cb = CpuBaseline(args.cpu_sites)
+        try:
+            cpu = cb.best()
+        finally:
+            cb.close()
     if rank == 0:
-        line = {"metric": METRIC, "value": value, "unit": "runs/s", "n_gpus": ws, "steps": args.steps,
+        cfg = dict(config(), precision_path="mixed: FP32 block solve + FP64-accurate refinement on "
+                                            "tensor cores; FP64 for refinement, rescale and Boltzmann sums")
+        if reduced:
+            cfg["workload"] += "_reduced_for_profiling"
+            cfg["sites"] = WORK["nsites"]
+        line = {"metric": metric(), "value": value, "unit": "runs/s", "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": per * 1e3, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64 (mixed)",
                 "data": "synthetic (model parameters of the workload; no dataset)",
-                "config": dict(CONFIG, precision_path="mixed: FP32 block solve + FP64-accurate refinement"),
-                "gpu_launches": launches,
-                "fp64_fallback_blocks": fallbacks,
+                "config": cfg, "gpu_launches": launches, "fp64_fallback_blocks": fallbacks,
                 "hbm_peak_bytes": hbm_peak,
-                "e2e": {"value": e2e_v, "unit": "runs/s", "h2d_bytes_per_step": int(h2d),
+                "e2e": {"value": e2e_v, "unit": "runs/s", "steps": len(e2e_times), "h2d_bytes_per_step": int(h2d),
                         "d2h_bytes_per_step": int(d2h)},
-                "serving": serving, "plain_fp64": plain, "roofline": rf,
+                "plain_fp64": plain, "error": errors, "sweep": sweep, "serving": serving, "roofline": rf,
                 "kernels_ms_per_engine_batch": {k: round(v[0], 3) for k, v in kt.items()},
                 "kernels_profiled": "one engine's %d-run batch alone, per-kernel CUDA events on its stream"
                                     % BATCH,
-                "cpu_baseline": cpu, "clocks": clk.summary()}
+                "cpu_baseline": cpu, "clocks": clocks}
         print(json.dumps(line))
     if ws > 1:
         torch.distributed.destroy_process_group()

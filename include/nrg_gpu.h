@@ -120,6 +120,13 @@ int nrg_engine_set_profiling(nrg_engine *eng, int on);
  * written.  Clears the record. */
 int nrg_engine_kernel_times(nrg_engine *eng, char *names, uint64_t names_cap, double *ms,
                             double *work, uint64_t *count, int cap, int *nk);
+/* Algorithmic work of the steps issued since the last reset (no counterpart
+ * in the reference): out[0] F_eig = sum (10/3) n^3 over the blocks solved,
+ * out[1] F_rot = sum 2 n_i n_j min(n_i, n_j) over the non-empty f-dagger
+ * blocks (operator, i, j) of each new basis, out[2] the FP64-accurate
+ * tensor-core GEMM work (2MNK per product), out[3] the bf16 tensor-pipe
+ * flops it took (2MNK per digit-plane product); n = entries written. */
+int nrg_engine_work_counters(nrg_engine *eng, double *out, int cap, int *n, int reset);
 int nrg_engine_sync(nrg_engine *eng);
 
 /* ---- one NRG run (nrgcore<Imp,Bath>) ---------------------------------- */
@@ -210,9 +217,10 @@ int nrg_broaden(nrg_engine *eng, const double *energies, const double *weights, 
  *   NRG_BROADEN_NOALLOC_MAX_BINS doubles (1 MiB); nbins above that is
  *   rejected with NRG_E_ARG.  No buffer has to start at zero: each call
  *   writes the nbins scratch entries it reads and every out[k].
- * - The current device is used; its first call looks up the scratch address
- *   (cudaGetSymbolAddress), which may load the kernels' module.  Make that
- *   first call on each device before any stream capture begins.
+ * - The current device is used.  Every call looks up the scratch address
+ *   with that device current (cudaGetSymbolAddress; no address is cached,
+ *   so a cudaDeviceReset between calls is safe); the first call on a device
+ *   may load the kernels' module, so make it before any stream capture.
  * - Asynchronous: the kernels are enqueued on `stream` (a cudaStream_t;
  *   NULL = the legacy default stream) and the call returns; read `out` after
  *   that stream has completed.  All pointers must stay valid until then.

@@ -58,8 +58,8 @@ class RunInfo(C.Structure):
 
 EXPORTS = [
     "nrg_last_error", "nrg_engine_create", "nrg_engine_destroy", "nrg_engine_phase_times",
-    "nrg_engine_launch_count", "nrg_engine_get_opts", "nrg_engine_fallback_count", "nrg_engine_memory", "nrg_engine_set_profiling",
-    "nrg_engine_kernel_times",
+    "nrg_engine_launch_count", "nrg_engine_get_opts", "nrg_engine_fallback_count", "nrg_engine_memory",
+    "nrg_engine_set_profiling", "nrg_engine_kernel_times", "nrg_engine_work_counters",
     "nrg_engine_sync", "nrg_run_create", "nrg_run_destroy",
     "nrg_run_set_parameters", "nrg_run_set_bath", "nrg_run_add_site", "nrg_run_update_state",
     "nrg_run_check_discarded", "nrg_run_get_info", "nrg_run_get_all_eigenvalues",
@@ -184,6 +184,14 @@ class Engine:
         v = C.c_uint64()
         _call(lib().nrg_engine_fallback_count, self.h, C.byref(v))
         return v.value
+
+    def work_counters(self, reset=False):
+        """Algorithmic work since the last reset: {'F_eig', 'F_rot',
+        'tc_useful', 'tc_bf16'} in flops (nrg_engine_work_counters)."""
+        out = (C.c_double * 4)()
+        n = C.c_int()
+        _call(lib().nrg_engine_work_counters, self.h, out, 4, C.byref(n), int(reset))
+        return dict(zip(("F_eig", "F_rot", "tc_useful", "tc_bf16"), list(out)[:n.value]))
 
     def sync(self):
         _call(lib().nrg_engine_sync, self.h)

@@ -13,6 +13,8 @@
 // the reference keeps them, but never reach the device.
 #include <algorithm>
 #include <map>
+#include <mutex>
+#include <set>
 #include <tuple>
 #include <unordered_map>
 #include <cmath>
@@ -135,6 +137,19 @@ void check_kernel_error(nrg_engine *e) {
 }
 
 static void post_launch(const char *what) { check_cuda(cudaGetLastError(), what); }
+
+void ensure_smem_limit(const void *kernel, int bytes) {
+  static std::mutex mu;
+  static std::set<std::tuple<const void *, int, int>> done;  // (kernel, device, bytes)
+  int dev = 0;
+  check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
+  std::lock_guard<std::mutex> lk(mu);
+  const auto key = std::make_tuple(kernel, dev, bytes);
+  if (done.count(key)) return;
+  check_cuda(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes),
+             "cudaFuncSetAttribute(dynamic shared memory)");
+  done.insert(key);
+}
 
 // ---------------------------------------------------------------- models
 static SiteModel parse_site(const nrg_site_desc *d, bool need_chi) {
@@ -523,6 +538,7 @@ void OzList::out(double *C, int ldc, int M, int N, bool acc, const std::vector<O
   for (auto &c : cs) {
     contribs.push_back(c);
     flops += 2.0 * M * N * double(c.K) * pairs;
+    useful += 2.0 * M * N * double(c.K);
   }
   g.c1 = int(contribs.size());
   const int gi = int(groups.size());
@@ -565,7 +581,9 @@ void OzList::launch(nrg_engine *e, std::vector<DevPtr> &hold) {
   DevPtr d;
   char *p = a.push(e, d);
   hold.push_back(d);
-  Prof pf(e, "k_gemm_oz", flops);
+  e->work[2] += useful;
+  e->work[3] += flops;
+  Prof pf(e, "k_gemm_oz", useful);
   launch_gemm_oz(at<GemmTile>(p, ot), int(tiles.size()), at<OzGroup>(p, og), at<OzContrib>(p, oc),
                  at<OzTensorMap>(p, om), e->d_kerr, e->stream);
   count_launch(e);
@@ -962,6 +980,7 @@ static void batch_add_site(nrg_run *const *runs, int nruns, const double *t, int
   std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return eblk[a].n > eblk[b].n; });
   std::vector<EigBlock> eblk_sorted;
   for (int o : order) eblk_sorted.push_back(eblk[o]);
+  e->work[0] += eig_flops(eblk);
   elem_block.insert(elem_block.end(), block_run.begin(), block_run.end());
 
   Arena ar;
@@ -1125,6 +1144,8 @@ static void batch_add_site(nrg_run *const *runs, int nruns, const double *t, int
     for (auto &kv : outs) {
       const int si = std::get<1>(kv.first), sj = std::get<2>(kv.first);
       fsz += r->kept_new[si] * r->kept_new[sj];
+      const double ni = sd.sectors[si].n, nj = sd.sectors[sj].n;
+      e->work[1] += 2.0 * ni * nj * std::min(ni, nj);
     }
     r->fcur_mem = dalloc(e, fsz * sizeof(double) + 8);
     r->fcur.clear();

@@ -695,6 +695,17 @@ int nrg_engine_fallback_count(nrg_engine *e, uint64_t *out) {
   });
 }
 
+int nrg_engine_work_counters(nrg_engine *e, double *out, int cap, int *n, int reset) {
+  return guard([&] {
+    if (!e || !out || !n || cap < 0) fail(NRG_E_ARG, "null argument");
+    const int k = std::min(cap, 4);
+    for (int i = 0; i < k; ++i) out[i] = e->work[i];
+    *n = k;
+    if (reset)
+      for (double &w : e->work) w = 0.0;
+  });
+}
+
 int nrg_engine_sync(nrg_engine *e) {
   return guard([&] {
     if (!e) fail(NRG_E_ARG, "null engine");

@@ -113,7 +113,8 @@ struct OzList {
   std::vector<OzGroup> groups;
   std::vector<OzContrib> contribs;
   std::vector<GemmTile> tiles;
-  double flops = 0;  // bf16 tensor flops: 2MNK per digit-plane product
+  double flops = 0;   // bf16 tensor-pipe flops: 2MNK per digit-plane product
+  double useful = 0;  // FP64-accurate work: 2MNK per contribution
   int planes = kDigitPlanes;  // digit planes of the products (fewer: a cheaper, less exact product)
   // upper: only the tiles that meet the upper triangle (symmetric outputs whose
   // readers use the upper triangle)
@@ -156,6 +157,13 @@ struct nrg_engine {
   std::deque<PinnedSpan> ring_busy;
   std::vector<cudaEvent_t> ring_events;
   uint64_t fallback_blocks = 0;  // mixed path: blocks re-solved in FP64
+  // algorithmic work since the last read (nrg_engine_work_counters):
+  // [0] F_eig = sum (10/3) n^3 over solved blocks, [1] F_rot = sum
+  // 2 n_i n_j min(n_i, n_j) over non-empty f-dagger blocks (i, j) of each
+  // operator, [2] FP64-accurate tensor-core GEMM work (2MNK per
+  // contribution), [3] the bf16 tensor-pipe flops that work took (2MNK per
+  // digit-plane product)
+  double work[4] = {0, 0, 0, 0};
   // mixed path: FP64-accurate GEMMs on the tensor cores, bit 0 for the
   // eigenvector refinement, bit 1 for the operator rotations
   int ozaki = 3;

@@ -791,10 +791,7 @@ template <typename T>
 void launch(const EigBlock *blocks, int nblocks, int max_n, int max_n_smem, int *status,
             cudaStream_t s, const int *gate = nullptr) {
   if (nblocks == 0) return;
-  // once per process, thread-safe (engines may launch from several threads)
-  static const bool configured =
-      (cudaFuncSetAttribute(k_eig<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes), true);
-  (void)configured;
+  ensure_smem_limit(reinterpret_cast<const void *>(k_eig<T>), kSmemBytes);
   // enough shared memory for the largest block of this launch
   size_t bytes = smem_bytes<T>(max_n, max_n <= max_n_smem);
   if (max_n > max_n_smem) bytes = std::max(bytes, smem_bytes<T>(max_n_smem, true));
@@ -825,10 +822,7 @@ void launch_eig_f64(const EigBlock *blocks, int nblocks, int max_n, int max_n_sm
 void launch_eig_bisect_f32(const EigBlock *blocks, int nblocks, int max_n, int max_n_smem,
                            cudaStream_t s) {
   if (nblocks == 0) return;
-  // once per process, thread-safe (engines may launch from several threads)
-  static const bool configured =
-      (cudaFuncSetAttribute(k_eig_bi, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes), true);
-  (void)configured;
+  ensure_smem_limit(reinterpret_cast<const void *>(k_eig_bi), kSmemBytes);
   size_t bytes = smem_bytes<float>(max_n, max_n <= max_n_smem);
   if (max_n > max_n_smem) bytes = std::max(bytes, smem_bytes<float>(max_n_smem, true));
   if (bytes > size_t(kSmemBytes)) bytes = kSmemBytes;
@@ -855,10 +849,7 @@ int reflect_max_n() {
 
 template <int TW> static void reflect_launch(const EigBlock *blocks, const int2 *tiles, int ntiles, int panel,
                                              size_t bytes, cudaStream_t s) {
-  // once per process, thread-safe (engines may launch from several threads)
-  static const bool cfg =
-      (cudaFuncSetAttribute(k_reflect<TW>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kReflectSmem)), true);
-  (void)cfg;
+  ensure_smem_limit(reinterpret_cast<const void *>(k_reflect<TW>), int(kReflectSmem));
   k_reflect<TW><<<ntiles, 256, bytes, s>>>(blocks, tiles, panel);
 }
 

@@ -500,10 +500,7 @@ void launch_split_grid(const SplitTask *tasks, const int64_t *chunk0, int ntasks
 void launch_gemm_oz(const GemmTile *tiles, int ntiles, const OzGroup *groups, const OzContrib *contribs,
                     const OzTensorMap *maps, int *err, cudaStream_t s) {
   if (ntiles == 0) return;
-  // once per process, thread-safe (engines may launch from several threads)
-  static const bool cfg =
-      (cudaFuncSetAttribute(k_gemm_oz, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kGemmSmem)), true);
-  (void)cfg;
+  ensure_smem_limit(reinterpret_cast<const void *>(k_gemm_oz), int(kGemmSmem));
   k_gemm_oz<<<ntiles, kTcThreads, kGemmSmem, s>>>(tiles, groups, contribs, maps, err);
 }
 

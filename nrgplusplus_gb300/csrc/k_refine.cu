@@ -245,20 +245,14 @@ int refine_max_n() {
 void launch_oa_update(const RefineBlock *blocks, int nblocks, int max_n, double tau_rel,
                       cudaStream_t s) {
   if (nblocks == 0) return;
-  // once per process, thread-safe (engines may launch from several threads)
-  static const bool cfg =
-      (cudaFuncSetAttribute(k_oa_update, cudaFuncAttributeMaxDynamicSharedMemorySize, 225 * 1024), true);
-  (void)cfg;
+  ensure_smem_limit(reinterpret_cast<const void *>(k_oa_update), 225 * 1024);
   k_oa_update<<<nblocks, kThreads, sizeof(double) * size_t(max_n) + 16, s>>>(blocks, tau_rel);
 }
 
 void launch_oa_final(const RefineBlock *blocks, int nblocks, int max_n, double tau_rel, int *status,
                      cudaStream_t s) {
   if (nblocks == 0) return;
-  // once per process, thread-safe (engines may launch from several threads)
-  static const bool cfg =
-      (cudaFuncSetAttribute(k_oa_final, cudaFuncAttributeMaxDynamicSharedMemorySize, 225 * 1024), true);
-  (void)cfg;
+  ensure_smem_limit(reinterpret_cast<const void *>(k_oa_final), 225 * 1024);
   k_oa_final<<<nblocks, kThreads, final_smem(max_n), s>>>(blocks, tau_rel, status);
 }
 

@@ -6,7 +6,6 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
-#include <mutex>
 #include <string>
 
 #include "nrg_gpu.h"
@@ -23,10 +22,6 @@ static __device__ __align__(256) double g_broaden_lnE[NRG_BROADEN_NOALLOC_MAX_BI
 
 namespace {
 
-constexpr int kMaxDevices = 64;
-std::mutex g_mu;
-double *g_scratch[kMaxDevices] = {};  // device address of g_broaden_lnE, per device
-
 __global__ void k_log_energies(const double *__restrict__ e, const double *__restrict__ w, int64_t n,
                                double *__restrict__ le) {
   for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
@@ -38,22 +33,19 @@ struct Fail {
   std::string msg;
 };
 
-// Device address of the scratch on the current device, looked up once per
-// device (cudaGetSymbolAddress with that device current).
+// Device address of the scratch on the current device.  Looked up with the
+// caller's device current on every call rather than cached: after a
+// cudaDeviceReset (or any re-creation of the primary context) the module is
+// loaded again and the array may move, so a cached address could point at
+// freed memory.  Once the module is loaded the lookup is a table search.
 double *scratch_for_current_device() {
-  int dev = -1;
-  cudaError_t rc = cudaGetDevice(&dev);
-  if (rc != cudaSuccess) throw Fail{NRG_E_NOCUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(rc)};
-  if (dev < 0 || dev >= kMaxDevices) throw Fail{NRG_E_ARG, "device ordinal out of range"};
-  std::lock_guard<std::mutex> lk(g_mu);
-  if (!g_scratch[dev]) {
-    void *p = nullptr;
-    rc = cudaGetSymbolAddress(&p, g_broaden_lnE);
-    if (rc != cudaSuccess || !p)
-      throw Fail{NRG_E_CUDA, std::string("cudaGetSymbolAddress(broaden scratch): ") + cudaGetErrorString(rc)};
-    g_scratch[dev] = static_cast<double *>(p);
-  }
-  return g_scratch[dev];
+  void *p = nullptr;
+  const cudaError_t rc = cudaGetSymbolAddress(&p, g_broaden_lnE);
+  if (rc == cudaErrorNoDevice || rc == cudaErrorInsufficientDriver)
+    throw Fail{NRG_E_NOCUDA, std::string("cudaGetSymbolAddress(broaden scratch): ") + cudaGetErrorString(rc)};
+  if (rc != cudaSuccess || !p)
+    throw Fail{NRG_E_CUDA, std::string("cudaGetSymbolAddress(broaden scratch): ") + cudaGetErrorString(rc)};
+  return static_cast<double *>(p);
 }
 
 }  // namespace

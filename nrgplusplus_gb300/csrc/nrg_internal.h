@@ -8,6 +8,12 @@
 
 namespace nrg {
 
+// Raises `kernel`'s dynamic shared-memory limit to `bytes` on the current
+// device.  cudaFuncSetAttribute applies per device, so this runs once per
+// (kernel, device) pair, thread-safe; throws the engine's error (NRG_E_CUDA)
+// when the runtime refuses.
+void ensure_smem_limit(const void *kernel, int bytes);
+
 // ---------------------------------------------------------------- assembly
 // One device block = one non-empty (Q,Sz) sector of one run.
 struct AsmBlock {

@@ -114,3 +114,53 @@ def siam_request(nkeep, nsites, lam, V, eps=-0.25, U=0.5, fdm=False, thermo=Fals
                 ops=M.d_dag_chi() if fdm else None, fdm=fdm,
                 temps=temperature_grid() if thermo else None, shell_scale=np.array(scale),
                 first_shell_site=1, keep_eigenvalues=keep_eigs)
+
+
+SWEEP_SEED = 20260512
+
+
+def sweep_instances(n=512, seed=SWEEP_SEED):
+    """The seeded SIAM parameter sweep: U ~ U[0.05, 1.0], eps_d = -U/2 +
+    U[-0.1, 0.1], V log-uniform on [0.03, 0.3], Lambda in {2, 2.5, 3}, Nkeep
+    in {256, 512, 1024, 2048}, 30-60 Wilson sites (both ends included).  Each
+    instance is an rgflowSIAM-form run (examples/rgflowSIAM/main.cpp:27-42):
+    the V site, then `nsites` Wilson sites, all eigenvalues per iteration."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n):
+        U = float(rng.uniform(0.05, 1.0))
+        eps = -0.5 * U + float(rng.uniform(-0.1, 0.1))
+        V = float(math.exp(rng.uniform(math.log(0.03), math.log(0.3))))
+        lam = float((2.0, 2.5, 3.0)[rng.integers(0, 3)])
+        nkeep = int((256, 512, 1024, 2048)[rng.integers(0, 4)])
+        nsites = int(rng.integers(30, 61))
+        out.append(dict(U=U, eps=eps, V=V, lam=lam, nkeep=nkeep, nsites=nsites))
+    return out
+
+
+def run_flow_batch(engine, instances, keep_eigs=True):
+    """RG flows of several SIAM instances (sweep_instances entries: eps, U,
+    V, lam, nkeep, nsites) stepped together through the batched API: one
+    launch per phase covers the blocks of every run still running, whatever
+    its Lambda, Nkeep or length.  Returns per instance the list of
+    all_eigenvalue arrays (V site excluded) and kept counts, as run_nrg does."""
+    runs = [api.NrgCore(engine, M.spinhalf(p["eps"], p["U"]), M.spinhalf(0.0, 0.0), p["nkeep"])
+            for p in instances]
+    out = [{"eig": [], "kept": []} for _ in instances]
+    try:
+        api.batch_add_site(runs, [[p["V"]] * 2 for p in instances], [1.0] * len(runs))
+        api.batch_update_state(runs)
+        for it in range(max(p["nsites"] for p in instances)):
+            act = [k for k, p in enumerate(instances) if it < p["nsites"]]
+            rs = [runs[k] for k in act]
+            api.batch_add_site(rs, [[M.hopping(it, instances[k]["lam"])] * 2 for k in act],
+                               [math.sqrt(instances[k]["lam"]) if it > 0 else 1.0 for k in act])
+            api.batch_update_state(rs)
+            if keep_eigs:
+                for k in act:
+                    out[k]["eig"].append(runs[k].all_eigenvalue)
+                    out[k]["kept"].append(runs[k].kept_counts)
+    finally:
+        for r in runs:
+            r.close()
+    return out

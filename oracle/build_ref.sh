@@ -21,6 +21,10 @@ PY
 )"
 if [ -z "$BLAS" ]; then echo "build_ref: scipy OpenBLAS not found" >&2; exit 1; fi
 mkdir -p "$OUT"
+if [ -x "$OUT/ref_nrg" ] && [ -z "$(find "$HERE/drivers" "$HERE/shim" "$HERE/build_ref.sh" -newer "$OUT/ref_nrg" -print -quit)" ]; then
+  echo "build_ref: $OUT/ref_nrg is up to date"
+  exit 0
+fi
 g++ -std=c++20 -O3 -fopenmp -w \
   -I"$HERE/shim" -I"$REF/nrgcore/include" \
   "$HERE/drivers/ref_nrg.cpp" "$REF/nrgcore/src/models/twoChannel.cpp" \

@@ -9,13 +9,15 @@ Two sources, both the reference's own numbers:
    (oracle/_ref/ref_nrg), for the workloads named in each case below.
 
 Run from the repository root after ``oracle/build_ref.sh``:
-    python tests/golden/make_golden.py
-Needs the reference tree (default /root/reference or $NRG_REF_ROOT); the
-fixtures it writes are committed so nothing else needs the tree.
+    NRG_REF_ROOT=<reference tree> python tests/golden/make_golden.py [names]
+The shipped .h5 datasets are read from $NRG_REF_ROOT; the fixtures it writes
+are committed so nothing else needs the tree.  Every iteration's eigenvalue
+array is stored whole (``eig<i>``), with its count and sum.
 """
 import os
 import subprocess
 import sys
+import tempfile
 
 import numpy as np
 
@@ -27,21 +29,25 @@ sys.path.insert(0, HERE)
 from h5mini import H5Mini  # noqa: E402
 from oracle.refio import read_named_arrays  # noqa: E402
 
-REF = os.environ.get("NRG_REF_ROOT", "/root/reference")
+REF = os.environ.get("NRG_REF_ROOT", "")
 BIN = os.path.join(ROOT, "oracle", "_ref", "ref_nrg")
-HEAD = 256  # lowest eigenvalues kept per iteration in the fixtures
+
+
+def _eig_entries(out, tag, e):
+    out["eig%s" % tag] = e
+    out["eig_count%s" % tag] = np.array([e.size])
+    out["eig_sum%s" % tag] = np.array([np.sum(e)])
 
 
 def shipped_h5():
+    if not REF:
+        raise SystemExit("set NRG_REF_ROOT to the reference tree")
     for tag, fn in (("kondo_J0.25", "resultsJ0.250000.h5"), ("kondo_zero", "resultsZero.h5")):
         h = H5Mini(os.path.join(REF, "examples", "entropyKondo", fn))
         out = {}
         n = 0
         while "Eigenvalues%d" % n in h.datasets:
-            e = h.read("Eigenvalues%d" % n)
-            out["eig_head%d" % n] = e[:HEAD]
-            out["eig_count%d" % n] = np.array([e.size])
-            out["eig_sum%d" % n] = np.array([np.sum(e)])
+            _eig_entries(out, n, h.read("Eigenvalues%d" % n))
             n += 1
         out["niter"] = np.array([n])
         for k in ("temperatureArray", "entropy", "specificHeat"):
@@ -51,24 +57,23 @@ def shipped_h5():
 
 
 def run_ref(model, name, **kw):
-    path = os.path.join(ROOT, "_work", "golden_tmp_%s.bin" % name)
-    os.makedirs(os.path.dirname(path), exist_ok=True)
-    args = [BIN, model, path] + ["%s=%r" % (k, v) for k, v in kw.items()]
-    env = dict(os.environ, OMP_NUM_THREADS="8", OPENBLAS_NUM_THREADS="8")
-    subprocess.run(args, check=True, stdout=subprocess.DEVNULL, env=env)
-    d = read_named_arrays(path)
-    os.remove(path)
-    return d
+    threads = os.environ.get("NRG_REF_THREADS", "8")
+    env = dict(os.environ, OMP_NUM_THREADS=threads, OPENBLAS_NUM_THREADS=threads)
+    with tempfile.TemporaryDirectory() as tmp:
+        path = os.path.join(tmp, "%s.bin" % name)
+        args = [BIN, model, path] + ["%s=%r" % (k, v) for k, v in kw.items()]
+        subprocess.run(args, check=True, stdout=subprocess.DEVNULL, env=env)
+        return read_named_arrays(path)
 
 
-def pack_run(d, with_ops=False, with_fdm=False, with_thermo=False):
+def pack_run(d, with_ops=False, with_fdm=False, with_thermo=False, full_eigs=True):
     out = {}
     iters = sorted(int(k[len("Eigenvalues"):]) for k in d
                    if k.startswith("Eigenvalues") and k[len("Eigenvalues"):].isdigit())
     out["niter"] = np.array([len(iters)])
     for i in iters:
         e = d["Eigenvalues%d" % i]
-        out["eig_head%d" % i] = e[:HEAD]
+        _eig_entries(out, i, e if full_eigs else e[:64])
         out["eig_count%d" % i] = np.array([e.size])
         out["eig_sum%d" % i] = np.array([np.sum(e)])
         out["kept%d" % i] = d["kept%d" % i].astype(np.int64)
@@ -106,9 +111,17 @@ CASES = [
     ("ref_c2_siam_fdm_nk1024", "siam",
      dict(eps=-0.4, U=0.8, V=0.15, **{"lambda": 2.0}, nkeep=1024, nsites=50, fdm=1),
      {"with_fdm": True}),
+    # the same forward run as ref_c2_siam_fdm_nk1024: its eigenvalues are not repeated
     ("ref_c2_siam_thermo_nk1024", "siam",
      dict(eps=-0.4, U=0.8, V=0.15, **{"lambda": 2.0}, nkeep=1024, nsites=50, thermo=1),
-     {"with_thermo": True}),
+     {"with_thermo": True, "full_eigs": False}),
+    # the spectral workload at Nkeep=2048 (40 Wilson sites)
+    ("ref_siam_fdm_nk2048", "siam",
+     dict(eps=-0.4, U=0.8, V=0.15, **{"lambda": 2.0}, nkeep=2048, nsites=40, fdm=1),
+     {"with_fdm": True}),
+    ("ref_siam_thermo_nk2048", "siam",
+     dict(eps=-0.4, U=0.8, V=0.15, **{"lambda": 2.0}, nkeep=2048, nsites=40, thermo=1),
+     {"with_thermo": True, "full_eigs": False}),
     ("ref_kondo_thermo_nk512", "kondo",
      dict(J=0.25, **{"lambda": 2.0}, nkeep=512, nsites=30, thermo=1), {"with_thermo": True}),
     ("ref_twochannel_nk256", "twochannel",
@@ -116,9 +129,27 @@ CASES = [
 ]
 
 
+def sweep_cases(count=6):
+    """RG flows of the first instances of the seeded SIAM sweep
+    (nrgplusplus_gb300.workloads.sweep_instances) with Nkeep <= 1024, each
+    Lambda of the sweep represented."""
+    from nrgplusplus_gb300.workloads import sweep_instances
+    out = []
+    for k, p in enumerate(sweep_instances()):
+        if p["nkeep"] > 1024:
+            continue
+        out.append(("ref_sweep_%03d" % k, "siam",
+                    dict(eps=p["eps"], U=p["U"], V=p["V"], **{"lambda": p["lam"]}, nkeep=p["nkeep"],
+                         nsites=p["nsites"]), {}))
+        if len(out) == count:
+            break
+    return out
+
+
 def main(which=None):
-    shipped_h5()
-    for name, model, params, opts in CASES:
+    if not which:
+        shipped_h5()
+    for name, model, params, opts in CASES + sweep_cases():
         if which and name not in which:
             continue
         d = run_ref(model, name, **params)

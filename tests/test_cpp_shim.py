@@ -11,7 +11,7 @@ import numpy as np
 import pytest
 
 from conftest import ROOT, golden
-from parity import eig_tol
+from parity import check_eigs
 from nrgplusplus_gb300 import models as M
 from nrgplusplus_gb300 import workloads
 
@@ -79,8 +79,5 @@ def test_shim_kondo_against_shipped_fixture(tmp_path):
         entropy = np.frombuffer(f.read(8 * ns), "<f8")
     fx = golden("shipped_kondo_J0.25")
     assert n == 41
-    for i in range(41):
-        h = fx["eig_head%d" % i]
-        assert eigs[i].size == int(fx["eig_count%d" % i][0])
-        assert np.abs(eigs[i][:h.size] - h).max() <= eig_tol(i, 2.0), i
+    check_eigs(fx, eigs, 2.0)
     assert np.abs(entropy - fx["entropy"]).max() < 1e-8

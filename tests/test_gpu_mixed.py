@@ -6,7 +6,7 @@ import numpy as np
 import pytest
 
 from conftest import golden
-from parity import degenerate_weights, eig_tol
+from parity import check_eigs, degenerate_weights, eig_tol, max_rel_cv
 from nrgplusplus_gb300 import api, workloads
 from nrgplusplus_gb300 import models as M
 from oracle.nrg_oracle import FdmSpectrumOracle, NrgOracle, broaden
@@ -37,11 +37,8 @@ def test_mixed_small_against_oracle(mixed_engine):
 def test_mixed_c1_against_reference(mixed_engine):
     fx = golden("ref_c1_siam_nk512")
     out = workloads.run_nrg(mixed_engine, "siam", 512, 40, 2.0, V=0.1, eps=-0.25, U=0.5)
+    check_eigs(fx, out["eig"], 2.0)
     for i in range(40):
-        e = out["eig"][i]
-        assert e.size == int(fx["eig_count%d" % i][0])
-        h = fx["eig_head%d" % i]
-        assert np.abs(e[:h.size] - h).max() <= eig_tol(i, 2.0), (i, np.abs(e[:h.size] - h).max())
         assert np.array_equal(np.array(out["kept"][i]), fx["kept%d" % i]), i
     out["run"].close()
 
@@ -49,12 +46,9 @@ def test_mixed_c1_against_reference(mixed_engine):
 def test_mixed_kondo_against_shipped_fixture(mixed_engine):
     fx = golden("shipped_kondo_J0.25")
     out = workloads.run_nrg(mixed_engine, "kondo", 1024, 41, 2.0, J=0.25, thermo=True)
-    for i in range(41):
-        e = out["eig"][i]
-        h = fx["eig_head%d" % i]
-        assert e.size == int(fx["eig_count%d" % i][0])
-        assert np.abs(e[:h.size] - h).max() <= eig_tol(i, 2.0), i
+    check_eigs(fx, out["eig"], 2.0)
     assert np.abs(out["entropy"] - fx["entropy"]).max() < 1e-8
+    assert max_rel_cv(out["specificHeat"], fx["specificHeat"], fx["temperatureArray"]) < 1e-5
     out["run"].close()
 
 
@@ -77,9 +71,7 @@ def test_mixed_fdm_spectrum_against_reference(mixed_engine):
 def test_mixed_twochannel_against_reference(mixed_engine):
     fx = golden("ref_twochannel_nk256")
     out = workloads.run_nrg(mixed_engine, "twochannel", 256, 8, 4.0, V=0.12, eps=-0.3, U=0.6)
+    check_eigs(fx, out["eig"], 4.0)
     for i in range(8):
-        e = out["eig"][i]
-        h = fx["eig_head%d" % i]
-        assert np.abs(e[:h.size] - h).max() <= eig_tol(i, 4.0), i
         assert np.array_equal(np.array(out["kept"][i]), fx["kept%d" % i]), i
     out["run"].close()

@@ -10,25 +10,17 @@ import numpy as np
 import pytest
 
 from conftest import golden
-from parity import degenerate_weights, eig_tol
+from parity import check_eigs, degenerate_weights, max_rel_cv, stable_sites
 from nrgplusplus_gb300 import models as M
 from oracle.nrg_oracle import (FdmSpectrumOracle, NrgOracle, broaden, siam_run,
                                temperature_grid)
 
 
-def _check_eigs(fx, eigs, lam, offset=0, strict_kept=None):
-    n = int(fx["niter"][0])
-    assert len(eigs) >= n
-    worst = 0.0
-    for i in range(n):
-        e = eigs[i]
-        assert e.size == int(fx["eig_count%d" % i][0]), i
-        h = fx["eig_head%d" % i]
-        d = np.abs(e[:h.size] - h).max()
-        worst = max(worst, d / eig_tol(i + offset, lam))
-        assert d <= eig_tol(i + offset, lam), (i, d)
-        assert abs(e.sum() - fx["eig_sum%d" % i][0]) <= e.size * eig_tol(i + offset, lam) * 10
-    return worst
+def _check_eigs(fx, eigs, lam, offset=0):
+    return check_eigs(fx, eigs, lam, offset)
+
+
+CV_RTOL = 1e-5  # specific heat, max relative error over T >= 2.6e-7
 
 
 @pytest.fixture(scope="module")
@@ -48,9 +40,7 @@ def test_shipped_kondo_thermodynamics(kondo_run):
     assert np.allclose(T, fx["temperatureArray"], rtol=1e-14, atol=0)
     assert np.abs(kondo_run["entropy"] - fx["entropy"]).max() < 1e-8
     # C(T) suffers cancellation at the lowest temperatures (as in the reference itself)
-    m = T >= 2.6e-7
-    rel = np.abs(kondo_run["cv"][m] - fx["specificHeat"][m]) / np.abs(fx["specificHeat"][m])
-    assert np.median(rel) < 1e-6
+    assert max_rel_cv(kondo_run["cv"], fx["specificHeat"], T) < CV_RTOL
 
 
 def test_shipped_free_chain_entropy():
@@ -158,6 +148,19 @@ def test_ref_kondo_thermo_nk512():
                    thermo=True, full_fdag=False)
     _check_eigs(fx, res["eig"], 2.0)
     assert np.abs(res["entropy"] - fx["entropy"]).max() < 1e-8
-    m = fx["temperatureArray"] >= 2.6e-7
-    rel = np.abs(res["cv"][m] - fx["specificHeat"][m]) / np.abs(fx["specificHeat"][m])
-    assert np.median(rel) < 1e-6
+    assert max_rel_cv(res["cv"], fx["specificHeat"], fx["temperatureArray"]) < CV_RTOL
+
+
+@pytest.mark.parametrize("k", [2, 3])
+def test_ref_sweep_instances(k):
+    """Instances of the seeded parameter sweep (Lambda 2.5 and 3) against the
+    reference's runs of them."""
+    from nrgplusplus_gb300.workloads import sweep_instances
+    p = sweep_instances()[k]
+    fx = golden("ref_sweep_%03d" % k)
+    n = min(p["nsites"], stable_sites(p["lam"]))
+    res = siam_run(M.spinhalf(p["eps"], p["U"]), M.spinhalf(0, 0), p["nkeep"], n, p["lam"],
+                   V=p["V"], full_fdag=False)
+    check_eigs(fx, res["eig"], p["lam"], niter=n)
+    for i in range(n):
+        assert np.array_equal(np.array(res["kept"][i]), fx["kept%d" % i]), i

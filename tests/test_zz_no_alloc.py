@@ -65,6 +65,52 @@ def test_noalloc_broaden_matches_broaden(gpu_engine, torch_cuda, nbins):
     assert np.array_equal(outs[0], outs[1])
 
 
+def _noalloc(torch, e, w, om, b=0.6):
+    """One nrg_broaden_noalloc call on device copies of e, w, om (empty
+    arrays pass a valid dummy pointer); returns out on the host."""
+    dummy = torch.zeros(1, dtype=torch.float64, device="cuda")
+
+    def dev(a):
+        return torch.tensor(a, dtype=torch.float64, device="cuda") if len(a) else dummy
+
+    de, dw, dom = dev(e), dev(w), dev(om)
+    dout = torch.full((max(len(om), 1),), float("nan"), dtype=torch.float64, device="cuda")
+    api.broaden_noalloc(de.data_ptr(), dw.data_ptr(), len(e), dom.data_ptr(), len(om), b,
+                        dout.data_ptr(), torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    return dout.cpu().numpy()[:len(om)]
+
+
+@pytest.mark.parametrize("case", ["no_bins", "no_omegas", "zero_energy_empty_bin",
+                                  "zero_energy_weighted_bin"])
+def test_noalloc_broaden_edge_cases(gpu_engine, torch_cuda, case):
+    """Empty inputs and a bin at energy 0 give what nrg_broaden gives: no
+    bins -> all zeros; no frequencies -> nothing written; a zero-weight bin
+    at e = 0 is skipped (ln 0 is never used); a weighted bin at e = 0 follows
+    nrg_broaden's arithmetic, non-finite values included."""
+    om = np.logspace(-8, 0, 81)
+    e, w = _histogram(64, 5)
+    if case == "no_bins":
+        e, w = e[:0], w[:0]
+    elif case == "no_omegas":
+        om = om[:0]
+    else:
+        e = e.copy()
+        w = w.copy()
+        e[3] = 0.0
+        w[3] = 0.0 if case == "zero_energy_empty_bin" else 1e-3
+    ref = gpu_engine.broaden(e, w, om, 0.6)
+    got = _noalloc(torch_cuda, e, w, om)
+    assert got.shape == ref.shape
+    if case == "no_bins":
+        assert np.array_equal(got, np.zeros(om.size))
+    fin = np.isfinite(ref)
+    assert np.array_equal(fin, np.isfinite(got))
+    if fin.any():
+        scale = max(np.abs(ref[fin]).max(), 1e-300)
+        assert np.abs(got[fin] - ref[fin]).max() <= RTOL * scale
+
+
 def test_noalloc_broaden_rejects_oversize(torch_cuda):
     torch = torch_cuda
     buf = torch.zeros(16, dtype=torch.float64, device="cuda")

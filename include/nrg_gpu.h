@@ -199,6 +199,20 @@ int nrg_fdm_calc(nrg_fdm *f, double energy_scale);               /* calcSpectrum
  * its snapshot loaded, in shared launches (one per phase); same results as
  * n nrg_fdm_calc calls.  No counterpart in the reference (it runs one). */
 int nrg_fdm_calc_batch(nrg_fdm *const *fdms, int n, const double *energy_scales);
+/* Finite temperature T (fdmSpectrum is T = 0 only, fdmSpectrum.hpp:27,284):
+ * every shell's density matrix takes the Boltzmann weights of its discarded
+ * states on the diagonal, the form fdmBackwardIteration::setRhoZero(
+ * tBoltzmannFactor) takes (dynamics/fdmBackwardIteration.hpp:207-239), with
+ * the weights the thermodynamics average with (w_m exp((E0_m - E)/T) / Z'_m,
+ * fdmThermodynamics.hpp:159-218).  `thermo` must already have seen, in the
+ * same backward order and energy scales, every shell this object will see
+ * (nrg_thermo_calc per shell).  Call before the first nrg_fdm_calc. */
+int nrg_fdm_set_temperature(nrg_fdm *f, double T, nrg_thermo *thermo);
+/* rhoDotStaticOperators (fdmBackwardIteration.hpp:166-199) summed over the
+ * shells computed so far: per operator, Tr(O_ii rho_i) over its diagonal
+ * blocks with the kept x kept part of O left out; <O>(T) after the whole
+ * backward pass at finite temperature. */
+int nrg_fdm_get_static(nrg_fdm *f, double *out, int nops);
 /* saveFinalData (:322-337): energy points and the positive/negative weights,
  * each nops x npts; npts = 100000 */
 int nrg_fdm_get(nrg_fdm *f, double *energy_points, double *positive, double *negative,
@@ -238,6 +252,14 @@ int nrg_thermo_create(nrg_run *run, const double *temps, int nt, nrg_thermo **ou
 int nrg_thermo_destroy(nrg_thermo *t);
 int nrg_thermo_calc(nrg_thermo *t, double energy_scale);        /* calcThermodynamics :42-89 */
 int nrg_thermo_final(nrg_thermo *t, double *entropy, double *specific_heat); /* :101-236 */
+/* setSystemOperator (:37-39): the operators op_index[0..n) (n <= 8) of the
+ * operator set saved with each snapshot (nrg_run_snapshot) are the system
+ * operators; calcThermodynamics keeps their (i, i) diagonals on the
+ * discarded states (:63-88) and nrg_thermo_final averages them
+ * (qsysOPeratorExpValue, :200-218).  Call before the first calc. */
+int nrg_thermo_set_operator(nrg_thermo *t, const int *op_index, int n);
+/* qsysOPeratorExpValue after nrg_thermo_final: n x nt values, row per operator. */
+int nrg_thermo_get_operator(nrg_thermo *t, double *out, int n, int nt);
 
 /* ---- standalone batched symmetric eigensolver --------------------------- */
 /* The block solver behind qmatrix::diag (qmatrix.hpp:375-404, LAPACKE_dsyevd

@@ -68,7 +68,8 @@ EXPORTS = [
     "nrg_opset_create", "nrg_opset_destroy", "nrg_opset_update", "nrg_opset_update_batch", "nrg_opset_get_block",
     "nrg_run_snapshot", "nrg_run_load_snapshot", "nrg_fdm_create", "nrg_fdm_destroy",
     "nrg_fdm_calc", "nrg_fdm_calc_batch", "nrg_fdm_get", "nrg_broaden", "nrg_thermo_create", "nrg_thermo_destroy",
-    "nrg_thermo_calc", "nrg_thermo_final", "nrg_batch_add_site", "nrg_batch_update_state",
+    "nrg_thermo_calc", "nrg_thermo_final", "nrg_thermo_set_operator", "nrg_thermo_get_operator",
+    "nrg_fdm_set_temperature", "nrg_fdm_get_static", "nrg_batch_add_site", "nrg_batch_update_state",
     "nrg_eigh_batched", "nrg_dgemm_tc", "nrg_broaden_noalloc",
     "nrg_server_create", "nrg_server_destroy", "nrg_server_submit", "nrg_server_wait",
     "nrg_server_result_info", "nrg_server_get_result", "nrg_server_release", "nrg_server_stats",
@@ -488,7 +489,8 @@ class NrgData:
 
 
 class FdmSpectrum:
-    """fdmSpectrum<N> at T = 0 (dynamics/fdmSpectrum.hpp)."""
+    """fdmSpectrum<N> (dynamics/fdmSpectrum.hpp): T = 0 as the reference, or
+    at a finite temperature after setTemperature(T, thermodynamics)."""
 
     def __init__(self, run, nops):
         self.run = run
@@ -497,8 +499,22 @@ class FdmSpectrum:
         _call(lib().nrg_fdm_create, run.h, nops, C.byref(self.h))
         run.engine._adopt(self)
 
+    def setTemperature(self, T, thermodynamics):
+        """Finite-temperature density matrix: each shell's discarded states
+        get the Boltzmann weights at T that `thermodynamics` (an
+        FdmThermodynamics that has already seen every shell of this backward
+        pass) averages with (nrg_fdm_set_temperature)."""
+        _call(lib().nrg_fdm_set_temperature, self.h, C.c_double(T), thermodynamics.h)
+
     def calcSpectrum(self, energy_scale):
         _call(lib().nrg_fdm_calc, self.h, C.c_double(energy_scale))
+
+    def staticExpectation(self):
+        """rhoDotStaticOperators summed over the shells so far, per operator
+        (<O> at the temperature of the density matrix)."""
+        out = np.zeros(self.nops)
+        _call(lib().nrg_fdm_get_static, self.h, _dp(out), self.nops)
+        return out
 
     def saveFinalData(self):
         e = np.zeros(FDM_POINTS)
@@ -528,6 +544,14 @@ class FdmThermodynamics:
         self.h = C.c_void_p()
         _call(lib().nrg_thermo_create, run.h, _dp(self.temps), len(self.temps), C.byref(self.h))
         run.engine._adopt(self)
+        self.sysops = []
+
+    def setSystemOperator(self, op_index):
+        """setSystemOperator (:37-39): operators op_index of the operator set
+        saved with each snapshot are averaged as <O>(T)."""
+        idx = np.ascontiguousarray(op_index, np.int32)
+        _call(lib().nrg_thermo_set_operator, self.h, _ip(idx), len(idx))
+        self.sysops = [int(i) for i in idx]
 
     def calcThermodynamics(self, energy_scale):
         _call(lib().nrg_thermo_calc, self.h, C.c_double(energy_scale))
@@ -536,7 +560,12 @@ class FdmThermodynamics:
         s = np.zeros(len(self.temps))
         c = np.zeros(len(self.temps))
         _call(lib().nrg_thermo_final, self.h, _dp(s), _dp(c))
-        return {"temperatureArray": self.temps.copy(), "entropy": s, "specificHeat": c}
+        out = {"temperatureArray": self.temps.copy(), "entropy": s, "specificHeat": c}
+        if self.sysops:
+            q = np.zeros((len(self.sysops), len(self.temps)))
+            _call(lib().nrg_thermo_get_operator, self.h, _dp(q), len(self.sysops), len(self.temps))
+            out["qsysOPeratorExpValue"] = q
+        return out
 
     def close(self):
         if self.h:

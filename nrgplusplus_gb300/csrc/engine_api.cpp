@@ -289,7 +289,23 @@ static void fdm_calc_batch(const std::vector<nrg_fdm *> &fs, const std::vector<d
     f->prev_kept = sd.kept_prev;
     if (int(f->cur_kept.size()) != nsec) fail(NRG_E_STATE, "snapshot order does not match the backward pass");
     std::vector<std::vector<double>> boltz;
-    if (f->last) {  // setLocalPartitionFunction (:122-155)
+    if (f->finite_t) {  // setRhoZero(tBoltzmannFactor), fdmBackwardIteration.hpp:207-239
+      if (f->ncalc >= f->shell_weights.size())
+        fail(NRG_E_STATE, "finite-temperature FDM: more shells than the thermodynamics saw");
+      const std::vector<double> &wt = f->shell_weights[f->ncalc];
+      size_t o = 0;
+      boltz.resize(nsec);
+      for (int i = 0; i < nsec; ++i) {
+        const size_t n = sd.E_host[i].size(), kc = size_t(f->cur_kept[i]);
+        boltz[i].assign(n, 0.0);
+        for (size_t x = kc; x < n; ++x) {
+          if (o >= wt.size()) fail(NRG_E_STATE, "finite-temperature FDM: shell does not match the thermodynamics");
+          boltz[i][x] = wt[o++];
+        }
+      }
+      if (o != wt.size()) fail(NRG_E_STATE, "finite-temperature FDM: shell does not match the thermodynamics");
+      f->ncalc++;
+    } else if (f->last) {  // setLocalPartitionFunction (:122-155)
       double gs = 0;
       for (auto &v : sd.E_host)
         if (!v.empty()) gs = std::min(gs, *std::min_element(v.begin(), v.end()));
@@ -319,7 +335,7 @@ static void fdm_calc_batch(const std::vector<nrg_fdm *> &fs, const std::vector<d
       RhoTask t{};
       t.rho = wk.rp[b];
       t.n = db.n;
-      if (f->last) {
+      if (!boltz.empty()) {
         diag_fix.push_back({rtasks.size(), diag_host.size()});
         diag_host.insert(diag_host.end(), boltz[db.sector].begin(), boltz[db.sector].end());
       }
@@ -354,6 +370,43 @@ static void fdm_calc_batch(const std::vector<nrg_fdm *> &fs, const std::vector<d
     check_cuda(cudaGetLastError(), "rho init");
     hold.push_back(dd);
     hold.push_back(h);
+  }
+  // ---- rhoDotStaticOperators (fdmBackwardIteration.hpp:166-199): Tr(O_ii rho_i)
+  // per operator over its diagonal blocks, the kept x kept part of O left out
+  for (size_t w = 0; w < nf; ++w) {
+    Work &wk = W[w];
+    nrg_fdm *f = wk.f;
+    SiteData &sd = *wk.sd;
+    std::vector<StaticTask> st;
+    for (auto &kv : wk.S->ops) {
+      const int ip = std::get<0>(kv.first), i = std::get<1>(kv.first), j = std::get<2>(kv.first);
+      if (i != j || ip < 0 || ip >= f->nops || sd.sectors[i].dev < 0) continue;
+      const int b = sd.sectors[i].dev;
+      StaticTask t{};
+      t.O = kv.second.p;
+      t.ldo = kv.second.ld;
+      t.rho = wk.rp[b];
+      t.n = sd.blocks[b].n;
+      t.kc = int(f->cur_kept[i]);
+      t.op = ip;
+      st.push_back(t);
+    }
+    if (st.empty()) continue;
+    if (!f->static_acc) {
+      f->static_acc = engine_alloc(e, f->nops * sizeof(double));
+      check_cuda(cudaMemsetAsync(f->static_acc->ptr, 0, f->nops * sizeof(double), s), "static sums");
+    }
+    Staged sg;
+    size_t ot = sg.add(st);
+    std::vector<double> partial(st.size(), 0.0);
+    size_t opart = sg.add(partial);
+    DevPtr h;
+    char *d = sg.push(e, h);
+    hold.push_back(h);
+    launch_fdm_static(at<StaticTask>(d, ot), int(st.size()), f->nops, at<double>(d, opart),
+                      static_cast<double *>(f->static_acc->ptr), s);
+    engine_count_launch(e, 2);
+    check_cuda(cudaGetLastError(), "static expectation values");
   }
   // ---- rhoDotOperators (:207-277): B rho_j and rho_i B, then binning
   const bool oz = W[0].oz;
@@ -1159,10 +1212,60 @@ int nrg_thermo_calc(nrg_thermo *t, double scale) {
         disc.push_back(sd.E_host[i][j] * scale);
     for (int i = 0; i < nsec; ++i)
       for (double x : sd.E_host[i]) all.push_back(x * scale);
+    if (!t->sysops.empty()) {  // diagonals of the system operators on the discarded states (:63-88)
+      std::vector<double> q(t->sysops.size() * disc.size(), 0.0);
+      nrg_engine *e = r->eng;
+      for (size_t iq = 0; iq < t->sysops.size(); ++iq) {
+        size_t o = 0;
+        for (int i = 0; i < nsec; ++i) {
+          const size_t n = sd.E_host[i].size(), kc = size_t(t->cur_kept[i]);
+          const size_t nd = n > kc ? n - kc : 0;
+          auto it = r->loaded->ops.find(OpKey{t->sysops[iq], i, i});
+          if (nd && it != r->loaded->ops.end()) {
+            const FBlock &B = it->second;
+            if (B.rows != int(n) || B.cols != int(n)) fail(NRG_E_STATE, "system operator block size");
+            check_cuda(cudaMemcpy2DAsync(q.data() + iq * disc.size() + o, sizeof(double),
+                                         B.p + int64_t(kc) * (B.ld + 1), size_t(B.ld + 1) * sizeof(double),
+                                         sizeof(double), nd, cudaMemcpyDeviceToHost, e->stream),
+                       "system operator diagonal");
+          }
+          o += nd;
+        }
+      }
+      check_cuda(cudaStreamSynchronize(e->stream), "system operator diagonal");
+      t->qval.push_back(std::move(q));
+    }
     t->disc.push_back(std::move(disc));
     t->allv.push_back(std::move(all));
   });
 }
+
+namespace {
+// Discarded energies relative to each shell's minimum (flattened, with
+// offsets) and the one-step corrected shell ground energies
+// (fdmThermodynamics::saveFinalData, fdmThermodynamics.hpp:114-140).
+void thermo_shells(const nrg_thermo *t, std::vector<double> &flat, std::vector<int64_t> &off,
+                   std::vector<double> &gs) {
+  const int nsh = int(t->allv.size());
+  gs.assign(nsh, 0.0);
+  off.assign(nsh + 1, 0);
+  flat.clear();
+  for (int it = 0; it < nsh; ++it) {  // :114-131
+    const double m = *std::min_element(t->allv[it].begin(), t->allv[it].end());
+    gs[it] = m;
+    off[it] = int64_t(flat.size());
+    for (double x : t->disc[it]) flat.push_back(x - m);
+  }
+  off[nsh] = int64_t(flat.size());
+  for (int it = 0; it + 1 < nsh; ++it) gs[it] += gs[it + 1];  // one-step correction :133-135
+  const double g0 = gs.empty() ? 0.0 : gs[0];
+  for (auto &x : gs) x -= g0;
+}
+
+double regulate_exp_host(double x) {  // fdmThermodynamics.hpp:240-249
+  return std::exp(std::min(100.0, std::max(-100.0, x)));
+}
+}  // namespace
 
 int nrg_thermo_final(nrg_thermo *t, double *entropy, double *cv) {
   return guard([&] {
@@ -1170,33 +1273,101 @@ int nrg_thermo_final(nrg_thermo *t, double *entropy, double *cv) {
     nrg_engine *e = t->run->eng;
     const int nsh = int(t->allv.size());
     if (nsh == 0) fail(NRG_E_STATE, "no shells");
-    std::vector<double> gs(nsh), flat;
-    std::vector<int64_t> off(nsh + 1, 0);
-    for (int it = 0; it < nsh; ++it) {  // :114-131
-      const double m = *std::min_element(t->allv[it].begin(), t->allv[it].end());
-      gs[it] = m;
-      off[it] = int64_t(flat.size());
-      for (double x : t->disc[it]) flat.push_back(x - m);
-    }
-    off[nsh] = int64_t(flat.size());
-    for (int it = 0; it + 1 < nsh; ++it) gs[it] += gs[it + 1];  // one-step correction :133-135
-    const double g0 = gs[0];
-    for (auto &x : gs) x -= g0;
+    std::vector<double> gs, flat;
+    std::vector<int64_t> off;
+    thermo_shells(t, flat, off, gs);
     const int nt = int(t->temps.size());
+    const int nq = int(t->sysops.size());
+    const int64_t ndisc = int64_t(flat.size());
+    std::vector<double> qv(size_t(nq) * ndisc, 0.0);  // operator diagonals in the layout of flat
+    for (int it = 0; it < nsh && nq; ++it) {
+      const int64_t nd = off[it + 1] - off[it];
+      for (int iq = 0; iq < nq; ++iq)
+        std::copy(t->qval[it].begin() + iq * nd, t->qval[it].begin() + (iq + 1) * nd,
+                  qv.begin() + int64_t(iq) * ndisc + off[it]);
+    }
     Staged st;
-    size_t of = st.add(flat), oo = st.add(off), og = st.add(gs), ot = st.add(t->temps);
-    std::vector<double> scratch(size_t(3) * nsh * nt + 2 * nt, 0.0);
+    size_t of = st.add(flat), oo = st.add(off), og = st.add(gs), ot = st.add(t->temps), oq = st.add(qv);
+    std::vector<double> scratch(size_t(3 + nq) * nsh * nt + size_t(2 + nq) * nt, 0.0);
     size_t os = st.add(scratch);
     DevPtr hold;
     char *d = st.push(e, hold);
-    double *ent = at<double>(d, os) + size_t(3) * nsh * nt;
+    double *ent = at<double>(d, os) + size_t(3 + nq) * nsh * nt;
     launch_thermo(at<double>(d, of), at<int64_t>(d, oo), at<double>(d, og), nsh, at<double>(d, ot), nt,
-                  t->bathdim, at<double>(d, os), ent, ent + nt, e->stream);
+                  t->bathdim, at<double>(d, oq), nq, ndisc, at<double>(d, os), ent, ent + nt, ent + 2 * nt,
+                  e->stream);
     engine_count_launch(e, 1);
     check_cuda(cudaGetLastError(), "thermo");
     check_cuda(cudaMemcpyAsync(entropy, ent, nt * sizeof(double), cudaMemcpyDeviceToHost, e->stream), "D2H");
     check_cuda(cudaMemcpyAsync(cv, ent + nt, nt * sizeof(double), cudaMemcpyDeviceToHost, e->stream), "D2H");
+    t->opexp.assign(size_t(nq) * nt, 0.0);
+    if (nq)
+      check_cuda(cudaMemcpyAsync(t->opexp.data(), ent + 2 * nt, size_t(nq) * nt * sizeof(double),
+                                 cudaMemcpyDeviceToHost, e->stream), "D2H");
     check_cuda(cudaStreamSynchronize(e->stream), "thermo");
+  });
+}
+
+int nrg_thermo_set_operator(nrg_thermo *t, const int *op_index, int n) {
+  return guard([&] {
+    if (!t || n < 0 || (n > 0 && !op_index)) fail(NRG_E_ARG, "bad argument");
+    if (n > kThermoMaxOps) fail(NRG_E_ARG, "at most " + std::to_string(kThermoMaxOps) + " system operators");
+    if (!t->allv.empty()) fail(NRG_E_STATE, "setSystemOperator must come before the first calcThermodynamics");
+    for (int i = 0; i < n; ++i)
+      if (op_index[i] < 0) fail(NRG_E_ARG, "negative operator index");
+    t->sysops.assign(op_index, op_index + n);
+  });
+}
+
+int nrg_thermo_get_operator(nrg_thermo *t, double *out, int n, int nt) {
+  return guard([&] {
+    if (!t || (!out && n * nt > 0)) fail(NRG_E_ARG, "bad argument");
+    if (n != int(t->sysops.size()) || nt != int(t->temps.size()))
+      fail(NRG_E_ARG, "operator / temperature count differs from the thermodynamics object");
+    if (t->opexp.size() != size_t(n) * nt) fail(NRG_E_STATE, "nrg_thermo_final has not run");
+    std::copy(t->opexp.begin(), t->opexp.end(), out);
+  });
+}
+
+int nrg_fdm_set_temperature(nrg_fdm *f, double T, nrg_thermo *t) {
+  return guard([&] {
+    if (!f || !t) fail(NRG_E_ARG, "null argument");
+    if (!(T > 0.0)) fail(NRG_E_ARG, "temperature must be > 0");
+    if (!f->last || f->ncalc) fail(NRG_E_STATE, "setTemperature must come before the first calcSpectrum");
+    if (t->run != f->run) fail(NRG_E_ARG, "the thermodynamics object belongs to another run");
+    const int nsh = int(t->allv.size());
+    if (nsh == 0) fail(NRG_E_STATE, "the thermodynamics object has seen no shells");
+    std::vector<double> gs, flat;
+    std::vector<int64_t> off;
+    thermo_shells(t, flat, off, gs);
+    // w_m (:159-175) and the per-state probabilities exp((E0_m - E)/T) / Z'_m (:183-218)
+    std::vector<double> z(nsh, 0.0);
+    double lpart = 0.0;
+    for (int i = 0; i < nsh; ++i) {
+      for (int64_t a = off[i]; a < off[i + 1]; ++a) z[i] += regulate_exp_host((gs[i] - flat[a]) / T);
+      lpart += z[i] * std::pow(t->bathdim, double(i));
+    }
+    f->shell_weights.assign(nsh, {});
+    for (int i = 0; i < nsh; ++i) {
+      const double wm = z[i] * std::pow(t->bathdim, double(i)) / lpart;
+      for (int64_t a = off[i]; a < off[i + 1]; ++a)
+        f->shell_weights[i].push_back(z[i] > 0 ? wm * regulate_exp_host((gs[i] - flat[a]) / T) / z[i] : 0.0);
+    }
+    f->finite_t = true;
+    f->temperature = T;
+  });
+}
+
+int nrg_fdm_get_static(nrg_fdm *f, double *out, int nops) {
+  return guard([&] {
+    if (!f || (!out && nops > 0)) fail(NRG_E_ARG, "bad argument");
+    if (nops != f->nops) fail(NRG_E_ARG, "operator count differs from the FDM object");
+    std::fill(out, out + nops, 0.0);
+    if (!f->static_acc) return;
+    nrg_engine *e = f->run->eng;
+    check_cuda(cudaMemcpyAsync(out, f->static_acc->ptr, nops * sizeof(double), cudaMemcpyDeviceToHost, e->stream),
+               "static D2H");
+    check_cuda(cudaStreamSynchronize(e->stream), "static D2H");
   });
 }
 

@@ -258,6 +258,14 @@ struct nrg_fdm {
   nrg::DevPtr hist;                        // 2 * nops * npts
   double local_gs = 0, local_z = 0;
   std::vector<double> partitions;
+  // finite temperature (nrg_fdm_set_temperature): per shell in backward
+  // order, the Boltzmann weights of its discarded states (thermodynamics
+  // layout: sectors in order, states past the kept prefix)
+  bool finite_t = false;
+  double temperature = 0;
+  std::vector<std::vector<double>> shell_weights;
+  size_t ncalc = 0;
+  nrg::DevPtr static_acc;                  // nops running sums of rhoDotStaticOperators
 };
 
 struct nrg_thermo {
@@ -268,4 +276,9 @@ struct nrg_thermo {
   bool have_cur = false;
   std::vector<int64_t> cur_kept, prev_kept;
   std::vector<std::vector<double>> disc, allv;
+  // system operators (setSystemOperator): indices into each snapshot's
+  // operator set, and per shell their diagonals on the discarded states
+  std::vector<int> sysops;
+  std::vector<std::vector<double>> qval;  // per shell: nq x (discarded states)
+  std::vector<double> opexp;              // nq x nt after nrg_thermo_final
 };

@@ -120,22 +120,30 @@ __device__ __forceinline__ double regulate_exp(double x) {  // fdmThermodynamics
 // ground energies.
 // One CTA per temperature; warp w takes shells w, w + 8, ... and sums, over
 // the shell's discarded states with x = E - E_gs(shell) and
-// e = regulate_exp(-x / kT), the three moments Z_i = sum e, M1_i = sum x e,
-// M2_i = sum x^2 e in one pass (each Boltzmann factor once).  With the
-// reference's shell weights w_i = Z_i d^i / sum_j Z_j d^j and per-shell
-// probabilities e / Z_i (fdmThermodynamics.hpp:42-236):
+// e = regulate_exp(-x / kT), the moments Z_i = sum e, M1_i = sum x e,
+// M2_i = sum x^2 e and, per system operator q, Q_qi = sum O_q(x) e in one
+// pass (each Boltzmann factor once).  With the reference's shell weights
+// w_i = Z_i d^i / sum_j Z_j d^j and per-shell probabilities e / Z_i
+// (fdmThermodynamics.hpp:42-236):
 //   <E> = sum_i d^i M1_i / L,  <E^2> = sum_i d^i M2_i / L,  L = sum_i d^i Z_i,
-//   S = ln L + <E> / kT,  C = (<E^2> - <E>^2) / kT^2.
-// sums: 3 * nshell doubles of scratch per temperature.
+//   S = ln L + <E> / kT,  C = (<E^2> - <E>^2) / kT^2,
+//   <O_q> = sum_i d^i Q_qi / L   (qsysOPeratorExpValue, :200-218).
+// qv: nq arrays in the layout of disc (the diagonal of each operator on the
+// discarded states); sums: (3 + nq) * nshell doubles of scratch per
+// temperature; opexp: nq x nt.
 __global__ void k_thermo(const double *__restrict__ disc, const int64_t *__restrict__ disc_off,
                          const double *__restrict__ gs, int nshell, const double *__restrict__ temps,
-                         double bathdim, double *__restrict__ sums, double *__restrict__ entropy,
-                         double *__restrict__ cv) {
+                         double bathdim, const double *__restrict__ qv, int nq, int64_t ndisc,
+                         double *__restrict__ sums, double *__restrict__ entropy, double *__restrict__ cv,
+                         double *__restrict__ opexp, int nt) {
   const double kbt = temps[blockIdx.x], inv = 1.0 / kbt;
-  double *z = sums + int64_t(blockIdx.x) * 3 * nshell, *m1 = z + nshell, *m2 = m1 + nshell;
+  double *z = sums + int64_t(blockIdx.x) * (3 + nq) * nshell, *m1 = z + nshell, *m2 = m1 + nshell;
+  double *mq = m2 + nshell;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
   for (int i = warp; i < nshell; i += nw) {
-    double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0, sq[kThermoMaxOps];
+#pragma unroll
+    for (int q = 0; q < kThermoMaxOps; ++q) sq[q] = 0.0;
     const double g = gs[i];
     for (int64_t a = disc_off[i] + lane; a < disc_off[i + 1]; a += 32) {
       const double x = disc[a] - g;
@@ -143,16 +151,23 @@ __global__ void k_thermo(const double *__restrict__ disc, const int64_t *__restr
       s0 += w;
       s1 += x * w;
       s2 += x * x * w;
+#pragma unroll
+      for (int q = 0; q < kThermoMaxOps; ++q)
+        if (q < nq) sq[q] += qv[int64_t(q) * ndisc + a] * w;
     }
     for (int o = 16; o > 0; o >>= 1) {
       s0 += __shfl_xor_sync(0xffffffffu, s0, o);
       s1 += __shfl_xor_sync(0xffffffffu, s1, o);
       s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+#pragma unroll
+      for (int q = 0; q < kThermoMaxOps; ++q)
+        if (q < nq) sq[q] += __shfl_xor_sync(0xffffffffu, sq[q], o);  // nq is uniform
     }
     if (lane == 0) {
       z[i] = s0;
       m1[i] = s1;
       m2[i] = s2;
+      for (int q = 0; q < nq; ++q) mq[int64_t(q) * nshell + i] = sq[q];
     }
   }
   __syncthreads();
@@ -167,7 +182,48 @@ __global__ void k_thermo(const double *__restrict__ disc, const int64_t *__restr
     const double eav = e1 / lpart, esq = e2 / lpart;
     entropy[blockIdx.x] = log(lpart) + eav / kbt;
     cv[blockIdx.x] = (esq - eav * eav) / (kbt * kbt);
+    for (int q = 0; q < nq; ++q) {
+      double oq = 0.0;
+      for (int i = 0; i < nshell; ++i) oq += mq[int64_t(q) * nshell + i] * pow(bathdim, double(i));
+      opexp[int64_t(q) * nt + blockIdx.x] = oq / lpart;
+    }
   }
+}
+
+// Static expectation values of one shell (fdmBackwardIteration::
+// rhoDotStaticOperators, dynamics/fdmBackwardIteration.hpp:166-199): for each
+// diagonal operator block (i, i), sum over v, v' of O(v, v') rho_i(v', v) with
+// the kept x kept part of O left out.  One CTA per task writes its partial
+// sum; k_fdm_static_sum then adds the partials of each operator in task order
+// (deterministic) to that operator's running total.
+__global__ void k_fdm_static(const StaticTask *__restrict__ tasks, double *__restrict__ partial) {
+  const StaticTask T = tasks[blockIdx.x];
+  __shared__ double red[8];
+  double s = 0.0;
+  const int64_t nel = int64_t(T.n) * T.n;
+  for (int64_t e = threadIdx.x; e < nel; e += blockDim.x) {
+    const int r = int(e / T.n), c = int(e - int64_t(r) * T.n);
+    if (r < T.kc && c < T.kc) continue;
+    s += T.O[int64_t(r) * T.ldo + c] * T.rho[int64_t(c) * T.n + r];
+  }
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int i = 0; i < int(blockDim.x >> 5); ++i) t += red[i];
+    partial[blockIdx.x] = t;
+  }
+}
+
+__global__ void k_fdm_static_sum(const StaticTask *__restrict__ tasks, int ntasks,
+                                 const double *__restrict__ partial, double *__restrict__ acc) {
+  if (threadIdx.x != 0) return;
+  const int op = blockIdx.x;
+  double s = acc[op];
+  for (int t = 0; t < ntasks; ++t)
+    if (tasks[t].op == op) s += partial[t];
+  acc[op] = s;
 }
 
 }  // namespace
@@ -197,10 +253,18 @@ void launch_broaden(const double *e, const double *w, int64_t nbins, const doubl
 }
 
 void launch_thermo(const double *disc, const int64_t *disc_off, const double *gs, int nshell,
-                   const double *temps, int nt, double bathdim, double *sums, double *entropy,
-                   double *cv, cudaStream_t s) {
+                   const double *temps, int nt, double bathdim, const double *qv, int nq, int64_t ndisc,
+                   double *sums, double *entropy, double *cv, double *opexp, cudaStream_t s) {
   if (nt == 0) return;
-  k_thermo<<<nt, 256, 0, s>>>(disc, disc_off, gs, nshell, temps, bathdim, sums, entropy, cv);
+  k_thermo<<<nt, 256, 0, s>>>(disc, disc_off, gs, nshell, temps, bathdim, qv, nq, ndisc, sums, entropy, cv,
+                              opexp, nt);
+}
+
+void launch_fdm_static(const StaticTask *tasks, int ntasks, int nops, double *partial, double *acc,
+                       cudaStream_t s) {
+  if (ntasks == 0) return;
+  k_fdm_static<<<ntasks, 256, 0, s>>>(tasks, partial);
+  k_fdm_static_sum<<<nops, 32, 0, s>>>(tasks, ntasks, partial, acc);
 }
 
 }  // namespace nrg

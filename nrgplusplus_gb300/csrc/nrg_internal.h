@@ -228,9 +228,19 @@ void launch_partial_trace(const TraceTask *tasks, int ntask, const TraceIn *ins,
                           cudaStream_t s);
 void launch_broaden(const double *e, const double *w, int64_t nbins, const double *omegas,
                     int64_t nomega, double b, double *out, cudaStream_t s);
-// sums: 3 * nshell * nt doubles of scratch
+// sums: (3 + nq) * nshell * nt doubles of scratch; qv: nq system-operator
+// diagonals in the layout of disc (ndisc entries each), opexp: nq x nt
+constexpr int kThermoMaxOps = 8;
 void launch_thermo(const double *disc, const int64_t *disc_off, const double *gs, int nshell,
-                   const double *temps, int nt, double bathdim, double *sums, double *entropy,
-                   double *cv, cudaStream_t s);
+                   const double *temps, int nt, double bathdim, const double *qv, int nq, int64_t ndisc,
+                   double *sums, double *entropy, double *cv, double *opexp, cudaStream_t s);
+struct StaticTask {       // one diagonal operator block (i, i) of one shell
+  const double *O;        // operator block, n x n, leading dimension ldo
+  const double *rho;      // the shell's density-matrix block, n x n
+  int n, ldo, kc, op;     // kc: kept states of block i (kept x kept part skipped)
+};
+// acc[op] += sum over the op's tasks, in task order; partial: ntasks doubles
+void launch_fdm_static(const StaticTask *tasks, int ntasks, int nops, double *partial, double *acc,
+                       cudaStream_t s);
 
 }  // namespace nrg

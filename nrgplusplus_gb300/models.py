@@ -207,6 +207,16 @@ def d_dag_chi():
     return fb.block_operators([x @ chi for x in f])
 
 
+def n_d():
+    """Impurity occupancy n_d = sum_sigma d_sigma-dagger d_sigma in the
+    spinhalf sector basis (block diagonal), built as the reference's
+    fermionBasis::get_block_operators of the raw occupancy matrix
+    (models/fermionBasis.hpp:292-330)."""
+    fb = FermionBasis(2, CHARGE_AND_SPIN)
+    f = fb.raw_fdag
+    return fb.block_operators([sum(x @ x.T for x in f)])
+
+
 def hopping(site, lam):
     """Wilson-chain hopping t_n (examples/rgflowSIAM/main.cpp:5-10)."""
     return (0.5 * (1.0 + 1.0 / lam) * (1.0 - lam ** (-site - 1))

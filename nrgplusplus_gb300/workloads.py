@@ -35,29 +35,34 @@ def build_models(kind, eps=-0.25, U=0.5, J=0.25):
 
 
 def run_nrg(engine, kind, nkeep, nsites, lam, V=None, eps=-0.25, U=0.5, J=0.25, fdm=False,
-            thermo=False, keep_eigs=True):
+            thermo=False, keep_eigs=True, fdm_T=None, with_nd=False):
     """One NRG run through the public API.  Kondo-type impurities ('kondo',
-    'zero') have no V site and rescale by sqrt(Lambda) from the first site."""
+    'zero') have no V site and rescale by sqrt(Lambda) from the first site.
+    fdm_T: the FDM spectrum at that temperature (a thermodynamics pass over
+    the same shells first provides the Boltzmann weights) instead of T = 0.
+    with_nd: n_d is tracked beside d-dagger-chi (operator 2) and averaged by
+    the thermodynamics (qsysOPeratorExpValue) and the FDM (static)."""
     imp, bath = build_models(kind, eps, U, J)
     kondo = kind in ("kondo", "zero")
     nops = len(imp.fdag)
     run = api.NrgCore(engine, imp, bath, nkeep)
     data = api.NrgData(run)
+    track = M.d_dag_chi() + (M.n_d() if with_nd else [])
     ops = None
     out = {"eig": [], "kept": [], "run": run}
     if not kondo:
         run.add_bath_site([V] * nops, 1.0)
-        if fdm:
-            ops = api.OperatorSet(run, M.d_dag_chi())
+        if fdm or with_nd:
+            ops = api.OperatorSet(run, track)
             api.update_system_operator(run, ops)
         run.update_internal_state()
     min_it = 0
     for it in range(nsites):
         r = math.sqrt(lam) if (kondo or it > 0) else 1.0
         run.add_bath_site([M.hopping(it, lam)] * nops, r)
-        if fdm:
+        if fdm or with_nd:
             if ops is None:
-                ops = api.OperatorSet(run, M.d_dag_chi())
+                ops = api.OperatorSet(run, track)
             api.update_system_operator(run, ops)
         if fdm or thermo:
             if run.checkHigherEnergyDiscarded():
@@ -70,23 +75,40 @@ def run_nrg(engine, kind, nkeep, nsites, lam, V=None, eps=-0.25, U=0.5, J=0.25, 
             out["kept"].append(run.kept_counts)
     out["min_it"] = min_it
     out["nsites"] = nsites
-    if fdm:
-        f = api.FdmSpectrum(run, ops.nops)
-        cnt = run.nrg_iterations_cnt
-        for it in range(nsites, min_it, -1):
-            cnt -= 1
-            data.loadCurrentData(cnt)
-            f.calcSpectrum(lam ** (-(it - 1.0) / 2.0))
-        out.update(f.saveFinalData())
-        f.close()
-    if thermo:
-        th = api.FdmThermodynamics(run, temperature_grid())
+
+    def thermo_pass(temps):
+        th = api.FdmThermodynamics(run, temps)
+        if with_nd:
+            th.setSystemOperator([2])
         cnt = run.nrg_iterations_cnt
         lo = min_it + (1 if kondo else 0)
         for it in range(nsites, lo, -1):
             cnt -= 1
             data.loadCurrentData(cnt)
             th.calcThermodynamics(lam ** (-(1.0 * it - 1.0) / 2.0))
+        return th
+
+    if fdm:
+        tw = None
+        if fdm_T is not None:
+            if kondo:
+                raise ValueError("finite-T FDM: the thermodynamic shells of a Kondo run start one later")
+            tw = thermo_pass([fdm_T])
+        f = api.FdmSpectrum(run, ops.nops)
+        if tw is not None:
+            f.setTemperature(fdm_T, tw)
+        cnt = run.nrg_iterations_cnt
+        for it in range(nsites, min_it, -1):
+            cnt -= 1
+            data.loadCurrentData(cnt)
+            f.calcSpectrum(lam ** (-(it - 1.0) / 2.0))
+        out.update(f.saveFinalData())
+        out["static"] = f.staticExpectation()
+        f.close()
+        if tw is not None:
+            tw.close()
+    if thermo:
+        th = thermo_pass(temperature_grid())
         out.update(th.saveFinalData())
         th.close()
     return out

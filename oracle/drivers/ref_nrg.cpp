@@ -13,7 +13,11 @@
 // public members that nrgData.hpp:150-157 saves.
 //
 // usage: ref_nrg <siam|kondo|twochannel> <out.bin> key=value ...
-//   keys: eps U V J lambda nkeep nsites fdm thermo dumpops opsites
+//   keys: eps U V J lambda nkeep nsites fdm thermo dumpops opsites sysop
+//   sysop=1 (with thermo): the impurity occupancy n_d is tracked through
+//   update_system_operator and handed to fdmThermodynamics::setSystemOperator
+//   (static/fdmThermodynamics.hpp:37-39, :63-88, :200-218), whose
+//   qsysOPeratorExpValue (<n_d>(T)) is written out.
 #include "dynamics/fdmSpectrum.hpp"
 #include "models/fermionBasis.hpp"
 #include "models/spinhalf.hpp"
@@ -57,7 +61,7 @@ struct Snap {
   std::vector<std::vector<int>> cur, pre;
   std::vector<std::vector<double>> ev;
   std::vector<std::vector<size_t>> cpl, kept;
-  std::vector<qOperator> op;
+  std::vector<qOperator> op, sysop;
 };
 
 template <class N> static void dump_ops(Out &o, std::vector<qOperator> &ops, const std::string &tag) {
@@ -82,7 +86,15 @@ static void run(IMP &imp, BATH &bath, std::map<std::string, double> &P, bool fir
   int dumpops = int(P["dumpops"]);
   nrgcore<IMP, BATH> n(imp, bath);
   n.set_parameters(nk);
-  std::vector<qOperator> d;
+  std::vector<qOperator> d, nd;
+  const bool sysop = thermo && P["sysop"] != 0;
+  if (sysop) {
+    fermionBasis b(2, fermionBasis::chargeAndSpin);
+    auto f = b.get_raw_f_dag_operator();
+    auto nt = f[0].dot(f[0].cTranspose());
+    for (size_t i = 1; i < f.size(); i++) nt = nt + f[i].dot(f[i].cTranspose());
+    nd = b.get_block_operators(std::vector<qmatrix<>>{nt});
+  }
   if (fdm) {
     fermionBasis b(2, fermionBasis::chargeAndSpin);
     auto f = b.get_raw_f_dag_operator();
@@ -110,6 +122,7 @@ static void run(IMP &imp, BATH &bath, std::map<std::string, double> &P, bool fir
     std::vector<double> t(nops, V);
     n.add_bath_site(t, 1.0);
     if (fdm) update_system_operator(&n, d);
+    if (sysop) update_system_operator(&n, nd);
     n.update_internal_state();
     record("V");
   }
@@ -118,10 +131,11 @@ static void run(IMP &imp, BATH &bath, std::map<std::string, double> &P, bool fir
     std::vector<double> t(nops, hopping(in, L));
     n.add_bath_site(t, r);
     if (fdm) update_system_operator(&n, d);
+    if (sysop) update_system_operator(&n, nd);
     if (fdm || thermo) {
       if (n.checkHigherEnergyDiscarded())
         st[n.nrg_iterations_cnt] = {n.current_hamiltonQ, n.current_sysmQ, n.pre_sysmQ, n.eigenvaluesQ,
-                                    n.coupled_nQ_index, n.eigenvaluesQ_kept_indices, d};
+                                    n.coupled_nQ_index, n.eigenvaluesQ_kept_indices, d, nd};
       else
         minIt++;
     }
@@ -160,6 +174,8 @@ static void run(IMP &imp, BATH &bath, std::map<std::string, double> &P, bool fir
     std::vector<double> T(tP);
     for (int i = 0; i < tP; i++) T[i] = vMin * std::exp(std::fabs(i) * 1. / dT);
     fdmThermodynamics<decltype(n)> th(&n, T);
+    std::vector<qOperator> ndShell;
+    if (sysop) th.setSystemOperator(&ndShell);
     size_t lo = minIt + (kondoRescale ? 1 : 0);
     for (size_t in = nMax; in > lo; in--) {
       double sc = std::pow(L, -(1.0 * in - 1.0) / 2.0);
@@ -167,6 +183,7 @@ static void run(IMP &imp, BATH &bath, std::map<std::string, double> &P, bool fir
       auto &s = st.at(n.nrg_iterations_cnt);
       n.current_hamiltonQ = s.H; n.current_sysmQ = s.cur; n.pre_sysmQ = s.pre;
       n.eigenvaluesQ = s.ev; n.coupled_nQ_index = s.cpl; n.eigenvaluesQ_kept_indices = s.kept;
+      ndShell = s.sysop;
       th.calcThermodynamics(sc);
     }
     th.saveFinalData(&o);
@@ -181,7 +198,7 @@ int main(int argc, char **argv) {
   std::string model = argv[1];
   std::map<std::string, double> P = {{"eps", -0.25}, {"U", 0.5},  {"V", 0.1},   {"J", 0.25},
                                      {"lambda", 2.0}, {"nkeep", 512}, {"nsites", 40}, {"fdm", 0},
-                                     {"thermo", 0},  {"dumpops", 0}};
+                                     {"thermo", 0},  {"dumpops", 0},  {"sysop", 0}};
   for (int i = 3; i < argc; i++) {
     std::string a = argv[i];
     auto p = a.find('=');

@@ -228,15 +228,25 @@ class NrgOracle:
 
 
 class FdmSpectrumOracle:
-    """Restatement of fdmSpectrum (dynamics/fdmSpectrum.hpp), T = 0."""
+    """Restatement of fdmSpectrum (dynamics/fdmSpectrum.hpp): T = 0 as the
+    reference runs it, or at a finite temperature when `shell_weights` is
+    given -- per calc_spectrum call (backward order) the Boltzmann weights of
+    that shell's discarded states in FdmThermoOracle.shell_weights layout,
+    placed on the diagonal as fdmBackwardIteration::setRhoZero(tBoltzmannFactor)
+    does (dynamics/fdmBackwardIteration.hpp:207-239).  `static` accumulates
+    rhoDotStaticOperators (:166-199) over the shells: Tr(O_ii rho_i) with the
+    kept x kept part of O zeroed, per operator."""
 
-    def __init__(self, nops):
+    def __init__(self, nops, shell_weights=None):
         self.last = True                                     # setup :44-48
         self.cur_kept = None
         self.prev_kept = None
         self.reduced = []
         self.pos = np.zeros((nops, FDM_ENERGY_PTS))          # setOperator :306-314
         self.neg = np.zeros((nops, FDM_ENERGY_PTS))
+        self.shell_weights = shell_weights
+        self.ncalc = 0
+        self.static = np.zeros(nops)
 
     def calc_spectrum(self, snap, scale):                    # :55-63
         nsec = len(snap["current_sysmQ"])
@@ -247,14 +257,24 @@ class FdmSpectrumOracle:
         self.prev_kept = list(snap["kept"])
         E = snap["eigenvaluesQ"]
         rho = []                                             # setRhoZero :165-199
-        if self.last:                                        # setLocalPartitionFunction :122-155
+        if self.shell_weights is not None:                   # setRhoZero(tBoltzmannFactor)
+            w, o = self.shell_weights[self.ncalc], 0
+            for i in range(nsec):
+                n, kc = len(E[i]), self.cur_kept[i]
+                m = np.zeros((n, n))
+                m[np.arange(kc, n), np.arange(kc, n)] = w[o:o + n - kc]
+                o += n - kc
+                if self.reduced and kc:
+                    m[:kc, :kc] = self.reduced[i][:kc, :kc]
+                rho.append(m)
+        elif self.last:                                      # setLocalPartitionFunction :122-155
             egs = 0.0
             for e in E:
                 if len(e):
                     egs = min(egs, float(np.min(e)))
             z = sum(int(np.count_nonzero(np.abs(e - egs) < FDM_ENERGY_ERRORBAR)) for e in E)
             self.boltz = [np.where(np.abs(e - egs) < FDM_ENERGY_ERRORBAR, 1.0 / z, 0.0) for e in E]
-        for i in range(nsec):
+        for i in range(nsec if self.shell_weights is None else 0):
             n = len(E[i])
             m = np.zeros((n, n))
             if self.last:
@@ -263,7 +283,16 @@ class FdmSpectrumOracle:
                 kc = self.cur_kept[i]
                 m[:kc, :kc] = self.reduced[i][:kc, :kc]
             rho.append(m)
-        ops = snap["ops"]                                    # rhoDotOperators :207-277
+        ops = snap["ops"]
+        for ip, op in enumerate(ops):                        # rhoDotStaticOperators :166-199
+            for (i, j), O in op.items():
+                if i != j or O.size == 0:
+                    continue
+                O = O.copy()
+                kc = self.cur_kept[i]
+                O[:kc, :kc] = 0.0
+                self.static[ip] += float(np.sum(O * rho[i].T))
+        # rhoDotOperators :207-277
         for ip, op in enumerate(ops):
             for (i, j), B in op.items():
                 if B.size == 0:
@@ -298,6 +327,7 @@ class FdmSpectrumOracle:
                     acc += r[a:a + k, a:a + k]
                 self.reduced[ii] += acc
         self.last = False
+        self.ncalc += 1
 
     @staticmethod
     def energy_points():                                     # saveFinalData :322-337
@@ -327,8 +357,13 @@ class FdmThermoOracle:
         self.cur_kept = None
         self.prev_kept = None
         self.disc, self.allv = [], []
+        self.qval = []
 
-    def calc(self, snap, scale):                              # :42-89
+    def calc(self, snap, scale, sysops=None):                 # :42-89
+        """One shell (backward order).  sysops: the system operators of
+        this shell ({(i, j): block} per operator, setSystemOperator :37-39);
+        the diagonal elements of their (i, i) blocks on the discarded states
+        are kept (:63-88)."""
         if self.cur_kept is None:                             # setCurrentKeptIndex :91-100
             self.cur_kept = [0] * len(snap["current_sysmQ"])
         else:
@@ -338,8 +373,23 @@ class FdmThermoOracle:
         self.disc.append(np.concatenate([np.asarray(E[i][self.cur_kept[i]:]) * scale
                                          for i in range(len(E))] or [np.zeros(0)]))
         self.allv.append(np.concatenate([np.asarray(e) * scale for e in E]))
+        if sysops is not None:
+            q = []
+            for op in sysops:
+                v = np.zeros(self.disc[-1].size)
+                o = 0
+                for i in range(len(E)):
+                    nd = len(E[i]) - self.cur_kept[i]
+                    B = op.get((i, i))
+                    if B is not None and B.size:
+                        v[o:o + nd] = np.diag(B)[self.cur_kept[i]:]
+                    o += nd
+                q.append(v)
+            self.qval.append(q)
 
-    def final(self):                                          # saveFinalData :101-236
+    def _shells(self):
+        """Discarded energies relative to each shell's ground state and the
+        one-step corrected shell ground-state energies (:114-140)."""
         nsh = len(self.allv)
         gs = np.zeros(nsh)
         disc = [d.copy() for d in self.disc]
@@ -349,33 +399,58 @@ class FdmThermoOracle:
             gs[it] = r
         for it in range(nsh - 1):                             # one-step correction :133-135
             gs[it] += gs[it + 1]
-        gs = gs - gs[0]
+        return disc, gs - gs[0]
+
+    @staticmethod
+    def _rexp(x):                                             # regulateExp :240-249
+        return np.exp(np.clip(x, -100.0, 100.0))
+
+    def _weights(self, disc, gs, kbt):
+        """w_m (normalised), Z'_m and the partition sum at one temperature
+        (:159-175)."""
+        nsh = len(disc)
+        cnt = self.nmax
+        wm = np.zeros(nsh)
+        zp = np.zeros(nsh)
+        for i in range(nsh):
+            pref = float(self.bathdim) ** (self.nmax - cnt)
+            zi = float(np.sum(self._rexp((gs[i] - disc[i]) / kbt)))
+            cnt -= 1
+            wm[i] = zi * pref
+            zp[i] = zi
+        lpart = float(np.sum(wm))
+        return wm / lpart, zp, lpart
+
+    def shell_weights(self, kbt):
+        """Boltzmann weight of every discarded state of every shell at
+        temperature kbt, w_m exp((E0_m - E)/T) / Z'_m (the weights the
+        thermodynamic averages use, :183-218), in the layout of `disc`:
+        the form fdmBackwardIteration::setRhoZero(tBoltzmannFactor)
+        (dynamics/fdmBackwardIteration.hpp:207-239) takes per shell."""
+        disc, gs = self._shells()
+        wm, zp, _ = self._weights(disc, gs, kbt)
+        return [wm[i] * self._rexp((gs[i] - disc[i]) / kbt) / zp[i] if disc[i].size else np.zeros(0)
+                for i in range(len(disc))]
+
+    def final(self):                                          # saveFinalData :101-236
+        disc, gs = self._shells()
+        nsh = len(disc)
         ent = np.zeros(len(self.T))
         cv = np.zeros(len(self.T))
-
-        def rexp(x):                                          # regulateExp :240-249
-            return np.exp(np.clip(x, -100.0, 100.0))
-
+        nq = len(self.qval[0]) if self.qval else 0
+        self.opexp = np.zeros((nq, len(self.T)))
         for itm, kbt in enumerate(self.T):
-            cnt = self.nmax
-            wm = np.zeros(nsh)
-            zp = np.zeros(nsh)
-            for i in range(nsh):
-                pref = float(self.bathdim) ** (self.nmax - cnt)
-                zi = float(np.sum(rexp((gs[i] - disc[i]) / kbt)))
-                cnt -= 1
-                wm[i] = zi * pref
-                zp[i] = zi
-            lpart = float(np.sum(wm))
-            wm = wm / lpart
+            wm, zp, lpart = self._weights(disc, gs, kbt)
             eav = esq = 0.0
             for i in range(nsh):
                 if disc[i].size == 0:
                     continue
-                blm = rexp((gs[i] - disc[i]) / kbt) / zp[i]
+                blm = self._rexp((gs[i] - disc[i]) / kbt) / zp[i]
                 x = disc[i] - gs[i]
                 eav += float(np.sum(x * wm[i] * blm))
                 esq += float(np.sum(x * x * wm[i] * blm))
+                for iq in range(nq):                          # qsysOPeratorExpValue :200-218
+                    self.opexp[iq, itm] += float(np.sum(self.qval[i][iq] * wm[i] * blm))
             ent[itm] = math.log(lpart) + eav / kbt
             cv[itm] = (esq - eav * eav) / (kbt * kbt)
         return ent, cv
@@ -388,10 +463,13 @@ def temperature_grid(points=200, tmin=1e-10, tmax=2.0):
 
 
 def siam_run(imp, bath, nkeep, nsites, lam, V=None, kondo=False, track_ops=None,
-             fdm=False, thermo=False, full_fdag=True, record_h=False):
+             fdm=False, thermo=False, full_fdag=True, record_h=False, fdm_T=None, sysop_index=None):
     """Drive the oracle the way the reference's example mains do.  Returns a
     dict with per-iteration eigenvalues, kept counts and (optionally) FDM and
-    thermodynamic results."""
+    thermodynamic results.  fdm_T: the FDM spectrum at that temperature
+    (shell Boltzmann weights from the thermodynamics pass) instead of T = 0;
+    sysop_index: tracked operators handed to the thermodynamics as system
+    operators (their <O>(T) in res["opexp"])."""
     from nrgplusplus_gb300.models import hopping
     nops = len(imp.fdag)
     n = NrgOracle(imp, bath, nkeep)
@@ -422,20 +500,32 @@ def siam_run(imp, bath, nkeep, nsites, lam, V=None, kondo=False, track_ops=None,
         res["dims"].append([len(e) for e in n.eigenvaluesQ])
     res["min_it"] = min_it
     res["nrg"] = n
+    def thermo_pass(temps):
+        th = FdmThermoOracle(n.nrg_iterations_cnt, sum(len(e) for e in bath.energies), temps)
+        cnt = n.nrg_iterations_cnt
+        lo = min_it + (1 if kondo else 0)
+        for it in range(nsites, lo, -1):
+            cnt -= 1
+            snap = res["snaps"][cnt]
+            sys = None if sysop_index is None else [snap["ops"][k] for k in sysop_index]
+            th.calc(snap, lam ** (-(1.0 * it - 1.0) / 2.0), sys)
+        return th
+
     if fdm:
-        f = FdmSpectrumOracle(len(ops))
+        weights = None
+        if fdm_T is not None:
+            if kondo:
+                raise ValueError("finite-T FDM: the thermodynamic shells of a Kondo run start one later")
+            weights = thermo_pass([fdm_T]).shell_weights(fdm_T)
+        f = FdmSpectrumOracle(len(ops), weights)
         cnt = n.nrg_iterations_cnt
         for it in range(nsites, min_it, -1):
             cnt -= 1
             f.calc_spectrum(res["snaps"][cnt], lam ** (-(it - 1.0) / 2.0))
         res["pos"], res["neg"] = f.pos, f.neg
+        res["static"] = f.static
     if thermo:
-        th = FdmThermoOracle(n.nrg_iterations_cnt, sum(len(e) for e in bath.energies),
-                             temperature_grid())
-        cnt = n.nrg_iterations_cnt
-        lo = min_it + (1 if kondo else 0)
-        for it in range(nsites, lo, -1):
-            cnt -= 1
-            th.calc(res["snaps"][cnt], lam ** (-(1.0 * it - 1.0) / 2.0))
+        th = thermo_pass(temperature_grid())
         res["entropy"], res["cv"] = th.final()
+        res["opexp"] = th.opexp
     return res

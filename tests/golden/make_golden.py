@@ -95,6 +95,9 @@ def pack_run(d, with_ops=False, with_fdm=False, with_thermo=False, full_eigs=Tru
     if with_thermo:
         for k in ("temperatureArray", "entropy", "specificHeat"):
             out[k] = d[k]
+        for k, v in d.items():
+            if k.startswith("qsysOPeratorExpValue"):
+                out[k] = v
     return out
 
 
@@ -124,6 +127,10 @@ CASES = [
      {"with_thermo": True, "full_eigs": False}),
     ("ref_kondo_thermo_nk512", "kondo",
      dict(J=0.25, **{"lambda": 2.0}, nkeep=512, nsites=30, thermo=1), {"with_thermo": True}),
+    # <n_d>(T) through fdmThermodynamics::setSystemOperator (asymmetric SIAM)
+    ("ref_siam_thermo_nd_nk256", "siam",
+     dict(eps=-0.25, U=0.8, V=0.15, **{"lambda": 2.0}, nkeep=256, nsites=30, thermo=1, sysop=1),
+     {"with_thermo": True}),
     ("ref_twochannel_nk256", "twochannel",
      dict(eps=-0.3, U=0.6, V=0.12, **{"lambda": 4.0}, nkeep=256, nsites=8), {}),
 ]

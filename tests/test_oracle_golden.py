@@ -164,3 +164,42 @@ def test_ref_sweep_instances(k):
     check_eigs(fx, res["eig"], p["lam"], niter=n)
     for i in range(n):
         assert np.array_equal(np.array(res["kept"][i]), fx["kept%d" % i]), i
+
+
+def _nd_run(**kw):
+    ops = M.d_dag_chi() + M.n_d()
+    return siam_run(M.spinhalf(-0.25, 0.8), M.spinhalf(0, 0), 256, 30, 2.0, V=0.15, track_ops=ops,
+                    full_fdag=False, **kw)
+
+
+def test_ref_thermo_system_operator():
+    """<n_d>(T) of fdmThermodynamics::setSystemOperator against the reference."""
+    fx = golden("ref_siam_thermo_nd_nk256")
+    res = _nd_run(thermo=True, sysop_index=[2])
+    check_eigs(fx, res["eig"], 2.0)
+    assert np.abs(res["entropy"] - fx["entropy"]).max() < 1e-8
+    assert np.abs(res["opexp"][0] - fx["qsysOPeratorExpValue0"]).max() < 1e-10
+
+
+@pytest.mark.parametrize("itemp", [0, 60, 120, 160, 199])
+def test_finite_t_static_equals_thermodynamic_average(itemp):
+    """Two reference formulas for one number: rhoDotStaticOperators on the
+    finite-T FDM density matrix (fdmBackwardIteration.hpp:166-239) and the
+    thermodynamic average of the discarded-state diagonals
+    (fdmThermodynamics.hpp:63-88, :200-218) give the same <n_d>(T); the
+    density matrix has unit trace at every T."""
+    T = temperature_grid()[itemp]
+    th = _nd_run(thermo=True, sysop_index=[2])
+    res = _nd_run(fdm=True, fdm_T=T)
+    assert res["static"][0] == 0.0 and res["static"][1] == 0.0  # d-dagger-chi has no (i, i) blocks
+    assert abs(res["static"][2] - th["opexp"][0][itemp]) < 1e-12
+
+
+def test_finite_t_fdm_low_temperature_limit():
+    """At the lowest grid temperature the finite-T spectrum is the T = 0 one
+    (the ground state lies in the last shell): the same histograms."""
+    T = temperature_grid()[0]
+    r0 = _nd_run(fdm=True)
+    rt = _nd_run(fdm=True, fdm_T=T)
+    for a, b in ((r0["pos"], rt["pos"]), (r0["neg"], rt["neg"])):
+        assert np.abs(a - b).max() < 1e-12

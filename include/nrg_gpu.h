@@ -190,6 +190,19 @@ int nrg_opset_get_block(nrg_opset *ops, int ip, int64_t i, int64_t j, double *ou
 int nrg_run_snapshot(nrg_run *run, nrg_opset *ops);
 /* loadCurrentData(iteration): select a stored snapshot for the backward pass */
 int nrg_run_load_snapshot(nrg_run *run, int64_t iteration);
+/* The run's snapshots written to a file in the layout NrgData writes into its
+ * HDF5 file (nrgData.hpp:134-165 saveCurrentData, :175-210 saveqOperator,
+ * :106-110 saveFinalState), as a flat container of named float64 arrays
+ * (HDF5 itself is not linked): magic "NGRA" (u32 0x4152474e), u32 version 1,
+ * then per array u32 name length, name, u64 count, count float64.  Per saved
+ * iteration N: /NrgItrN/current_sysmQ, pre_sysmQ (flattened, nq per sector),
+ * nq, eigenvaluesQ_kept_indices (kept count per pre sector; the kept states
+ * are a prefix), eigenvaluesQ/<sector>, coupled_nQ_index/<sector>, with
+ * with_vectors != 0 current_hamiltonQ/<sector> (eigenvectors as columns,
+ * row-major), and the saved operator set op/operatorSize,
+ * op/at<ip>/{qmat<k>, idVector, rowVector, colVector}; then savedNRGIndex
+ * and relativeGroundStateEnergy.  Reader: nrgplusplus_gb300.archive. */
+int nrg_run_export_snapshots(nrg_run *run, const char *path, int with_vectors);
 
 /* ---- FDM spectral function, T = 0 (fdmSpectrum.hpp) ------------------- */
 int nrg_fdm_create(nrg_run *run, int nops, nrg_fdm **out);     /* ctor + setOperator */

@@ -3,7 +3,9 @@
 // the FDM spectral pass (fdmSpectrum) and thermodynamics (fdmThermodynamics).
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <cstdlib>
+#include <memory>
 #include <cstring>
 #include <numeric>
 #include <set>
@@ -1095,6 +1097,106 @@ int nrg_run_load_snapshot(nrg_run *r, int64_t iteration) {
   });
 }
 
+}  // extern "C"
+
+namespace {
+// One named array of the export container: u32 name length, the name, u64
+// element count, the elements as little-endian float64.
+void put_array(FILE *fp, const std::string &name, const double *v, uint64_t n) {
+  const uint32_t len = uint32_t(name.size());
+  bool ok = std::fwrite(&len, 4, 1, fp) == 1 && std::fwrite(name.data(), 1, len, fp) == len &&
+            std::fwrite(&n, 8, 1, fp) == 1 && (n == 0 || std::fwrite(v, 8, n, fp) == n);
+  if (!ok) fail(NRG_E_ARG, "export: write failed");
+}
+void put_array(FILE *fp, const std::string &name, const std::vector<double> &v) {
+  put_array(fp, name, v.data(), v.size());
+}
+template <class T> std::vector<double> as_doubles(const std::vector<T> &v) {
+  return std::vector<double>(v.begin(), v.end());
+}
+}  // namespace
+
+extern "C" {
+
+int nrg_run_export_snapshots(nrg_run *r, const char *path, int with_vectors) {
+  return guard([&] {
+    if (!r || !path) fail(NRG_E_ARG, "null argument");
+    nrg_engine *e = r->eng;
+    FILE *fp = std::fopen(path, "wb");
+    if (!fp) fail(NRG_E_ARG, std::string("export: cannot open ") + path);
+    std::unique_ptr<FILE, int (*)(FILE *)> guard_fp(fp, std::fclose);
+    const uint32_t magic = 0x4152474eu;  // "NGRA"
+    const uint32_t version = 1;
+    if (std::fwrite(&magic, 4, 1, fp) != 1 || std::fwrite(&version, 4, 1, fp) != 1)
+      fail(NRG_E_ARG, "export: write failed");
+    std::vector<double> saved;
+    for (auto &kv : r->snaps) {
+      const int64_t it = kv.first;
+      const Snapshot &S = *kv.second;
+      const SiteData &sd = *S.site;
+      saved.push_back(double(it));
+      const std::string g = "/NrgItr" + std::to_string(it) + "/";
+      const size_t nq = sd.cur_q.empty() ? 0 : sd.cur_q[0].size();
+      std::vector<double> q;
+      for (auto &v : sd.cur_q) q.insert(q.end(), v.begin(), v.end());
+      put_array(fp, g + "current_sysmQ", q);
+      q.clear();
+      for (auto &v : sd.pre_q) q.insert(q.end(), v.begin(), v.end());
+      put_array(fp, g + "pre_sysmQ", q);
+      put_array(fp, g + "nq", std::vector<double>{double(nq)});
+      put_array(fp, g + "eigenvaluesQ_kept_indices", as_doubles(sd.kept_prev));
+      for (size_t sidx = 0; sidx < sd.cur_q.size(); ++sidx) {
+        const std::string k = std::to_string(sidx);
+        put_array(fp, g + "eigenvaluesQ/" + k, sidx < sd.E_host.size() ? sd.E_host[sidx] : std::vector<double>{});
+        put_array(fp, g + "coupled_nQ_index/" + k, as_doubles(sd.coupled[sidx]));
+        if (with_vectors) {  // current_hamiltonQ: eigenvectors as columns, row-major n x n
+          const Sector &Sc = sd.sectors[sidx];
+          std::vector<double> u;
+          if (Sc.dev >= 0) {
+            const DevBlock &db = sd.blocks[Sc.dev];
+            u.resize(size_t(db.n) * db.n);
+            check_cuda(cudaMemcpy2DAsync(u.data(), db.n * sizeof(double), db.U, db.ld * sizeof(double),
+                                         db.n * sizeof(double), db.n, cudaMemcpyDeviceToHost, e->stream),
+                       "export eigenvectors");
+            check_cuda(cudaStreamSynchronize(e->stream), "export eigenvectors");
+          }
+          put_array(fp, g + "current_hamiltonQ/" + k, u);
+        }
+      }
+      // the operator set saved with the shell (NrgData::saveqOperator layout:
+      // per operator the (row, col) block ids, their shapes and the blocks)
+      put_array(fp, g + "op/operatorSize", std::vector<double>{double(S.nops)});
+      for (int ip = 0; ip < S.nops; ++ip) {
+        const std::string og = g + "op/at" + std::to_string(ip) + "/";
+        std::vector<double> ids, rows, cols;
+        int ic = 0;
+        for (auto &b : S.ops) {
+          if (std::get<0>(b.first) != ip) continue;
+          const FBlock &B = b.second;
+          ids.push_back(std::get<1>(b.first));
+          ids.push_back(std::get<2>(b.first));
+          rows.push_back(B.rows);
+          cols.push_back(B.cols);
+          std::vector<double> m(size_t(B.rows) * B.cols);
+          if (!m.empty()) {
+            check_cuda(cudaMemcpy2DAsync(m.data(), B.cols * sizeof(double), B.p, B.ld * sizeof(double),
+                                         B.cols * sizeof(double), B.rows, cudaMemcpyDeviceToHost, e->stream),
+                       "export operator");
+            check_cuda(cudaStreamSynchronize(e->stream), "export operator");
+          }
+          put_array(fp, og + "qmat" + std::to_string(ic++), m);
+        }
+        put_array(fp, og + "idVector", ids);
+        put_array(fp, og + "rowVector", rows);
+        put_array(fp, og + "colVector", cols);
+      }
+    }
+    put_array(fp, "savedNRGIndex", saved);  // NrgData::saveFinalState (nrgData.hpp:106-110)
+    put_array(fp, "relativeGroundStateEnergy", r->relgs);
+    if (std::fflush(fp) != 0) fail(NRG_E_ARG, "export: write failed");
+  });
+}
+
 int nrg_fdm_create(nrg_run *r, int nops, nrg_fdm **out) {
   return guard([&] {
     if (!r || !out || nops <= 0) fail(NRG_E_ARG, "bad argument");
@@ -1240,6 +1342,8 @@ int nrg_thermo_calc(nrg_thermo *t, double scale) {
   });
 }
 
+}  // extern "C"
+
 namespace {
 // Discarded energies relative to each shell's minimum (flattened, with
 // offsets) and the one-step corrected shell ground energies
@@ -1266,6 +1370,8 @@ double regulate_exp_host(double x) {  // fdmThermodynamics.hpp:240-249
   return std::exp(std::min(100.0, std::max(-100.0, x)));
 }
 }  // namespace
+
+extern "C" {
 
 int nrg_thermo_final(nrg_thermo *t, double *entropy, double *cv) {
   return guard([&] {

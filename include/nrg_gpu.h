@@ -184,6 +184,20 @@ int nrg_opset_update_batch(nrg_opset *const *ops, int n);
 int nrg_opset_get_block(nrg_opset *ops, int ip, int64_t i, int64_t j, double *out, uint64_t cap,
                         int64_t *rows, int64_t *cols);
 
+/* Enumeration of the blocks behind nrg_opset_get_block / the f-dagger
+ * (getPreWilsonSiteOperators) / the loaded snapshot's operator set
+ * (NrgData::loadqOperator, nrgData.hpp:213-246): n = number of blocks; the
+ * first min(n, cap) (operator, row sector, column sector, rows, cols) are
+ * written to the arrays given (any may be NULL).  With these a host layer
+ * rebuilds a caller's vector<qOperator> (qOperator::getMap) block by block. */
+int nrg_opset_list_blocks(nrg_opset *ops, int *ip, int64_t *i, int64_t *j, int64_t *rows, int64_t *cols,
+                          uint64_t cap, uint64_t *n);
+int nrg_run_list_fdag_blocks(nrg_run *run, int *ip, int64_t *i, int64_t *j, int64_t *rows, int64_t *cols,
+                             uint64_t cap, uint64_t *n);
+int nrg_run_list_snapshot_ops(nrg_run *run, int *ip, int64_t *i, int64_t *j, int64_t *rows, int64_t *cols,
+                              uint64_t cap, uint64_t *n);
+int nrg_run_get_snapshot_op_block(nrg_run *run, int ip, int64_t i, int64_t j, double *out, uint64_t cap);
+
 /* ---- device-resident snapshots (NrgData, nrgData.hpp:134-293) ---------- */
 /* saveCurrentData + saveqOperator: keep this site's U, eigenvalues, kept
  * counts, sectors and the tracked operators on the device */

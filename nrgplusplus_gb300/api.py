@@ -66,7 +66,9 @@ EXPORTS = [
     "nrg_run_get_relgs", "nrg_run_get_sectors", "nrg_run_get_eigenvalues_q", "nrg_run_get_kept",
     "nrg_run_get_coupled", "nrg_run_get_eigenvectors", "nrg_run_get_fdag_block",
     "nrg_opset_create", "nrg_opset_destroy", "nrg_opset_update", "nrg_opset_update_batch", "nrg_opset_get_block",
-    "nrg_run_snapshot", "nrg_run_load_snapshot", "nrg_run_export_snapshots", "nrg_fdm_create", "nrg_fdm_destroy",
+    "nrg_run_snapshot", "nrg_run_load_snapshot", "nrg_run_export_snapshots",
+    "nrg_opset_list_blocks", "nrg_run_list_fdag_blocks", "nrg_run_list_snapshot_ops",
+    "nrg_run_get_snapshot_op_block", "nrg_fdm_create", "nrg_fdm_destroy",
     "nrg_fdm_calc", "nrg_fdm_calc_batch", "nrg_fdm_get", "nrg_broaden", "nrg_thermo_create", "nrg_thermo_destroy",
     "nrg_thermo_calc", "nrg_thermo_final", "nrg_thermo_set_operator", "nrg_thermo_get_operator",
     "nrg_fdm_set_temperature", "nrg_fdm_get_static", "nrg_batch_add_site", "nrg_batch_update_state",

@@ -1072,6 +1072,66 @@ int nrg_opset_get_block(nrg_opset *o, int ip, int64_t i, int64_t j, double *out,
   });
 }
 
+}  // extern "C"
+
+namespace {
+// Enumerates a block map: n = blocks; the first min(n, cap) of each array
+// written (any array may be null).
+void list_blocks(const std::map<OpKey, FBlock> &m, int *ip, int64_t *i, int64_t *j, int64_t *rows,
+                 int64_t *cols, uint64_t cap, uint64_t *n) {
+  if (!n) fail(NRG_E_ARG, "null argument");
+  uint64_t k = 0;
+  for (auto &kv : m) {
+    if (k < cap) {
+      if (ip) ip[k] = std::get<0>(kv.first);
+      if (i) i[k] = std::get<1>(kv.first);
+      if (j) j[k] = std::get<2>(kv.first);
+      if (rows) rows[k] = kv.second.rows;
+      if (cols) cols[k] = kv.second.cols;
+    }
+    ++k;
+  }
+  *n = k;
+}
+}  // namespace
+
+extern "C" {
+
+int nrg_opset_list_blocks(nrg_opset *o, int *ip, int64_t *i, int64_t *j, int64_t *rows, int64_t *cols,
+                          uint64_t cap, uint64_t *n) {
+  return guard([&] {
+    if (!o) fail(NRG_E_ARG, "null opset");
+    list_blocks(o->blocks, ip, i, j, rows, cols, cap, n);
+  });
+}
+
+int nrg_run_list_fdag_blocks(nrg_run *r, int *ip, int64_t *i, int64_t *j, int64_t *rows, int64_t *cols,
+                             uint64_t cap, uint64_t *n) {
+  return guard([&] {
+    if (!r) fail(NRG_E_ARG, "null run");
+    list_blocks(r->have_site ? r->fcur : r->fprev, ip, i, j, rows, cols, cap, n);
+  });
+}
+
+int nrg_run_list_snapshot_ops(nrg_run *r, int *ip, int64_t *i, int64_t *j, int64_t *rows, int64_t *cols,
+                              uint64_t cap, uint64_t *n) {
+  return guard([&] {
+    if (!r) fail(NRG_E_ARG, "null run");
+    if (!r->loaded) fail(NRG_E_STATE, "no snapshot loaded");
+    list_blocks(r->loaded->ops, ip, i, j, rows, cols, cap, n);
+  });
+}
+
+int nrg_run_get_snapshot_op_block(nrg_run *r, int ip, int64_t i, int64_t j, double *out, uint64_t cap) {
+  return guard([&] {
+    if (!r || !out) fail(NRG_E_ARG, "null argument");
+    if (!r->loaded) fail(NRG_E_STATE, "no snapshot loaded");
+    auto it = r->loaded->ops.find(OpKey{ip, int(i), int(j)});
+    if (it == r->loaded->ops.end()) fail(NRG_E_ARG, "no such block in the loaded snapshot");
+    copy_block(r->eng, it->second, out, cap);
+  });
+}
+
 int nrg_run_snapshot(nrg_run *r, nrg_opset *ops) {
   return guard([&] {
     if (!r) fail(NRG_E_ARG, "null run");

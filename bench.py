@@ -29,6 +29,8 @@ their blocks).  The reference publishes no number for this metric.
   serving    : the workload's runs as requests to the continuous-batching
                server, seeded Poisson arrivals at 80 % of the batch
                throughput: p50 / p99 latency and served runs/s
+  serving_mix: the seeded request mix (60 % SIAM, 25 % Kondo, 15 %
+               two-channel RG flows) under a 160 GB admission budget
   roofline   : the dominant kernel, useful work only (an FP64-accurate
                tensor-core product counts 2MNK, not its digit-plane
                products), plus the path-level (F_eig + F_rot) / t
@@ -128,6 +130,50 @@ def serving_run(engine, rate, n, seed=2024, max_active=None, workers=None):
             "p99_latency_s": st["p99_latency_s"], "mean_latency_s": st["mean_latency_s"],
             "max_active_seen": int(st["max_active_seen"]), "failed": int(st["failed"]),
             "arrivals": "Poisson, seeded; every request the full workload run (FDM + thermodynamics)"}
+
+
+def serving_mix_run(engine, rate, n, seed=None, max_active=None, workers=None, budget=160 * 10 ** 9):
+    """The serving mix: n seeded requests (60 % SIAM, 25 % Kondo, 15 %
+    two-channel RG flows; workloads.serving_mix) arriving as a seeded Poisson
+    stream at `rate` per second into a server with an HBM admission budget
+    of `budget` bytes."""
+    import threading
+    import numpy as np
+    from nrgplusplus_gb300 import api, workloads
+    seed = workloads.SERVING_SEED if seed is None else seed
+    max_active = BATCH if max_active is None else max_active
+    workers = ENGINES if workers is None else workers
+    mix = workloads.serving_mix(n, seed)
+    reqs = [workloads.mix_request(p) for p in mix]
+    gaps = np.random.default_rng(seed + 1).exponential(1.0 / rate, size=n)
+    srv = api.Server(engine, max_active=max_active, workers=workers, hbm_budget_bytes=budget)
+    ids = []
+
+    def arrivals():
+        for g, r in zip(gaps, reqs):
+            time.sleep(float(g))
+            ids.append(srv.submit(**r))
+
+    t0 = time.perf_counter()
+    th = threading.Thread(target=arrivals)
+    th.start()
+    th.join()
+    for i in ids:
+        srv.wait(i, 3600.0)
+        srv.result(i)
+    wall = time.perf_counter() - t0
+    st = srv.stats()
+    srv.close()
+    fam = {}
+    for p in mix:
+        fam.setdefault(p["kind"], []).append(p["nkeep"])
+    return {"requests": n, "arrival_rate_per_s": rate, "seed": seed, "hbm_budget_bytes": budget,
+            "max_active_per_worker": max_active, "workers": workers,
+            "families": {k: {"count": len(v), "nkeep": sorted(set(v))} for k, v in fam.items()},
+            "runs_per_s": st["completed"] / wall, "p50_latency_s": st["p50_latency_s"],
+            "p99_latency_s": st["p99_latency_s"], "mean_latency_s": st["mean_latency_s"],
+            "max_active_seen": int(st["max_active_seen"]), "failed": int(st["failed"]),
+            "what": "RG flows (all eigenvalues per site) of the seeded mix, 30-50 sites each"}
 
 
 def _dist():
@@ -691,7 +737,8 @@ def main():
     ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 comparator")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving-loop measurement")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
-    ap.add_argument("--serving-requests", type=int, default=48)
+    ap.add_argument("--serving-requests", type=int, default=24)
+    ap.add_argument("--mix-requests", type=int, default=48, help="requests of the serving mix (0: skip)")
     ap.add_argument("--sites", type=int, default=0,
                     help="Wilson sites per run (default: the workload's; fewer only for profiling captures)")
     args = ap.parse_args()
@@ -759,9 +806,12 @@ def main():
         sweep["mixed_runs_per_s"] = args.sweep_runs / t
     for e in engines[1:]:
         e.close()
-    serving = None
+    serving = mix = None
     if not args.no_serving and not reduced:
         serving = serving_run(engine, 0.8 * runs / per, args.serving_requests)
+        if args.mix_requests > 0:
+            rate = 0.8 * sweep["mixed_runs_per_s"] if sweep else 2.0
+            mix = serving_mix_run(engine, rate, args.mix_requests)
     engine.close()
     plain, got_fp64 = None, None
     if not args.no_fp64:
@@ -812,7 +862,8 @@ def main():
                 "hbm_peak_bytes": hbm_peak,
                 "e2e": {"value": e2e_v, "unit": "runs/s", "steps": len(e2e_times), "h2d_bytes_per_step": int(h2d),
                         "d2h_bytes_per_step": int(d2h)},
-                "plain_fp64": plain, "error": errors, "sweep": sweep, "serving": serving, "roofline": rf,
+                "plain_fp64": plain, "error": errors, "sweep": sweep, "serving": serving, "serving_mix": mix,
+                "roofline": rf,
                 "kernels_ms_per_engine_batch": {k: round(v[0], 3) for k, v in kt.items()},
                 "kernels_profiled": "one engine's %d-run batch alone, per-kernel CUDA events on its stream"
                                     % BATCH,

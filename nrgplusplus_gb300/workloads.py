@@ -186,3 +186,60 @@ def run_flow_batch(engine, instances, keep_eigs=True):
         for r in runs:
             r.close()
     return out
+
+
+def flow_request(kind, nkeep, nsites, lam, V=None, eps=-0.25, U=0.5, J=0.25):
+    """Server.submit keyword arguments of one RG-flow request (all
+    eigenvalues per site, no backward pass) for the model families the
+    serving mix draws: 'siam' (V site, then Wilson sites; rgflowSIAM form),
+    'kondo' (no V site, sqrt(Lambda) rescale from the first site;
+    rgflowKondo form, examples/rgflowKondo/main.cpp:20-31) and 'twochannel'
+    (four hoppings per site; examples/twoChannelSiam/main.cpp:24-40)."""
+    imp, bath = build_models(kind, eps, U, J)
+    nops = len(imp.fdag)
+    if kind in ("kondo", "zero"):
+        t = [[M.hopping(it, lam)] * nops for it in range(nsites)]
+        rescale = [math.sqrt(lam)] * nsites
+    else:
+        t = [[V] * nops] + [[M.hopping(it, lam)] * nops for it in range(nsites)]
+        rescale = [1.0] + [math.sqrt(lam) if it > 0 else 1.0 for it in range(nsites)]
+    return dict(impurity=imp, bath=bath, nkeep=nkeep, t=np.array(t), rescale=np.array(rescale),
+                keep_eigenvalues=True)
+
+
+SERVING_SEED = 20261204
+
+
+def serving_mix(n, seed=SERVING_SEED, nkeep_siam=(256, 512, 1024, 2048, 4096),
+                nkeep_kondo=(256, 512, 1024, 2048, 4096), nkeep_twochannel=(256, 512, 1024)):
+    """The seeded request mix of the serving workload: 60 % SIAM (parameters
+    drawn as in the sweep: U ~ U[0.05, 1], eps_d = -U/2 + U[-0.1, 0.1], V
+    log-uniform on [0.03, 0.3], Lambda in {2, 2.5, 3}), 25 % Kondo (J
+    log-uniform on [0.05, 0.3], Lambda = 2.5), 15 % two-channel SIAM (eps_d =
+    -0.3, U = 0.6, Lambda = 4, V ~ U[0.08, 0.15]); 30-50 Wilson sites; Nkeep
+    drawn per family from the given sets.  Returns [(family, params)]."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n):
+        u = float(rng.random())
+        ns = int(rng.integers(30, 51))
+        if u < 0.60:
+            U = float(rng.uniform(0.05, 1.0))
+            p = dict(kind="siam", U=U, eps=-0.5 * U + float(rng.uniform(-0.1, 0.1)),
+                     V=float(math.exp(rng.uniform(math.log(0.03), math.log(0.3)))),
+                     lam=float((2.0, 2.5, 3.0)[rng.integers(0, 3)]),
+                     nkeep=int(nkeep_siam[rng.integers(0, len(nkeep_siam))]), nsites=ns)
+        elif u < 0.85:
+            p = dict(kind="kondo", J=float(math.exp(rng.uniform(math.log(0.05), math.log(0.3)))), lam=2.5,
+                     nkeep=int(nkeep_kondo[rng.integers(0, len(nkeep_kondo))]), nsites=ns)
+        else:
+            p = dict(kind="twochannel", eps=-0.3, U=0.6, V=float(rng.uniform(0.08, 0.15)), lam=4.0,
+                     nkeep=int(nkeep_twochannel[rng.integers(0, len(nkeep_twochannel))]), nsites=ns)
+        out.append(p)
+    return out
+
+
+def mix_request(p):
+    """flow_request of one serving_mix entry."""
+    return flow_request(p["kind"], p["nkeep"], p["nsites"], p["lam"], V=p.get("V"), eps=p.get("eps", -0.25),
+                        U=p.get("U", 0.5), J=p.get("J", 0.25))

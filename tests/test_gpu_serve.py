@@ -181,3 +181,38 @@ def test_workers_give_the_same_results():
     eng.close()
     assert st["completed"] == 6 and st["failed"] == 0
     assert st["max_active_seen"] > 2  # more runs active than one worker may hold
+
+
+def test_model_mix_alone_and_in_mix_are_equal():
+    """A Kondo run (no V site, Lambda 2.5) and a two-channel run (four
+    hoppings per site, Lambda 4), each served alone and then in a mix with
+    SIAM runs of other Lambda and Nkeep that share its ticks: every site's
+    eigenvalues bit for bit."""
+    kondo = workloads.flow_request("kondo", 96, 12, 2.5, J=0.2)
+    twoch = workloads.flow_request("twochannel", 64, 6, 4.0, V=0.12, eps=-0.3, U=0.6)
+    eng = api.Engine(api.PREC_MIXED)
+    alone = []
+    for req in (kondo, twoch):
+        srv = api.Server(eng, max_active=1)
+        rid = srv.submit(**req)
+        assert srv.wait(rid)
+        alone.append(srv.result(rid)["eig"])
+        srv.close()
+    srv = api.Server(eng, max_active=8)
+    ids = [srv.submit(**workloads.flow_request("siam", 128, 10, 3.0, V=0.1, eps=-0.2, U=0.5)),
+           srv.submit(**kondo),
+           srv.submit(**workloads.flow_request("siam", 64, 14, 2.0, V=0.2, eps=-0.4, U=0.8)),
+           srv.submit(**twoch),
+           srv.submit(**workloads.flow_request("kondo", 80, 9, 2.5, J=0.08))]
+    got = []
+    for i in ids:
+        assert srv.wait(i)
+        got.append(srv.result(i)["eig"])
+    st = srv.stats()
+    srv.close()
+    eng.close()
+    assert st["completed"] == 5 and st["failed"] == 0 and st["max_active_seen"] > 1
+    for a, b in ((alone[0], got[1]), (alone[1], got[3])):
+        assert len(a) == len(b)
+        for x, y in zip(a, b):
+            assert np.array_equal(x, y)

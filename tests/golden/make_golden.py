@@ -56,6 +56,19 @@ def shipped_h5():
         print("shipped", tag, n, "iterations")
 
 
+def shipped_zaverage():
+    """The Wilson-chain coefficients shipped with independFiles/zAverage:
+    the flat band at z = 1, Lambda = 3 (hoppingElementsL3.h5, main.cpp) and
+    the pseudogap baths |e|^r, r = 1 and 1/2 (pseudoGap3.h5, pseudogap.cpp)."""
+    base = os.path.join(REF, "independFiles", "zAverage")
+    out = {"flat_tn_z1_L3": H5Mini(os.path.join(base, "hoppingElementsL3.h5")).read("tnZ1.000lmd3.000")}
+    h = H5Mini(os.path.join(base, "pseudoGap3.h5"))
+    for k in ("tnPseudo", "enPseudo", "tnPseudo2", "enPseudo2"):
+        out[k] = h.read(k)
+    np.savez_compressed(os.path.join(HERE, "shipped_zaverage.npz"), **out)
+    print("shipped zaverage")
+
+
 def run_ref(model, name, **kw):
     threads = os.environ.get("NRG_REF_THREADS", "8")
     env = dict(os.environ, OMP_NUM_THREADS=threads, OPENBLAS_NUM_THREADS=threads)
@@ -156,6 +169,7 @@ def sweep_cases(count=6):
 def main(which=None):
     if not which:
         shipped_h5()
+        shipped_zaverage()
     for name, model, params, opts in CASES + sweep_cases():
         if which and name not in which:
             continue

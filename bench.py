@@ -68,6 +68,14 @@ BATCH = int(os.environ.get("NRG_BENCH_BATCH", "0")) or WORK["batch"]      # runs
 ENGINES = int(os.environ.get("NRG_BENCH_ENGINES", "0")) or WORK["engines"]  # engines (host threads) per step
 
 
+def log(*a):
+    """Progress of the phases on stderr (the result line alone goes to stdout)."""
+    print("[bench %.0f s]" % (time.perf_counter() - T0), *a, file=sys.stderr, flush=True)
+
+
+T0 = time.perf_counter()
+
+
 def select_workload(name):
     global WORK, NAME, BATCH, ENGINES
     if name not in WORKLOADS:
@@ -398,7 +406,7 @@ class CpuBaseline:
                 os.environ[k] = "1"
             try:
                 self.pool = mp.get_context("spawn").Pool(self.cores)
-                self.pool.map(_cpu_sample, [(dict(WORK, nkeep=16), 1)] * self.cores)  # imports done
+                self.pool.starmap(_cpu_sample, [(dict(WORK, nkeep=16), 1)] * self.cores)  # imports done
             finally:
                 for k, v in old.items():
                     if v is None:
@@ -744,7 +752,7 @@ def main():
     args = ap.parse_args()
     select_workload(args.workload)
     if not args.cpu_sites:
-        args.cpu_sites = 12 if WORK["nkeep"] >= 2048 else 20
+        args.cpu_sites = 14 if WORK["nkeep"] >= 2048 else 20
     reduced = bool(args.sites) and args.sites != WORK["nsites"]
     if reduced:
         WORK["nsites"] = args.sites
@@ -770,6 +778,7 @@ def main():
             torch.distributed.barrier()
         torch.cuda.synchronize()
 
+    log("workload", NAME, "engines", ENGINES, "runs per engine", BATCH, "FP64 peak %.3f TFLOP/s" % fp64_peak)
     got_mixed = None
     for w in range(max(1, args.warmup)):
         _, _, got = step(engines, e2e=False, collect=(w == 0 and not reduced))
@@ -782,6 +791,8 @@ def main():
         e2e_times, h2d, d2h, _ = timed_steps(engines, max(1, args.e2e_steps), True, barrier, flush)
     clocks = clk.summary()
     runs = ENGINES * BATCH
+    log("mixed: %d steps, %.3f s/step; e2e %.3f s/step" % (len(times), sum(times) / len(times),
+                                                          sum(e2e_times) / len(e2e_times)))
     tsum, esum = max_over_ranks([sum(times), sum(e2e_times)])
     per = tsum / args.steps
     value = ws * runs / per
@@ -794,6 +805,7 @@ def main():
     path["frac_of_fp64_peak"] = path["achieved"] / fp64_peak
     kt, wc = kernel_profile(engine)
     rf = roofline_from(kt, wc, fp64_peak)
+    log("kernels (ms per engine batch):", {k: round(v[0], 1) for k, v in kt.items()})
     rf["path"] = path
     fallbacks = sum(e.fallback_count() for e in engines)
     hbm_peak = sum(e.memory()[1] for e in engines)
@@ -804,14 +816,17 @@ def main():
                          "one heterogeneous batch per engine, one pass after the workload warmed the engines"}
         t = sweep_pass(engines, args.sweep_runs)
         sweep["mixed_runs_per_s"] = args.sweep_runs / t
+        log("sweep mixed: %.3f runs/s" % sweep["mixed_runs_per_s"])
     for e in engines[1:]:
         e.close()
     serving = mix = None
     if not args.no_serving and not reduced:
         serving = serving_run(engine, 0.8 * runs / per, args.serving_requests)
+        log("serving:", serving)
         if args.mix_requests > 0:
             rate = 0.8 * sweep["mixed_runs_per_s"] if sweep else 2.0
             mix = serving_mix_run(engine, rate, args.mix_requests)
+            log("serving mix:", mix)
     engine.close()
     plain, got_fp64 = None, None
     if not args.no_fp64:
@@ -819,6 +834,7 @@ def main():
         _, _, got_fp64 = step(e64s, e2e=False, collect=not reduced)  # warm-up
         t64s, _, _, work64 = timed_steps(e64s, max(1, args.fp64_steps), False, barrier, flush)
         t64 = max_over_ranks([sum(t64s)])[0] / len(t64s)
+        log("fp64: %.3f s/step" % t64)
         kt64, wc64 = kernel_profile(e64s[0])
         rf64 = roofline_from(kt64, wc64, fp64_peak)
         p64 = path_roofline(work64, sum(t64s), fp64_peak, "of measured (cuBLAS DGEMM 8192^3 in this run)",
@@ -829,6 +845,7 @@ def main():
         if sweep is not None:
             sweep["fp64_runs_per_s"] = args.sweep_runs / sweep_pass(e64s, args.sweep_runs)
             sweep["speedup_mixed_over_fp64"] = sweep["mixed_runs_per_s"] / sweep["fp64_runs_per_s"]
+            log("sweep fp64: %.3f runs/s" % sweep["fp64_runs_per_s"])
         for e in e64s:
             e.close()
         plain = {"value": ws * runs / t64, "unit": "runs/s", "ms_per_step": t64 * 1e3,
@@ -841,6 +858,7 @@ def main():
         e0 = api.Engine(api.PREC_FP64, device=local)
         errors = output_errors(e0, got_mixed, got_fp64)
         e0.close()
+        log("errors:", errors)
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
         cb = CpuBaseline(args.cpu_sites)
@@ -848,6 +866,7 @@ def main():
             cpu = cb.best()
         finally:
             cb.close()
+        log("cpu:", cpu)
     if rank == 0:
         cfg = dict(config(), precision_path="mixed: FP32 block solve + FP64-accurate refinement on "
                                             "tensor cores; FP64 for refinement, rescale and Boltzmann sums")

@@ -75,12 +75,13 @@ def run_nrg(engine, kind, nkeep, nsites, lam, V=None, eps=-0.25, U=0.5, J=0.25, 
             out["kept"].append(run.kept_counts)
     out["min_it"] = min_it
     out["nsites"] = nsites
+    last = run.nrg_iterations_cnt  # loadCurrentData moves the counter (nrgData.hpp:273)
 
     def thermo_pass(temps):
         th = api.FdmThermodynamics(run, temps)
         if with_nd:
             th.setSystemOperator([2])
-        cnt = run.nrg_iterations_cnt
+        cnt = last
         lo = min_it + (1 if kondo else 0)
         for it in range(nsites, lo, -1):
             cnt -= 1
@@ -97,7 +98,7 @@ def run_nrg(engine, kind, nkeep, nsites, lam, V=None, eps=-0.25, U=0.5, J=0.25, 
         f = api.FdmSpectrum(run, ops.nops)
         if tw is not None:
             f.setTemperature(fdm_T, tw)
-        cnt = run.nrg_iterations_cnt
+        cnt = last
         for it in range(nsites, min_it, -1):
             cnt -= 1
             data.loadCurrentData(cnt)

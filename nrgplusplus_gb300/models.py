@@ -7,6 +7,8 @@ restating the reference's model builders:
 * ``spinhalf``       - models/spinhalf.hpp:81-124
 * ``spinhalf_kondo`` - models/spinhalfKondo.hpp:28-166
 * ``two_channel``    - src/models/twoChannel.cpp:12-45
+* ``spinhalf_sc``, ``sc_bath`` - models/spinhalfSC.hpp:26-125 (S_z-only sectors,
+  pairing bath refreshed per site)
 * ``d_dag_chi``      - the d-dagger-chi operators of examples/fdmSpectrumSiam/main.cpp:40-60
 
 A :class:`Site` carries exactly what ``nrgcore`` reads from a model
@@ -179,6 +181,41 @@ def spinhalf_kondo(J, S=0.5):
                     d[(i, j)] = vecs[i].T @ sub @ vecs[j]
         fdag.append(d)
     return Site(qnums, energies, _chi(qnums), fdag)
+
+
+def _rotated_site(fb, H):
+    """Sector eigenvalues of H and the f-dagger blocks rotated into the
+    sector eigenbases, U_i^T f U_j (spinhalfSC.hpp:57-84)."""
+    energies, vecs = [], []
+    for b in fb.block_diag(H):
+        w, v = np.linalg.eigh(b)
+        energies.append(w)
+        vecs.append(v)
+    fdag = []
+    for d in fb.block_operators(fb.raw_fdag):
+        fdag.append({(i, j): vecs[i].T @ m @ vecs[j] for (i, j), m in d.items()})
+    return Site(list(fb.qnums), energies, _chi(fb.qnums), fdag, {"basis": fb})
+
+
+def spinhalf_sc(eps, U, h=0.0):
+    """Spin-1/2 site with S_z as its only quantum number, for baths with a
+    pairing term (models/spinhalfSC.hpp:26-85): H = eps n + h (n_up - n_down)
+    + U n_up n_down, sectors S_z = 0, +1, -1, f-dagger in the sector
+    eigenbasis."""
+    fb = FermionBasis(2, SPIN_ONLY)
+    fu, fd = fb.raw_fdag
+    nu, nd = fu @ fu.T, fd @ fd.T
+    return _rotated_site(fb, (nu + nd) * eps + (nu - nd) * h + (nu @ nd) * U)
+
+
+def sc_bath(delta):
+    """spinhalfSC::addSCDelta (spinhalfSC.hpp:87-125): the site Hamiltonian
+    replaced by the s-wave pairing delta (c_up c_down + c_down^+ c_up^+);
+    a Wilson site of a superconducting bath, refreshed every site
+    (nrgcore.hpp:68-70)."""
+    fb = FermionBasis(2, SPIN_ONLY)
+    fu, fd = fb.raw_fdag
+    return _rotated_site(fb, (fu.T @ fd.T + fd @ fu) * delta)
 
 
 def two_channel():

@@ -139,6 +139,25 @@ def siam_request(nkeep, nsites, lam, V, eps=-0.25, U=0.5, fdm=False, thermo=Fals
                 first_shell_site=1, keep_eigenvalues=keep_eigs)
 
 
+def run_sc(engine, nkeep, nsites, lam, V, eps, U, delta, keep_eigs=True):
+    """SIAM coupled to a superconducting bath: S_z-only sectors
+    (models.spinhalf_sc) and a pairing delta Lambda^(n/2) on Wilson site n
+    (delta on the V site), the bath refreshed before every site through
+    set_bath, as nrgcore re-reads its bath model (nrgcore.hpp:68-70)."""
+    run = api.NrgCore(engine, M.spinhalf_sc(eps, U), M.sc_bath(delta), nkeep)
+    out = {"eig": [], "kept": [], "run": run}
+    run.add_bath_site([V, V], 1.0)
+    run.update_internal_state()
+    for it in range(nsites):
+        run.set_bath(M.sc_bath(delta * lam ** (0.5 * it)))
+        run.add_bath_site([M.hopping(it, lam)] * 2, math.sqrt(lam) if it > 0 else 1.0)
+        run.update_internal_state()
+        if keep_eigs:
+            out["eig"].append(run.all_eigenvalue)
+            out["kept"].append(run.kept_counts)
+    return out
+
+
 SWEEP_SEED = 20260512
 
 

@@ -12,7 +12,7 @@
 // with HDF5 snapshots (nrgData.hpp) replaced by in-memory copies of the same
 // public members that nrgData.hpp:150-157 saves.
 //
-// usage: ref_nrg <siam|kondo|twochannel> <out.bin> key=value ...
+// usage: ref_nrg <siam|kondo|twochannel|zero|sc> <out.bin> key=value ...
 //   keys: eps U V J lambda nkeep nsites fdm thermo dumpops opsites sysop
 //   sysop=1 (with thermo): the impurity occupancy n_d is tracked through
 //   update_system_operator and handed to fdmThermodynamics::setSystemOperator
@@ -22,12 +22,14 @@
 #include "models/fermionBasis.hpp"
 #include "models/spinhalf.hpp"
 #include "models/spinhalfKondo.hpp"
+#include "models/spinhalfSC.hpp"
 #include "models/twoChannel.hpp"
 #include "nrgcore/nrgcore.hpp"
 #include "nrgcore/sysOperator.hpp"
 #include "static/fdmThermodynamics.hpp"
 #include <cstdio>
 #include <cstdlib>
+#include <functional>
 #include <map>
 #include <string>
 #include <vector>
@@ -78,7 +80,7 @@ template <class N> static void dump_ops(Out &o, std::vector<qOperator> &ops, con
 
 template <class IMP, class BATH>
 static void run(IMP &imp, BATH &bath, std::map<std::string, double> &P, bool firstV, bool kondoRescale,
-                int nops, Out &o) {
+                int nops, Out &o, std::function<void(int)> pre_site = nullptr) {
   double L = P["lambda"], V = P["V"];
   size_t nk = size_t(P["nkeep"]);
   int nMax = int(P["nsites"]);
@@ -120,6 +122,7 @@ static void run(IMP &imp, BATH &bath, std::map<std::string, double> &P, bool fir
   };
   if (firstV) {
     std::vector<double> t(nops, V);
+    if (pre_site) pre_site(-1);
     n.add_bath_site(t, 1.0);
     if (fdm) update_system_operator(&n, d);
     if (sysop) update_system_operator(&n, nd);
@@ -129,6 +132,7 @@ static void run(IMP &imp, BATH &bath, std::map<std::string, double> &P, bool fir
   for (int in = 0; in < nMax; in++) {
     double r = kondoRescale ? std::sqrt(L) : (in > 0 ? std::sqrt(L) : 1.0);
     std::vector<double> t(nops, hopping(in, L));
+    if (pre_site) pre_site(in);
     n.add_bath_site(t, r);
     if (fdm) update_system_operator(&n, d);
     if (sysop) update_system_operator(&n, nd);
@@ -198,7 +202,7 @@ int main(int argc, char **argv) {
   std::string model = argv[1];
   std::map<std::string, double> P = {{"eps", -0.25}, {"U", 0.5},  {"V", 0.1},   {"J", 0.25},
                                      {"lambda", 2.0}, {"nkeep", 512}, {"nsites", 40}, {"fdm", 0},
-                                     {"thermo", 0},  {"dumpops", 0},  {"sysop", 0}};
+                                     {"thermo", 0},  {"dumpops", 0},  {"sysop", 0}, {"delta", 0}};
   for (int i = 3; i < argc; i++) {
     std::string a = argv[i];
     auto p = a.find('=');
@@ -221,6 +225,14 @@ int main(int argc, char **argv) {
     imp.f_dag_operator.push_back(imp.f_dag_operator[1]);
     twoChannel bath;
     run(imp, bath, P, true, false, 4, o);
+  } else if (model == "sc") {
+    // superconducting bath: spinhalfSC sites (S_z sectors only) whose pairing
+    // is refreshed before every site, delta Lambda^(n/2) at Wilson site n
+    // (delta at the V site); models/spinhalfSC.hpp:26-125, nrgcore.hpp:68-70
+    spinhalfSC imp(P["eps"], P["U"], 0.0), bath(0, 0, 0);
+    const double delta = P["delta"], L = P["lambda"];
+    run(imp, bath, P, true, false, 2, o,
+        [&](int site) { bath.addSCDelta(site < 0 ? delta : delta * std::pow(L, 0.5 * site)); });
   } else {
     fprintf(stderr, "unknown model %s\n", model.c_str());
     return 2;

@@ -144,6 +144,9 @@ CASES = [
     ("ref_siam_thermo_nd_nk256", "siam",
      dict(eps=-0.25, U=0.8, V=0.15, **{"lambda": 2.0}, nkeep=256, nsites=30, thermo=1, sysop=1),
      {"with_thermo": True}),
+    # superconducting bath (S_z sectors, pairing refreshed before every site)
+    ("ref_sc_nk256", "sc",
+     dict(eps=-0.3, U=0.6, V=0.12, **{"lambda": 2.0}, nkeep=256, nsites=20, delta=0.001), {}),
     ("ref_twochannel_nk256", "twochannel",
      dict(eps=-0.3, U=0.6, V=0.12, **{"lambda": 4.0}, nkeep=256, nsites=8), {}),
 ]

@@ -98,3 +98,18 @@ def test_sweep_instances_batched(gpu_engine, mixed_engine, path):
         check_eigs(f, o["eig"], p["lam"], niter=n)
         for i in range(n):
             assert np.array_equal(np.array(o["kept"][i]), f["kept%d" % i]), (k, i)
+
+
+@pytest.mark.parametrize("path", ["fp64", "mixed"])
+def test_superconducting_bath_against_reference(gpu_engine, mixed_engine, path):
+    """S_z-only sectors (one quantum number) and a pairing bath refreshed
+    before every site (set_bath), against the reference's run."""
+    eng = gpu_engine if path == "fp64" else mixed_engine
+    fx = golden("ref_sc_nk256")
+    out = workloads.run_sc(eng, 256, 20, 2.0, V=0.12, eps=-0.3, U=0.6, delta=0.001)
+    try:
+        check_eigs(fx, out["eig"], 2.0)
+        for i in range(20):
+            assert np.array_equal(np.array(out["kept"][i]), fx["kept%d" % i]), i
+    finally:
+        out["run"].close()

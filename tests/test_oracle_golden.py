@@ -203,3 +203,21 @@ def test_finite_t_fdm_low_temperature_limit():
     rt = _nd_run(fdm=True, fdm_T=T)
     for a, b in ((r0["pos"], rt["pos"]), (r0["neg"], rt["neg"])):
         assert np.abs(a - b).max() < 1e-12
+
+
+def test_ref_superconducting_bath():
+    """S_z-only sectors and a bath refreshed before every site (the pairing
+    grows as Lambda^(n/2) in iteration units) against the reference."""
+    fx = golden("ref_sc_nk256")
+    delta, lam = 0.001, 2.0
+    n = NrgOracle(M.spinhalf_sc(-0.3, 0.6), M.sc_bath(delta), 256)
+    n.add_bath_site([0.12, 0.12], 1.0, full_fdag=False)
+    n.update_internal_state()
+    eigs = []
+    for it in range(20):
+        n.bath = M.sc_bath(delta * lam ** (0.5 * it))
+        n.add_bath_site([M.hopping(it, lam)] * 2, math.sqrt(lam) if it else 1.0, full_fdag=False)
+        n.update_internal_state()
+        eigs.append(n.all_eigenvalue.copy())
+        assert np.array_equal(np.array(n.kept), fx["kept%d" % it]), it
+    check_eigs(fx, eigs, lam)

@@ -557,13 +557,13 @@ def kernel_models(fp64_peak):
 MEASURED_TRAFFIC = {"k_gemm_oz": 221.0e6}
 
 
-def kernel_profile(engine):
+def kernel_profile(engine, batch=None):
     """One extra engine batch with per-kernel CUDA events on the engine
     stream; returns ({kernel: (ms, work, launches)}, work counters)."""
     engine.set_profiling(True)
     engine.kernel_times()
     engine.work_counters(reset=True)
-    one_run(engine, e2e=False)
+    one_run(engine, e2e=False, batch=batch)
     kt = engine.kernel_times()
     wc = engine.work_counters(reset=True)
     engine.set_profiling(False)
@@ -699,7 +699,7 @@ def sweep_pass(engines, count):
 
 
 # -------------------------------------------------------------------- main
-def timed_steps(engines, k, e2e, barrier, flush):
+def timed_steps(engines, k, e2e, barrier, flush, batch=None):
     """k timed steps (L2 flushed before each, barrier + sync on both sides);
     returns (seconds per step list, h2d, d2h, algorithmic work of the steps)."""
     times, h2d, d2h = [], 0, 0
@@ -709,7 +709,7 @@ def timed_steps(engines, k, e2e, barrier, flush):
         flush.zero_()
         barrier()
         t0 = time.perf_counter()
-        h2d, d2h, _ = step(engines, e2e=e2e)
+        h2d, d2h, _ = step(engines, e2e=e2e, batch=batch)
         for e in engines:
             e.sync()
         barrier()
@@ -740,13 +740,15 @@ def main():
                     help="Wilson sites of one bounded CPU-baseline sample (default: per workload)")
     ap.add_argument("--e2e-steps", type=int, default=3, help="timed steps of the e2e measurement")
     ap.add_argument("--fp64-steps", type=int, default=3, help="timed steps of the plain FP64 comparator")
-    ap.add_argument("--sweep-runs", type=int, default=48,
+    ap.add_argument("--fp64-batch", type=int, default=0,
+                    help="runs per engine of the FP64 comparator (default: as the mixed path)")
+    ap.add_argument("--sweep-runs", type=int, default=32,
                     help="instances of the seeded sweep timed on both paths (0: skip)")
     ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 comparator")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving-loop measurement")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--serving-requests", type=int, default=24)
-    ap.add_argument("--mix-requests", type=int, default=48, help="requests of the serving mix (0: skip)")
+    ap.add_argument("--mix-requests", type=int, default=32, help="requests of the serving mix (0: skip)")
     ap.add_argument("--sites", type=int, default=0,
                     help="Wilson sites per run (default: the workload's; fewer only for profiling captures)")
     args = ap.parse_args()
@@ -831,16 +833,17 @@ def main():
     plain, got_fp64 = None, None
     if not args.no_fp64:
         e64s = [api.Engine(api.PREC_FP64, device=local) for _ in range(ENGINES)]
-        _, _, got_fp64 = step(e64s, e2e=False, collect=not reduced)  # warm-up
-        t64s, _, _, work64 = timed_steps(e64s, max(1, args.fp64_steps), False, barrier, flush)
+        b64 = args.fp64_batch or BATCH
+        _, _, got_fp64 = step(e64s, e2e=False, batch=b64, collect=not reduced)  # warm-up
+        t64s, _, _, work64 = timed_steps(e64s, max(1, args.fp64_steps), False, barrier, flush, batch=b64)
         t64 = max_over_ranks([sum(t64s)])[0] / len(t64s)
         log("fp64: %.3f s/step" % t64)
-        kt64, wc64 = kernel_profile(e64s[0])
+        kt64, wc64 = kernel_profile(e64s[0], b64)
         rf64 = roofline_from(kt64, wc64, fp64_peak)
         p64 = path_roofline(work64, sum(t64s), fp64_peak, "of measured (cuBLAS DGEMM 8192^3 in this run)",
                             "fp64")
-        p64["F_eig_per_run"] = work64["F_eig"] / (runs * len(t64s))
-        p64["F_rot_per_run"] = work64["F_rot"] / (runs * len(t64s))
+        p64["F_eig_per_run"] = work64["F_eig"] / (ENGINES * b64 * len(t64s))
+        p64["F_rot_per_run"] = work64["F_rot"] / (ENGINES * b64 * len(t64s))
         rf64["path"] = p64
         if sweep is not None:
             sweep["fp64_runs_per_s"] = args.sweep_runs / sweep_pass(e64s, args.sweep_runs)
@@ -848,8 +851,9 @@ def main():
             log("sweep fp64: %.3f runs/s" % sweep["fp64_runs_per_s"])
         for e in e64s:
             e.close()
-        plain = {"value": ws * runs / t64, "unit": "runs/s", "ms_per_step": t64 * 1e3,
-                 "steps": len(t64s), "warmup": 1, "speedup_mixed_over_fp64": value / (ws * runs / t64),
+        runs64 = ENGINES * b64
+        plain = {"value": ws * runs64 / t64, "unit": "runs/s", "ms_per_step": t64 * 1e3, "runs_per_step": runs64,
+                 "steps": len(t64s), "warmup": 1, "speedup_mixed_over_fp64": value / (ws * runs64 / t64),
                  "fp64_peak_tflops": fp64_peak, "fp64_peak_source": "cuBLAS DGEMM 8192^3 via torch.matmul, "
                  "best of 5, CUDA events (this run)", "roofline": rf64,
                  "kernels_ms_per_engine_batch": {k: round(v[0], 3) for k, v in kt64.items()}}

@@ -53,7 +53,16 @@ int main(int argc, char **argv) {
     size_t kept = 0;
     for (auto &k : siam.eigenvaluesQ_kept_indices) kept += k.size();
     if (kept < nkeep) throw std::runtime_error("eigenvaluesQ_kept_indices: fewer kept states than Nkeep");
-    if (siam.get_basis_nQ().empty() && siam.pre_sysmQ.empty()) throw std::runtime_error("no sectors");
+    // as in the reference, update_internal_state moved current_sysmQ into
+    // pre_sysmQ (nrgcore.hpp:105-109), so get_basis_nQ() throws here
+    bool threw = false;
+    try {
+      siam.get_basis_nQ();
+    } catch (const std::runtime_error &) {
+      threw = true;
+    }
+    if (!threw || siam.pre_sysmQ.empty() || siam.get_eigenvaluesQ().size() != siam.pre_sysmQ.size())
+      throw std::runtime_error("sector members");
     if (siam.nq_bath.size() != bathModel.get_basis().size()) throw std::runtime_error("nq_bath");
     auto *fdag = siam.getPreWilsonSiteOperators();
     if (fdag->size() != impurity.f_dag_operator.size() || (*fdag)[0].getMap()->empty())

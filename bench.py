@@ -897,5 +897,26 @@ def main():
     return 0
 
 
+def _close_engines():
+    """Close every engine still open (after a failure, before the CUDA
+    context goes away at exit)."""
+    import gc
+    try:
+        from nrgplusplus_gb300 import api
+    except Exception:
+        return
+    for obj in gc.get_objects():
+        if isinstance(obj, api.Engine):
+            try:
+                obj.close()
+            except Exception:
+                pass
+
+
 if __name__ == "__main__":
-    sys.exit(main())
+    try:
+        rc = main()
+    except BaseException:
+        _close_engines()
+        raise
+    sys.exit(rc)

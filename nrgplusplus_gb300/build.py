@@ -17,7 +17,7 @@ LIB = os.path.join(HERE, "libnrggpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 
-SOURCES = ["k_assemble.cu", "k_eig.cu", "k_gemm.cu", "k_trunc.cu", "k_fdm.cu", "k_refine.cu", "k_ozaki.cu",
+SOURCES = ["k_assemble.cu", "k_eig.cu", "k_eig_cluster.cu", "k_gemm.cu", "k_trunc.cu", "k_fdm.cu", "k_refine.cu", "k_ozaki.cu",
            "noalloc.cu", "engine.cpp", "engine_api.cpp",
            "serve.cpp"]
 

@@ -138,17 +138,31 @@ void check_kernel_error(nrg_engine *e) {
 
 static void post_launch(const char *what) { check_cuda(cudaGetLastError(), what); }
 
-void ensure_smem_limit(const void *kernel, int bytes) {
+void ensure_nonportable_cluster(const void *kernel) {
   static std::mutex mu;
-  static std::set<std::tuple<const void *, int, int>> done;  // (kernel, device, bytes)
+  static std::set<std::pair<const void *, int>> done;
   int dev = 0;
   check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
   std::lock_guard<std::mutex> lk(mu);
-  const auto key = std::make_tuple(kernel, dev, bytes);
-  if (done.count(key)) return;
+  if (done.count({kernel, dev})) return;
+  check_cuda(cudaFuncSetAttribute(kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1),
+             "cudaFuncSetAttribute(non-portable cluster size)");
+  done.insert({kernel, dev});
+}
+
+void ensure_smem_limit(const void *kernel, int bytes) {
+  // the attribute only ever grows: a launch needing less than the limit set
+  // for an earlier launch is fine, one needing more raises it
+  static std::mutex mu;
+  static std::map<std::pair<const void *, int>, int> limit;  // (kernel, device) -> bytes set
+  int dev = 0;
+  check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
+  std::lock_guard<std::mutex> lk(mu);
+  int &cur = limit[{kernel, dev}];
+  if (bytes <= cur) return;
   check_cuda(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes),
              "cudaFuncSetAttribute(dynamic shared memory)");
-  done.insert(key);
+  cur = bytes;
 }
 
 // ---------------------------------------------------------------- models
@@ -380,16 +394,17 @@ static cudaEvent_t take_event(nrg_engine *e) {
   return x;
 }
 
-Prof::Prof(nrg_engine *eng, const char *nm, double w) : e(eng), name(nm), work(w) {
+Prof::Prof(nrg_engine *eng, const char *nm, double w, cudaStream_t st)
+    : e(eng), name(nm), work(w), s(st ? st : eng->stream) {
   if (e->profile) {
     a = take_event(e);
-    cudaEventRecord(a, e->stream);
+    cudaEventRecord(a, s);
   }
 }
 Prof::~Prof() {
   if (a) {
     cudaEvent_t b = take_event(e);
-    cudaEventRecord(b, e->stream);
+    cudaEventRecord(b, s);
     e->prof.push_back({name, a, b, work});
   }
 }
@@ -675,17 +690,51 @@ static MixedStatus mixed_eigensolve(nrg_engine *e, std::vector<DevBlock *> &blks
     eb64[b].ld = blks[b]->ld;
     eb64[b].ldu = blks[b]->ld;
   }
+  // blocks above the one-CTA shared-memory limit that a cluster's distributed
+  // shared memory holds go to k_eig_cluster, the others to k_eig_bi
+  std::vector<EigBlock> eb_one, eb_cl;
+  int max_one = 0, max_cl = 0;
+  for (size_t b = 0; b < nb; ++b) {
+    if (e->eig_cluster && eb[b].n > e->eig_smem_f32 && eig_cluster_size_for(eb[b].n, false) > 0) {
+      eb_cl.push_back(eb[b]);
+      max_cl = std::max(max_cl, eb[b].n);
+    } else {
+      eb_one.push_back(eb[b]);
+      max_one = std::max(max_one, eb[b].n);
+    }
+  }
   Arena a;
   size_t oeb = a.add(eb), ost = a.add(stat), obt = a.add(bt_tiles), oeb64 = a.add(eb64), ost64 = a.add(stat);
   const size_t orb = a.add(rb);  // filled per step below (host copy re-uploaded)
+  const size_t oone = a.add(eb_one), ocl = a.add(eb_cl);
   DevPtr dd;
   char *dp = a.push(e, dd);
   hold.push_back(dd);
-  {
-    Prof pf(e, "k_eig_bi_f32", eig_flops(eb) * 0.4);  // tridiagonal reduction + Q: 4/3 n^3
-    launch_eig_bisect_f32(at<EigBlock>(dp, oeb), int(nb), max_n, e->eig_smem_f32, s);
+  // the one-CTA solver runs on the side stream, beside the cluster solver
+  const bool fork = !eb_cl.empty() && !eb_one.empty();
+  if (fork) {
+    check_cuda(cudaEventRecord(e->fork_ev, s), "fork");
+    check_cuda(cudaStreamWaitEvent(e->side, e->fork_ev, 0), "fork");
+  }
+  if (!eb_cl.empty()) {
+    Prof pf(e, "k_eig_cluster_f32", eig_flops(eb_cl) * 0.4);  // tridiagonal reduction: 4/3 n^3
+    const int cs = eig_cluster_size_for(max_cl, false);
+    const std::string what = "eigensolve f32 (cluster of " + std::to_string(cs) + " CTAs, " +
+                             std::to_string(eb_cl.size()) + " blocks, largest " + std::to_string(max_cl) + ")";
+    check_cuda(launch_eig_cluster(at<EigBlock>(dp, ocl), int(eb_cl.size()), max_cl, cs, false, s), what.c_str());
+    count_launch(e);
+    post_launch("eigensolve f32 (cluster)");
+  }
+  if (!eb_one.empty()) {
+    cudaStream_t so = fork ? e->side : s;
+    Prof pf(e, "k_eig_bi_f32", eig_flops(eb_one) * 0.4, so);  // tridiagonal reduction: 4/3 n^3
+    launch_eig_bisect_f32(at<EigBlock>(dp, oone), int(eb_one.size()), max_one, e->eig_smem_f32, so);
     count_launch(e);
     post_launch("eigensolve f32");
+  }
+  if (fork) {
+    check_cuda(cudaEventRecord(e->join_ev, e->side), "join");
+    check_cuda(cudaStreamWaitEvent(s, e->join_ev, 0), "join");
   }
   {
     double f = 0;  // applying the reflectors: 2 n^3 per block
@@ -982,11 +1031,48 @@ static void batch_add_site(nrg_run *const *runs, int nruns, const double *t, int
   for (int o : order) eblk_sorted.push_back(eblk[o]);
   e->work[0] += eig_flops(eblk);
   elem_block.insert(elem_block.end(), block_run.begin(), block_run.end());
+  // FP64 path: blocks above the one-CTA shared-memory limit that a cluster
+  // holds are solved by the reflector solver (k_eig_cluster<double> +
+  // k_reflect<double>, the mixed path's first stage in FP64) and moved to the
+  // end of the list; the others by k_eig<double> (tred2 + QL)
+  int n_f64 = int(eblk_sorted.size()), max_cl64 = 0, tw64 = 8, panel64 = 1;
+  std::vector<int2> tiles64;
+  if (e->precision == NRG_PREC_FP64 && e->eig_cluster) {
+    std::vector<EigBlock> one, cl;
+    int64_t wsz = 0;
+    for (auto &b : eblk_sorted) {
+      if (b.n > e->eig_smem_f64 && eig_cluster_size_for(b.n, true) > 0 && reflect_config(b.n, &tw64, &panel64, true)) {
+        cl.push_back(b);
+        wsz += int64_t(b.n) * b.ld;
+        max_cl64 = std::max(max_cl64, b.n);
+      } else {
+        one.push_back(b);
+      }
+    }
+    if (!cl.empty()) {
+      reflect_config(max_cl64, &tw64, &panel64, true);
+      DevPtr w = dalloc(e, 3 * wsz * sizeof(double) + 16);
+      hold.push_back(w);
+      double *base = static_cast<double *>(w->ptr);
+      int64_t o = 0;
+      for (size_t k = 0; k < cl.size(); ++k) {
+        EigBlock &b = cl[k];
+        b.W64 = base + o;
+        b.V64 = base + wsz + o;
+        b.Bt64 = base + 2 * wsz + o;
+        o += int64_t(b.n) * b.ld;
+        for (int tn = 0; tn < (b.n + tw64 - 1) / tw64; ++tn) tiles64.push_back(make_int2(int(k), tn));
+      }
+      n_f64 = int(one.size());
+      eblk_sorted = one;
+      eblk_sorted.insert(eblk_sorted.end(), cl.begin(), cl.end());
+    }
+  }
 
   Arena ar;
   size_t o_ablk = ar.add(ablk), o_asub = ar.add(asub), o_apair = ar.add(apair),
          o_aterm = ar.add(aterm), o_eblk = ar.add(eblk_sorted), o_trun = ar.add(trun),
-         o_tblk = ar.add(tblk), o_elem = ar.add(elem_block);
+         o_tblk = ar.add(tblk), o_elem = ar.add(elem_block), o_t64 = ar.add(tiles64);
   std::vector<int> zeros(nblk_total + 1, 0);
   size_t o_kept = ar.add(zeros);
   std::vector<TruncResult> tres(nruns);
@@ -1011,11 +1097,35 @@ static void batch_add_site(nrg_run *const *runs, int nruns, const double *t, int
                         std::to_string(eig_max_n_f64()));
   MixedStatus mstat;
   if (e->precision == NRG_PREC_FP64) {
-    Prof pf(e, "k_eig_f64", eig_flops(eblk_sorted));
-    launch_eig_f64(at<EigBlock>(d, o_eblk), int(eblk_sorted.size()), max_n, e->eig_smem_f64,
-                   at<int>(d, o_stat), s);
-    count_launch(e);
-    post_launch("eigensolve");
+    const int ncl = int(eblk_sorted.size()) - n_f64;
+    if (ncl > 0) {
+      std::vector<EigBlock> clb(eblk_sorted.begin() + n_f64, eblk_sorted.end());
+      {
+        Prof pf(e, "k_eig_cluster_f64", eig_flops(clb) * 0.4);  // tridiagonal reduction: 4/3 n^3
+        const int cs = eig_cluster_size_for(max_cl64, true);
+        const std::string what = "eigensolve f64 (cluster of " + std::to_string(cs) + " CTAs, " +
+                                 std::to_string(ncl) + " blocks, largest " + std::to_string(max_cl64) + ")";
+        check_cuda(launch_eig_cluster(at<EigBlock>(d, o_eblk) + n_f64, ncl, max_cl64, cs, true, s), what.c_str());
+        count_launch(e);
+        post_launch("eigensolve f64 (cluster)");
+      }
+      double f = 0;  // applying the reflectors: 2 n^3 per block
+      for (auto &x : clb) f += 2.0 * double(x.n) * x.n * x.n;
+      Prof pf(e, "k_reflect_f64", f);
+      launch_reflect(at<EigBlock>(d, o_eblk) + n_f64, at<int2>(d, o_t64), int(tiles64.size()), max_cl64, tw64,
+                     panel64, s, true);
+      count_launch(e);
+      post_launch("reflect f64");
+    }
+    if (n_f64 > 0) {
+      int mx = 0;
+      for (int b = 0; b < n_f64; ++b) mx = std::max(mx, eblk_sorted[b].n);
+      std::vector<EigBlock> oneb(eblk_sorted.begin(), eblk_sorted.begin() + n_f64);
+      Prof pf(e, "k_eig_f64", eig_flops(oneb));
+      launch_eig_f64(at<EigBlock>(d, o_eblk), n_f64, mx, e->eig_smem_f64, at<int>(d, o_stat), s);
+      count_launch(e);
+      post_launch("eigensolve");
+    }
   } else {
     if (max_n > refine_max_n())
       fail(NRG_E_ARG, "block dimension " + std::to_string(max_n) + " exceeds the refinement limit");

@@ -635,12 +635,16 @@ int nrg_engine_create(const nrg_engine_opts *opts, nrg_engine **out) {
     }
     check_cuda(cudaSetDevice(e->device), "cudaSetDevice");
     check_cuda(cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking), "stream");
+    check_cuda(cudaStreamCreateWithFlags(&e->side, cudaStreamNonBlocking), "side stream");
+    check_cuda(cudaEventCreateWithFlags(&e->fork_ev, cudaEventDisableTiming), "event");
+    check_cuda(cudaEventCreateWithFlags(&e->join_ev, cudaEventDisableTiming), "event");
     for (auto &ev : e->ev) check_cuda(cudaEventCreate(&ev), "event");
     e->eig_smem_f64 = eig_smem_limit_f64();
     e->eig_smem_f32 = eig_smem_limit_f32();
     check_cuda(cudaMalloc(&e->d_kerr, sizeof(int)), "cudaMalloc (kernel error word)");
     check_cuda(cudaMemset(e->d_kerr, 0, sizeof(int)), "cudaMemset");
     if (const char *oz = std::getenv("NRG_OZAKI")) e->ozaki = std::atoi(oz) & 3;
+    if (const char *c = std::getenv("NRG_EIG_CLUSTER")) e->eig_cluster = std::atoi(c) != 0;
     *out = e;
   });
 }
@@ -653,6 +657,10 @@ int nrg_engine_destroy(nrg_engine *e) {
     for (auto ev : e->ring_events) cudaEventDestroy(ev);
     if (e->d_kerr) cudaFree(e->d_kerr);
     for (auto &ev : e->ev) cudaEventDestroy(ev);
+    cudaStreamSynchronize(e->side);
+    cudaEventDestroy(e->fork_ev);
+    cudaEventDestroy(e->join_ev);
+    cudaStreamDestroy(e->side);
     cudaStreamDestroy(e->stream);
     delete e;
   });

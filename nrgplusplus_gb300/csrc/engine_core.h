@@ -140,10 +140,17 @@ struct nrg_engine {
   uint64_t peak = 0;  // high-water mark of `used`
   int verbose = 0;
   cudaStream_t stream = nullptr;
+  // side stream: work of one phase that may overlap the main stream's
+  // (forked and joined with fork_ev / join_ev, both without timing)
+  cudaStream_t side = nullptr;
+  cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
   cudaEvent_t ev[8] = {};
   double phase_ms[5] = {0, 0, 0, 0, 0};
   uint64_t launches = 0;
   int eig_smem_f64 = 0, eig_smem_f32 = 0;
+  // blocks above the one-CTA shared-memory limit go to the cluster solver
+  // (NRG_EIG_CLUSTER=0 turns it off)
+  bool eig_cluster = true;
   int *d_kerr = nullptr;  // set by kernels whose bounded waits ran out (k_gemm_oz)
   // pinned ring for host -> device uploads (descriptor tables): a copy from
   // pageable memory may wait for the stream to drain, one from pinned memory
@@ -194,8 +201,9 @@ struct Prof {
   nrg_engine *e;
   const char *name;
   double work;
+  cudaStream_t s;
   cudaEvent_t a = nullptr;
-  Prof(nrg_engine *eng, const char *nm, double w = 0.0);
+  Prof(nrg_engine *eng, const char *nm, double w = 0.0, cudaStream_t st = nullptr);
   ~Prof();
 };
 }  // namespace nrg

@@ -703,62 +703,72 @@ k_eig_bi(const EigBlock *__restrict__ blocks, int max_n_smem, int smem_total) {
   for (int j = threadIdx.x; j < n; j += kThreads) B.E[j] = double(lam[j]);
 }
 
-// X = Q V for every block, Q = P_{n-1} ... P_1 from the reflectors k_eig_bi
-// left in W (row i: u_i in entries 0..i-1, h_i on the diagonal, 0 = none):
-// the reflectors are applied to X = V in the order P_1, P_2, ..., P_{n-1}.
-// One CTA owns TW columns of one block in shared memory (FP32) and each warp
-// TW / 8 of them, so a reflector needs no CTA barrier: a warp forms u^T x for
-// its columns with lane-strided sums and one shuffle reduction each, then
-// updates them.  Reflector rows are staged in panels of `panel` rows (one
-// barrier per panel).  The result is written in FP64 as the first
-// eigenvector estimate.
-template <int TW>
+// X = Q V for every block, Q = P_{n-1} ... P_1 from the reflectors the
+// first stage left in W (row i: u_i in entries 0..i-1, h_i on the diagonal,
+// 0 = none): the reflectors are applied to X = V in the order P_1, P_2, ...,
+// P_{n-1}.  One CTA owns TW columns of one block in shared memory and each
+// warp TW / 8 of them, so a reflector needs no CTA barrier: a warp forms
+// u^T x for its columns with lane-strided sums and one shuffle reduction
+// each, then updates them.  Reflector rows are staged in panels of `panel`
+// rows (one barrier per panel).  The result is written in FP64: the first
+// eigenvector estimate of the mixed path (T = float, W / V) or the
+// eigenvectors of the FP64 reflector solver (T = double, W64 / V64).
+template <typename T> __device__ __forceinline__ const T *refl_W(const EigBlock &b);
+template <> __device__ __forceinline__ const float *refl_W<float>(const EigBlock &b) { return b.W; }
+template <> __device__ __forceinline__ const double *refl_W<double>(const EigBlock &b) { return b.W64; }
+template <typename T> __device__ __forceinline__ const T *refl_V(const EigBlock &b);
+template <> __device__ __forceinline__ const float *refl_V<float>(const EigBlock &b) { return b.V; }
+template <> __device__ __forceinline__ const double *refl_V<double>(const EigBlock &b) { return b.V64; }
+
+template <typename T, int TW>
 __global__ void __launch_bounds__(256)
 k_reflect(const EigBlock *__restrict__ blocks, const int2 *__restrict__ tiles, int panel) {
   constexpr int CPW = TW / 8;  // columns per warp
   constexpr int XP = TW + 1;   // odd row pitch: lane-strided rows hit distinct banks
-  extern __shared__ __align__(16) float rsm[];
+  extern __shared__ __align__(16) unsigned char rsm_raw[];
+  T *rsm = reinterpret_cast<T *>(rsm_raw);
   const int2 t = tiles[blockIdx.x];
   const EigBlock B = blocks[t.x];
+  const T *Wm = refl_W<T>(B), *Vm = refl_V<T>(B);
   const int n = B.n, c0 = t.y * TW;
   const int nc = min(TW, n - c0);
-  float *X = rsm;                      // n x XP
-  float *Up = X + size_t(n) * XP;      // panel x n reflector rows
-  float *hs = Up + size_t(panel) * n;  // panel h values
+  T *X = rsm;                      // n x XP
+  T *Up = X + size_t(n) * XP;      // panel x n reflector rows
+  T *hs = Up + size_t(panel) * n;  // panel h values
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int cw = warp * CPW;
   for (int64_t idx = tid; idx < int64_t(n) * TW; idx += 256) {
     const int r = int(idx / TW), c = int(idx - int64_t(r) * TW);
-    X[int64_t(r) * XP + c] = (c < nc) ? B.V[int64_t(r) * B.ld + c0 + c] : 0.f;
+    X[int64_t(r) * XP + c] = (c < nc) ? Vm[int64_t(r) * B.ld + c0 + c] : T(0);
   }
   for (int p0 = 1; p0 < n; p0 += panel) {
     const int p1 = min(n, p0 + panel);
     __syncthreads();  // previous panel consumed (and X loaded)
     for (int q = p0 + warp; q < p1; q += 8) {
-      const float *src = B.W + int64_t(q) * B.ld;
-      float *dst = Up + size_t(q - p0) * n;
+      const T *src = Wm + int64_t(q) * B.ld;
+      T *dst = Up + size_t(q - p0) * n;
       for (int k = lane; k < q; k += 32) dst[k] = src[k];
       if (lane == 0) hs[q - p0] = src[q];
     }
     __syncthreads();
     for (int q = p0; q < p1; ++q) {
-      const float h = hs[q - p0];
-      if (h == 0.f) continue;
-      const float *uq = Up + size_t(q - p0) * n;
-      float w[CPW];
+      const T h = hs[q - p0];
+      if (h == T(0)) continue;
+      const T *uq = Up + size_t(q - p0) * n;
+      T w[CPW];
 #pragma unroll
-      for (int c = 0; c < CPW; ++c) w[c] = 0.f;
+      for (int c = 0; c < CPW; ++c) w[c] = T(0);
       for (int k = lane; k < q; k += 32) {
-        const float uk = uq[k];
+        const T uk = uq[k];
 #pragma unroll
-        for (int c = 0; c < CPW; ++c) w[c] = fmaf(uk, X[k * XP + cw + c], w[c]);
+        for (int c = 0; c < CPW; ++c) w[c] = fma(uk, X[k * XP + cw + c], w[c]);
       }
 #pragma unroll
       for (int c = 0; c < CPW; ++c) w[c] = warp_sum(w[c]) / h;
       for (int k = lane; k < q; k += 32) {
-        const float uk = uq[k];
+        const T uk = uq[k];
 #pragma unroll
-        for (int c = 0; c < CPW; ++c) X[k * XP + cw + c] = fmaf(-uk, w[c], X[k * XP + cw + c]);
+        for (int c = 0; c < CPW; ++c) X[k * XP + cw + c] = fma(-uk, w[c], X[k * XP + cw + c]);
       }
     }
   }
@@ -771,8 +781,8 @@ k_reflect(const EigBlock *__restrict__ blocks, const int2 *__restrict__ tiles, i
 
 constexpr size_t kReflectSmem = 225 * 1024;
 
-size_t reflect_bytes(int n, int tw, int panel) {
-  return sizeof(float) * (size_t(n) * (tw + 1) + size_t(panel) * (n + 1)) + 64;
+size_t reflect_bytes(int n, int tw, int panel, size_t elem = sizeof(float)) {
+  return elem * (size_t(n) * (tw + 1) + size_t(panel) * (n + 1)) + 64;
 }
 
 template <typename T> size_t smem_bytes(int n, bool in_smem) {
@@ -829,11 +839,12 @@ void launch_eig_bisect_f32(const EigBlock *blocks, int nblocks, int max_n, int m
   k_eig_bi<<<nblocks, kThreads, bytes, s>>>(blocks, max_n_smem, int(bytes));
 }
 
-bool reflect_config(int max_n, int *tw, int *panel) {
+bool reflect_config(int max_n, int *tw, int *panel, bool fp64) {
+  const size_t el = fp64 ? sizeof(double) : sizeof(float);
   for (int w = 64; w >= 8; w /= 2) {
-    if (reflect_bytes(max_n, w, 1) > kReflectSmem) continue;
+    if (reflect_bytes(max_n, w, 1, el) > kReflectSmem) continue;
     int pn = 32;
-    while (pn > 1 && reflect_bytes(max_n, w, pn) > kReflectSmem) --pn;
+    while (pn > 1 && reflect_bytes(max_n, w, pn, el) > kReflectSmem) --pn;
     *tw = w;
     *panel = pn;
     return true;
@@ -841,28 +852,36 @@ bool reflect_config(int max_n, int *tw, int *panel) {
   return false;
 }
 
-int reflect_max_n() {
+int reflect_max_n(bool fp64) {
+  const size_t el = fp64 ? sizeof(double) : sizeof(float);
   int n = 8;
-  while (reflect_bytes(n + 1, 8, 1) <= kReflectSmem) ++n;
+  while (reflect_bytes(n + 1, 8, 1, el) <= kReflectSmem) ++n;
   return n;
 }
 
-template <int TW> static void reflect_launch(const EigBlock *blocks, const int2 *tiles, int ntiles, int panel,
-                                             size_t bytes, cudaStream_t s) {
-  ensure_smem_limit(reinterpret_cast<const void *>(k_reflect<TW>), int(kReflectSmem));
-  k_reflect<TW><<<ntiles, 256, bytes, s>>>(blocks, tiles, panel);
+template <typename T, int TW> static void reflect_launch(const EigBlock *blocks, const int2 *tiles, int ntiles,
+                                                         int panel, size_t bytes, cudaStream_t s) {
+  ensure_smem_limit(reinterpret_cast<const void *>(k_reflect<T, TW>), int(kReflectSmem));
+  k_reflect<T, TW><<<ntiles, 256, bytes, s>>>(blocks, tiles, panel);
+}
+
+template <typename T>
+static void reflect_dispatch(const EigBlock *blocks, const int2 *tiles, int ntiles, int max_n, int tw, int panel,
+                             cudaStream_t s) {
+  const size_t bytes = reflect_bytes(max_n, tw, panel, sizeof(T));
+  switch (tw) {
+    case 64: reflect_launch<T, 64>(blocks, tiles, ntiles, panel, bytes, s); break;
+    case 32: reflect_launch<T, 32>(blocks, tiles, ntiles, panel, bytes, s); break;
+    case 16: reflect_launch<T, 16>(blocks, tiles, ntiles, panel, bytes, s); break;
+    default: reflect_launch<T, 8>(blocks, tiles, ntiles, panel, bytes, s); break;
+  }
 }
 
 void launch_reflect(const EigBlock *blocks, const int2 *tiles, int ntiles, int max_n, int tw, int panel,
-                    cudaStream_t s) {
+                    cudaStream_t s, bool fp64) {
   if (ntiles == 0) return;
-  const size_t bytes = reflect_bytes(max_n, tw, panel);
-  switch (tw) {
-    case 64: reflect_launch<64>(blocks, tiles, ntiles, panel, bytes, s); break;
-    case 32: reflect_launch<32>(blocks, tiles, ntiles, panel, bytes, s); break;
-    case 16: reflect_launch<16>(blocks, tiles, ntiles, panel, bytes, s); break;
-    default: reflect_launch<8>(blocks, tiles, ntiles, panel, bytes, s); break;
-  }
+  if (fp64) reflect_dispatch<double>(blocks, tiles, ntiles, max_n, tw, panel, s);
+  else reflect_dispatch<float>(blocks, tiles, ntiles, max_n, tw, panel, s);
 }
 void launch_eig_f32(const EigBlock *blocks, int nblocks, int max_n, int max_n_smem, int *status,
                     cudaStream_t s) {

@@ -13,6 +13,9 @@ namespace nrg {
 // (kernel, device) pair, thread-safe; throws the engine's error (NRG_E_CUDA)
 // when the runtime refuses.
 void ensure_smem_limit(const void *kernel, int bytes);
+// Allows `kernel` clusters above the portable 8 CTAs on the current device
+// (once per kernel and device); throws like ensure_smem_limit.
+void ensure_nonportable_cluster(const void *kernel);
 
 // ---------------------------------------------------------------- assembly
 // One device block = one non-empty (Q,Sz) sector of one run.
@@ -55,6 +58,7 @@ struct EigBlock {
   double *E;          // output eigenvalues, ascending
   float *W;           // FP32 workspace (n x ld): working matrix, then the reflectors
   float *V, *Bt;      // FP32 tridiagonal eigenvectors and LU pivots (n x ld)
+  double *W64, *V64, *Bt64;  // the same workspaces of the FP64 reflector solver
   int n, ld, ldu, pad;
 };
 // FP32 bisection + inverse-iteration solver (mixed path first stage): writes
@@ -66,10 +70,11 @@ struct EigBlock {
 // tiles: (block, column tile of width tw).
 void launch_eig_bisect_f32(const EigBlock *blocks, int nblocks, int max_n, int max_n_smem,
                            cudaStream_t s);
-bool reflect_config(int max_n, int *tw, int *panel);
-int reflect_max_n();
+// fp64: the FP64 reflector solver's buffers (W64, V64) and tiles.
+bool reflect_config(int max_n, int *tw, int *panel, bool fp64 = false);
+int reflect_max_n(bool fp64 = false);
 void launch_reflect(const EigBlock *blocks, const int2 *tiles, int ntiles, int max_n, int tw, int panel,
-                    cudaStream_t s);
+                    cudaStream_t s, bool fp64 = false);
 // FP64 Householder tridiagonalisation + implicit QL, one CTA per block.
 // status[b] != 0 if block b hit the QL iteration cap.
 // max_n: largest block of the launch; blocks with n <= max_n_smem are solved
@@ -80,6 +85,13 @@ void launch_eig_f64(const EigBlock *blocks, int nblocks, int max_n, int max_n_sm
 // Same algorithm in FP32 (mixed path first stage); writes U and E in FP64.
 void launch_eig_f32(const EigBlock *blocks, int nblocks, int max_n, int max_n_smem, int *status,
                     cudaStream_t s);
+// Thread-block-cluster solver (k_eig_cluster.cu) for blocks above the
+// one-CTA shared-memory limit: the cluster size (8 or 16 CTAs) whose
+// distributed shared memory holds an n-block, 0 when none does; launches one
+// cluster per block (the same outputs as k_eig_bi: E, reflectors in W, V).
+int eig_cluster_size_for(int n, bool fp64);
+cudaError_t launch_eig_cluster(const EigBlock *blocks, int nblocks, int max_n, int cs, bool fp64,
+                               cudaStream_t s);
 int eig_smem_limit_f64();
 int eig_smem_limit_f32();
 int eig_max_n_f64();

@@ -6,7 +6,7 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
-SIZES = [1, 2, 3, 17, 64, 150, 233, 240, 300, 420]
+SIZES = [1, 2, 3, 17, 64, 150, 233, 240, 300, 420, 706, 1000]
 
 
 def _blocks(seed=7):
@@ -25,6 +25,11 @@ def _blocks(seed=7):
     d = np.concatenate([d, d + np.logspace(-9, -5, 60)])
     q, _ = np.linalg.qr(rng.standard_normal((120, 120)))
     mats.append((q * d) @ q.T)
+    # a large block with a 2-fold degenerate spectrum and near-degenerate pairs
+    d = np.sort(rng.uniform(-4, 4, 160))
+    d = np.concatenate([d, d, d + np.logspace(-10, -4, 160)])
+    q, _ = np.linalg.qr(rng.standard_normal((480, 480)))
+    mats.append((q * d) @ q.T)
     return [0.5 * (m + m.T) for m in mats]
 
 
@@ -41,3 +46,29 @@ def test_eigh_batched(gpu_engine, mixed_engine, mode):
         assert np.all(np.diff(w) >= 0)
         assert np.abs(U.T @ U - np.eye(n)).max() <= 1e-12 * max(1, n) ** 0.5, (mode, n)
         assert np.abs(h @ U - U * w).max() <= 1e-11 * scale * max(1, n) ** 0.5, (mode, n)
+
+
+@pytest.mark.parametrize("sizes", [[240, 300, 420], [480, 640], [706]])
+def test_cluster_and_one_cta_solvers_agree(monkeypatch, sizes):
+    """The thread-block-cluster solver (blocks above one SM's shared memory;
+    8-CTA clusters below ~660 rows, 16 above) and the one-CTA solver give the
+    same refined eigenpairs, launch after launch of different sizes."""
+    from nrgplusplus_gb300 import api
+    rng = np.random.default_rng(len(sizes))
+    mats = []
+    for n in sizes:
+        a = rng.standard_normal((n, n))
+        mats.append((a + a.T) * 0.5)
+    out = {}
+    for flag in ("1", "0"):
+        monkeypatch.setenv("NRG_EIG_CLUSTER", flag)
+        eng = api.Engine(api.PREC_MIXED)
+        eng.eigh_batched(mats)        # the largest launch first,
+        eng.eigh_batched(mats[:1])    # a smaller one,
+        out[flag] = eng.eigh_batched(mats)  # and the largest again
+        eng.close()
+    for h, (w1, U1), (w0, U0) in zip(mats, out["1"], out["0"]):
+        n = h.shape[0]
+        scale = max(1.0, np.abs(h).max())
+        assert np.abs(w1 - w0).max() <= 1e-12 * scale * n ** 0.5
+        assert np.abs(h @ U1 - U1 * w1).max() <= 1e-11 * scale * n ** 0.5

@@ -127,6 +127,17 @@ int nrg_engine_kernel_times(nrg_engine *eng, char *names, uint64_t names_cap, do
  * tensor-core GEMM work (2MNK per product), out[3] the bf16 tensor-pipe
  * flops it took (2MNK per digit-plane product); n = entries written. */
 int nrg_engine_work_counters(nrg_engine *eng, double *out, int cap, int *n, int reset);
+/* Launch-shape autotuner (no counterpart in the reference; on by default):
+ * per block-size histogram of a launch (largest block, block count, total
+ * size), the reflector back-transform's column-tile width and panel are
+ * picked by timing every fitting candidate once, on the first launch that
+ * shows the histogram (one stream synchronisation), and reused.  All
+ * candidates compute every column in the same order, so results are the
+ * same bit for bit whichever is picked.  on = 0: the widest tile that fits. */
+int nrg_engine_set_autotune(nrg_engine *eng, int on);
+/* The decisions so far, one line per histogram with the candidates' times;
+ * len = bytes of the report (written up to cap, NUL-terminated). */
+int nrg_engine_autotune_report(nrg_engine *eng, char *buf, uint64_t cap, uint64_t *len);
 int nrg_engine_sync(nrg_engine *eng);
 
 /* ---- one NRG run (nrgcore<Imp,Bath>) ---------------------------------- */

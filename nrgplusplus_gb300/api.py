@@ -60,6 +60,7 @@ EXPORTS = [
     "nrg_last_error", "nrg_engine_create", "nrg_engine_destroy", "nrg_engine_phase_times",
     "nrg_engine_launch_count", "nrg_engine_get_opts", "nrg_engine_fallback_count", "nrg_engine_memory",
     "nrg_engine_set_profiling", "nrg_engine_kernel_times", "nrg_engine_work_counters",
+    "nrg_engine_set_autotune", "nrg_engine_autotune_report",
     "nrg_engine_sync", "nrg_run_create", "nrg_run_destroy",
     "nrg_run_set_parameters", "nrg_run_set_bath", "nrg_run_add_site", "nrg_run_update_state",
     "nrg_run_check_discarded", "nrg_run_get_info", "nrg_run_get_all_eigenvalues",
@@ -187,6 +188,18 @@ class Engine:
         v = C.c_uint64()
         _call(lib().nrg_engine_fallback_count, self.h, C.byref(v))
         return v.value
+
+    def set_autotune(self, on=True):
+        """Launch-shape autotuner on / off (nrg_engine_set_autotune)."""
+        _call(lib().nrg_engine_set_autotune, self.h, 1 if on else 0)
+
+    def autotune_report(self):
+        """The autotuner's decisions: one line per block-size histogram."""
+        n = C.c_uint64()
+        _call(lib().nrg_engine_autotune_report, self.h, None, C.c_uint64(0), C.byref(n))
+        buf = C.create_string_buffer(n.value + 1)
+        _call(lib().nrg_engine_autotune_report, self.h, buf, C.c_uint64(n.value + 1), C.byref(n))
+        return [x for x in buf.value.decode().split("\n") if x]
 
     def work_counters(self, reset=False):
         """Algorithmic work since the last reset: {'F_eig', 'F_rot',

@@ -12,6 +12,8 @@
 // Empty sectors (no kept states) stay in the API-level sector lists exactly as
 // the reference keeps them, but never reach the device.
 #include <algorithm>
+#include <cstdio>
+#include <functional>
 #include <map>
 #include <mutex>
 #include <set>
@@ -615,6 +617,104 @@ OzContrib ozc(const OzOperand &A, const OzOperand &B, int K, int trans, double a
   return c;
 }
 
+// ------------------------------------------------------------ autotuner
+// The block-size histogram of one launch, coarsened into a key: the largest
+// block in steps of 32 rows, the block count and the total n^2 in powers of
+// two, and the precision of the kernel.
+static uint64_t hist_key(const std::vector<EigBlock> &b, bool fp64) {
+  int mx = 0;
+  double n2 = 0;
+  for (auto &x : b) {
+    mx = std::max(mx, x.n);
+    n2 += double(x.n) * x.n;
+  }
+  const uint64_t cnt = uint64_t(std::ilogb(double(b.size()) + 1.0));
+  const uint64_t vol = uint64_t(std::ilogb(n2 + 1.0));
+  return (uint64_t((mx + 31) / 32) << 24) | (cnt << 16) | (vol << 8) | (fp64 ? 1u : 0u);
+}
+
+struct ReflectPlan {
+  int tw, panel;
+};
+
+// The reflector back-transform's launch shapes for one launch: the tuned one
+// when the histogram has been seen, every fitting tile width (largest panel
+// each) when it is to be tuned now, else the widest that fits.
+static std::vector<ReflectPlan> reflect_plans(nrg_engine *e, uint64_t key, int max_n, bool fp64) {
+  std::vector<ReflectPlan> out;
+  auto it = e->tuned.find(key);
+  if (e->autotune && it != e->tuned.end()) {
+    // the key coarsens max_n: the tuned width, with the panel that fits this
+    // launch's largest block
+    int pn = 1;
+    if (reflect_fits(max_n, it->second.tw, &pn, fp64)) return {{it->second.tw, std::min(pn, it->second.panel)}};
+  }
+  for (int tw : {64, 32, 16, 8}) {
+    int pn = 1;
+    if (!reflect_fits(max_n, tw, &pn, fp64)) continue;
+    out.push_back({tw, pn});
+    if (!e->autotune) break;
+  }
+  if (out.empty())
+    fail(NRG_E_ARG, "block dimension " + std::to_string(max_n) + " exceeds the back-transform limit " +
+                        std::to_string(reflect_max_n(fp64)));
+  return out;
+}
+
+// Column tiles (block, tile) of every plan.
+static std::vector<std::vector<int2>> reflect_tiles(const std::vector<EigBlock> &b,
+                                                    const std::vector<ReflectPlan> &plans) {
+  std::vector<std::vector<int2>> t(plans.size());
+  for (size_t p = 0; p < plans.size(); ++p)
+    for (size_t k = 0; k < b.size(); ++k)
+      for (int tn = 0; tn < (b[k].n + plans[p].tw - 1) / plans[p].tw; ++tn) t[p].push_back(make_int2(int(k), tn));
+  return t;
+}
+
+// Runs the back-transform: one plan as is; several (a histogram seen for the
+// first time) each timed with CUDA events after a stream synchronisation,
+// the fastest kept for the histogram.  Every plan writes the same U, bit for
+// bit (a column's arithmetic does not depend on the tile width or panel).
+static void run_reflect(nrg_engine *e, uint64_t key, const std::vector<ReflectPlan> &plans, const char *name,
+                        double flops, const std::function<void(size_t)> &launch) {
+  if (plans.size() == 1) {
+    Prof pf(e, name, flops);
+    launch(0);
+    count_launch(e);
+    post_launch(name);
+    return;
+  }
+  check_cuda(cudaStreamSynchronize(e->stream), "autotune");
+  std::vector<float> ms(plans.size(), 0.f);
+  for (size_t p = 0; p < plans.size(); ++p) {
+    cudaEvent_t a = take_event(e), b = take_event(e);
+    check_cuda(cudaEventRecord(a, e->stream), "autotune");
+    launch(p);
+    count_launch(e);
+    post_launch(name);
+    check_cuda(cudaEventRecord(b, e->stream), "autotune");
+    check_cuda(cudaEventSynchronize(b), "autotune");
+    check_cuda(cudaEventElapsedTime(&ms[p], a, b), "autotune");
+    e->ev_pool.push_back(a);
+    e->ev_pool.push_back(b);
+  }
+  size_t best = 0;
+  for (size_t p = 1; p < plans.size(); ++p)
+    if (ms[p] < ms[best]) best = p;
+  nrg_engine::Tuned t;
+  t.tw = plans[best].tw;
+  t.panel = plans[best].panel;
+  char buf[64];
+  t.what = std::string(name) + " histogram " + std::to_string(key) + ": tw=" + std::to_string(t.tw) +
+           " panel=" + std::to_string(t.panel) + " (";
+  for (size_t p = 0; p < plans.size(); ++p) {
+    std::snprintf(buf, sizeof(buf), "%s%d:%.3f ms", p ? ", " : "", plans[p].tw, double(ms[p]));
+    t.what += buf;
+  }
+  t.what += ")";
+  e->tuned[key] = t;
+}
+
 constexpr int kRefineSteps = 3;
 constexpr double kClusterTau = 1e-4;  // relative gap below which levels form a cluster
 // The first Newton step starts from FP32 eigenvectors (errors >= 1e-7), so
@@ -660,11 +760,6 @@ static MixedStatus mixed_eigensolve(nrg_engine *e, std::vector<DevBlock *> &blks
   float *wbase = static_cast<float *>(mw->ptr);
   // FP32 solve: eigenvectors (as FP64) into X0
   std::vector<EigBlock> eb(nb);
-  std::vector<int2> bt_tiles;
-  int tw = 64, panel = 1;
-  if (!reflect_config(max_n, &tw, &panel))
-    fail(NRG_E_ARG, "block dimension " + std::to_string(max_n) + " exceeds the mixed-precision limit " +
-                        std::to_string(reflect_max_n()));
   for (size_t b = 0; b < nb; ++b) {
     eb[b] = EigBlock{};
     eb[b].H = blks[b]->H;
@@ -676,8 +771,10 @@ static MixedStatus mixed_eigensolve(nrg_engine *e, std::vector<DevBlock *> &blks
     eb[b].n = blks[b]->n;
     eb[b].ld = blks[b]->ld;
     eb[b].ldu = blks[b]->ld;
-    for (int tn = 0; tn < (blks[b]->n + tw - 1) / tw; ++tn) bt_tiles.push_back(make_int2(int(b), tn));
   }
+  const uint64_t rkey = hist_key(eb, false);
+  const std::vector<ReflectPlan> rplans = reflect_plans(e, rkey, max_n, false);
+  const std::vector<std::vector<int2>> rtiles = reflect_tiles(eb, rplans);
   std::vector<int> stat(nb + 1, 0);
   std::vector<RefineBlock> rb(nb);
   std::vector<EigBlock> eb64(nb);  // FP64 re-solve of flagged blocks, in place
@@ -704,7 +801,9 @@ static MixedStatus mixed_eigensolve(nrg_engine *e, std::vector<DevBlock *> &blks
     }
   }
   Arena a;
-  size_t oeb = a.add(eb), ost = a.add(stat), obt = a.add(bt_tiles), oeb64 = a.add(eb64), ost64 = a.add(stat);
+  size_t oeb = a.add(eb), ost = a.add(stat), oeb64 = a.add(eb64), ost64 = a.add(stat);
+  std::vector<size_t> obt(rplans.size());
+  for (size_t p = 0; p < rplans.size(); ++p) obt[p] = a.add(rtiles[p]);
   const size_t orb = a.add(rb);  // filled per step below (host copy re-uploaded)
   const size_t oone = a.add(eb_one), ocl = a.add(eb_cl);
   DevPtr dd;
@@ -739,10 +838,10 @@ static MixedStatus mixed_eigensolve(nrg_engine *e, std::vector<DevBlock *> &blks
   {
     double f = 0;  // applying the reflectors: 2 n^3 per block
     for (auto &x : eb) f += 2.0 * double(x.n) * x.n * x.n;
-    Prof pf(e, "k_reflect", f);
-    launch_reflect(at<EigBlock>(dp, oeb), at<int2>(dp, obt), int(bt_tiles.size()), max_n, tw, panel, s);
-    count_launch(e);
-    post_launch("reflect");
+    run_reflect(e, rkey, rplans, "k_reflect", f, [&](size_t p) {
+      launch_reflect(at<EigBlock>(dp, oeb), at<int2>(dp, obt[p]), int(rtiles[p].size()), max_n, rplans[p].tw,
+                     rplans[p].panel, s);
+    });
   }
   int cur = 0;
   // digit planes for the tensor-core GEMMs (H once, X / Y / E per step)
@@ -1036,7 +1135,9 @@ static void batch_add_site(nrg_run *const *runs, int nruns, const double *t, int
   // k_reflect<double>, the mixed path's first stage in FP64) and moved to the
   // end of the list; the others by k_eig<double> (tred2 + QL)
   int n_f64 = int(eblk_sorted.size()), max_cl64 = 0, tw64 = 8, panel64 = 1;
-  std::vector<int2> tiles64;
+  uint64_t key64 = 0;
+  std::vector<ReflectPlan> plans64;
+  std::vector<std::vector<int2>> tiles64;
   if (e->precision == NRG_PREC_FP64 && e->eig_cluster) {
     std::vector<EigBlock> one, cl;
     int64_t wsz = 0;
@@ -1050,7 +1151,9 @@ static void batch_add_site(nrg_run *const *runs, int nruns, const double *t, int
       }
     }
     if (!cl.empty()) {
-      reflect_config(max_cl64, &tw64, &panel64, true);
+      key64 = hist_key(cl, true);
+      plans64 = reflect_plans(e, key64, max_cl64, true);
+      tiles64 = reflect_tiles(cl, plans64);
       DevPtr w = dalloc(e, 3 * wsz * sizeof(double) + 16);
       hold.push_back(w);
       double *base = static_cast<double *>(w->ptr);
@@ -1061,7 +1164,6 @@ static void batch_add_site(nrg_run *const *runs, int nruns, const double *t, int
         b.V64 = base + wsz + o;
         b.Bt64 = base + 2 * wsz + o;
         o += int64_t(b.n) * b.ld;
-        for (int tn = 0; tn < (b.n + tw64 - 1) / tw64; ++tn) tiles64.push_back(make_int2(int(k), tn));
       }
       n_f64 = int(one.size());
       eblk_sorted = one;
@@ -1072,7 +1174,9 @@ static void batch_add_site(nrg_run *const *runs, int nruns, const double *t, int
   Arena ar;
   size_t o_ablk = ar.add(ablk), o_asub = ar.add(asub), o_apair = ar.add(apair),
          o_aterm = ar.add(aterm), o_eblk = ar.add(eblk_sorted), o_trun = ar.add(trun),
-         o_tblk = ar.add(tblk), o_elem = ar.add(elem_block), o_t64 = ar.add(tiles64);
+         o_tblk = ar.add(tblk), o_elem = ar.add(elem_block);
+  std::vector<size_t> o_t64(tiles64.size());
+  for (size_t p = 0; p < tiles64.size(); ++p) o_t64[p] = ar.add(tiles64[p]);
   std::vector<int> zeros(nblk_total + 1, 0);
   size_t o_kept = ar.add(zeros);
   std::vector<TruncResult> tres(nruns);
@@ -1111,11 +1215,10 @@ static void batch_add_site(nrg_run *const *runs, int nruns, const double *t, int
       }
       double f = 0;  // applying the reflectors: 2 n^3 per block
       for (auto &x : clb) f += 2.0 * double(x.n) * x.n * x.n;
-      Prof pf(e, "k_reflect_f64", f);
-      launch_reflect(at<EigBlock>(d, o_eblk) + n_f64, at<int2>(d, o_t64), int(tiles64.size()), max_cl64, tw64,
-                     panel64, s, true);
-      count_launch(e);
-      post_launch("reflect f64");
+      run_reflect(e, key64, plans64, "k_reflect_f64", f, [&](size_t p) {
+        launch_reflect(at<EigBlock>(d, o_eblk) + n_f64, at<int2>(d, o_t64[p]), int(tiles64[p].size()), max_cl64,
+                       plans64[p].tw, plans64[p].panel, s, true);
+      });
     }
     if (n_f64 > 0) {
       int mx = 0;

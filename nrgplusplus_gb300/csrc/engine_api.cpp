@@ -645,6 +645,7 @@ int nrg_engine_create(const nrg_engine_opts *opts, nrg_engine **out) {
     check_cuda(cudaMemset(e->d_kerr, 0, sizeof(int)), "cudaMemset");
     if (const char *oz = std::getenv("NRG_OZAKI")) e->ozaki = std::atoi(oz) & 3;
     if (const char *c = std::getenv("NRG_EIG_CLUSTER")) e->eig_cluster = std::atoi(c) != 0;
+    if (const char *c = std::getenv("NRG_AUTOTUNE")) e->autotune = std::atoi(c) != 0;
     *out = e;
   });
 }
@@ -766,6 +767,27 @@ int nrg_engine_work_counters(nrg_engine *e, double *out, int cap, int *n, int re
     *n = k;
     if (reset)
       for (double &w : e->work) w = 0.0;
+  });
+}
+
+int nrg_engine_set_autotune(nrg_engine *e, int on) {
+  return guard([&] {
+    if (!e) fail(NRG_E_ARG, "null engine");
+    e->autotune = on != 0;
+  });
+}
+
+int nrg_engine_autotune_report(nrg_engine *e, char *buf, uint64_t cap, uint64_t *len) {
+  return guard([&] {
+    if (!e || !len) fail(NRG_E_ARG, "null argument");
+    std::string r;
+    for (auto &kv : e->tuned) r += kv.second.what + "\n";
+    *len = r.size();
+    if (buf && cap) {
+      const size_t k = std::min<size_t>(r.size(), size_t(cap - 1));
+      std::memcpy(buf, r.data(), k);
+      buf[k] = 0;
+    }
   });
 }
 

@@ -151,6 +151,16 @@ struct nrg_engine {
   // blocks above the one-CTA shared-memory limit go to the cluster solver
   // (NRG_EIG_CLUSTER=0 turns it off)
   bool eig_cluster = true;
+  // launch-shape autotuner (nrg_engine_set_autotune): per block-size
+  // histogram, the reflector back-transform's column-tile width and panel,
+  // picked by timing every candidate on the first launch that shows the
+  // histogram (all candidates give bit-identical results)
+  bool autotune = true;
+  struct Tuned {
+    int tw = 0, panel = 0;
+    std::string what;
+  };
+  std::map<uint64_t, Tuned> tuned;
   int *d_kerr = nullptr;  // set by kernels whose bounded waits ran out (k_gemm_oz)
   // pinned ring for host -> device uploads (descriptor tables): a copy from
   // pageable memory may wait for the stream to drain, one from pinned memory

@@ -852,6 +852,15 @@ bool reflect_config(int max_n, int *tw, int *panel, bool fp64) {
   return false;
 }
 
+bool reflect_fits(int max_n, int tw, int *panel, bool fp64) {
+  const size_t el = fp64 ? sizeof(double) : sizeof(float);
+  if (reflect_bytes(max_n, tw, 1, el) > kReflectSmem) return false;
+  int pn = 32;
+  while (pn > 1 && reflect_bytes(max_n, tw, pn, el) > kReflectSmem) --pn;
+  *panel = pn;
+  return true;
+}
+
 int reflect_max_n(bool fp64) {
   const size_t el = fp64 ? sizeof(double) : sizeof(float);
   int n = 8;

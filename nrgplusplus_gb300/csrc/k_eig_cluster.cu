@@ -10,9 +10,9 @@
 //   Householder step i (n-1 down to 1), reflector u from row i:
 //     the owner of row i forms u, h and e_i              | cluster barrier
 //     every CTA copies u from the owner (DSMEM loads),
-//     p_j = (A u)_j / h for its rows, partial u.p to all  | cluster barrier
-//     q_j = p_j - (u.p / 2h) u_j for its rows to all CTAs | cluster barrier
-//     rank-2 update A -= u q^T + q u^T of its rows
+//     p_j = (A u)_j / h for its rows; p_j and the partial
+//     u.p to all CTAs                                     | cluster barrier
+//     q = p - (u.p / 2h) u locally, rank-2 update A -= u q^T + q u^T of its rows
 //   T's diagonal and off-diagonal gathered into every CTA; eigenvalue j is
 //   bisected and inverse-iterated by CTA j % CS; eigenvalues gathered again;
 //   near-degenerate clusters re-orthogonalised by the CTA owning their first
@@ -25,6 +25,8 @@
 // flow depends only on n and on values all CTAs read from the same place),
 // and no CTA leaves while others may still read its shared memory.
 #include <cooperative_groups.h>
+
+#include <algorithm>
 
 #include "nrg_internal.h"
 
@@ -176,7 +178,8 @@ __host__ __device__ inline int pitch_of(int n) { return (n + 3) & ~3; }
 template <typename T> __host__ __device__ inline size_t cluster_smem(int n, int cs) {
   const size_t nr = size_t(rows_of(n, cs, 0));
   size_t b = 64 + sizeof(T) * (kWarpsC + 1 + 16 + cs);  // ctl, red, part
-  b += sizeof(T) * (nr * size_t(pitch_of(n)));          // the CTA's rows
+  // the CTA's rows; afterwards the staging of the cluster solves (2n per warp)
+  b += sizeof(T) * std::max(nr * size_t(pitch_of(n)), size_t(2 * kWarpsC) * size_t(n));
   b += sizeof(T) * (5 * size_t(n) + 16);                 // u, q, d, e, lam
   b += sizeof(T) * (3 * nr + 8);                         // p, h, e of the own rows
   return b + 256;                                        // 16-byte alignment of 12 arrays
@@ -212,7 +215,7 @@ k_eig_cluster(const EigBlock *__restrict__ blocks) {
   T *ploc = reinterpret_cast<T *>(take(sizeof(T) * (nr0 + 1)));
   T *hloc = reinterpret_cast<T *>(take(sizeof(T) * (nr0 + 1)));
   T *eloc = reinterpret_cast<T *>(take(sizeof(T) * (nr0 + 1)));
-  T *A = reinterpret_cast<T *>(take(sizeof(T) * size_t(nr0) * P));
+  T *A = reinterpret_cast<T *>(take(sizeof(T) * max(size_t(nr0) * P, size_t(2 * kWarpsC) * size_t(n))));
   T *W = Bufs<T>::W(B), *V = Bufs<T>::V(B), *Bt = Bufs<T>::Bt(B);
   // load the CTA's rows (row g = rank + r * CS)
   for (int64_t idx = tid; idx < int64_t(nr) * n; idx += kThreadsC) {
@@ -276,22 +279,22 @@ k_eig_cluster(const EigBlock *__restrict__ blocks) {
       if (lane == 0) ploc[r] = s / h;
     }
     __syncthreads();
+    // p of the own rows and the partial u.p go to every CTA (p gathered into
+    // q): one barrier for both, q = p - (u.p / 2h) u is formed locally
     T fs = T(0);
     for (int r = tid; r < nact; r += kThreadsC) fs += ploc[r] * u[rank + r * CS];
     fs = block_sum_c(fs, red);
-    if (tid < CS) *cluster.map_shared_rank(part + rank, tid) = fs;  // partial u.p to every CTA
+    if (tid < CS) *cluster.map_shared_rank(part + rank, tid) = fs;
+    for (int idx = tid; idx < nact * CS; idx += kThreadsC) {
+      const int r = idx / CS, c = idx - r * CS;
+      *cluster.map_shared_rank(q + rank + r * CS, c) = ploc[r];
+    }
     cluster.sync();
     T f = T(0);
     for (int c = 0; c < CS; ++c) f += part[c];  // same order in every CTA
     const T hh = f / (h + h);
-    // q_j for the own rows, gathered into every CTA's q
-    for (int idx = tid; idx < nact * CS; idx += kThreadsC) {
-      const int r = idx / CS, c = idx - r * CS;
-      const int j = rank + r * CS;
-      const T qv = ploc[r] - hh * u[j];
-      *cluster.map_shared_rank(q + j, c) = qv;
-    }
-    cluster.sync();
+    for (int k = tid; k <= l; k += kThreadsC) q[k] -= hh * u[k];  // q = p - hh u
+    __syncthreads();
     // rank-2 update of the own rows, columns 0..l
     for (int r = warp; r < nact; r += kWarpsC) {
       T *rowj = A + int64_t(r) * P;
@@ -375,28 +378,35 @@ k_eig_cluster(const EigBlock *__restrict__ blocks) {
   }
   __syncthreads();
   const int ncl = ctl->ncl;
+  // each warp iterates its members in the (now free) matrix area of its own
+  // shared memory: the member x and its LU pivots, 2n entries per warp, so
+  // the sequential solves run at shared-memory latency
+  T *stage = A + size_t(warp) * 2 * n;
   for (int cq = warp; cq < ncl; cq += kWarpsC) {
     const int c0 = cl[2 * cq], c1 = cl[2 * cq + 1];
     for (int j = c0; j < c1; ++j) {
-      T *xv = V + j;
-      T *bv = Bt + j;
+      T *xv = stage, *bv = stage + n;
+      for (int i = lane; i < n; i += 32) xv[i] = V[int64_t(i) * B.ld + j];
+      __syncwarp();
       for (int rep = 0; rep < 2; ++rep) {
-        if (lane == 0) inv_solve_c(dv, ev, n, lam[j], pivmin, T(1), xv, bv, B.ld, 0);
+        if (lane == 0) inv_solve_c(dv, ev, n, lam[j], pivmin, T(1), xv, bv, 1, 0);
         __syncwarp();
-        for (int k = c0; k < j; ++k) {
+        for (int k = c0; k < j; ++k) {  // earlier members are final in V
           T dot = T(0);
-          for (int i = lane; i < n; i += 32) dot += V[int64_t(i) * B.ld + k] * xv[int64_t(i) * B.ld];
+          for (int i = lane; i < n; i += 32) dot += V[int64_t(i) * B.ld + k] * xv[i];
           dot = warp_sum_c(dot);
-          for (int i = lane; i < n; i += 32) xv[int64_t(i) * B.ld] -= dot * V[int64_t(i) * B.ld + k];
+          for (int i = lane; i < n; i += 32) xv[i] -= dot * V[int64_t(i) * B.ld + k];
           __syncwarp();
         }
         T nrm = T(0);
-        for (int i = lane; i < n; i += 32) nrm += xv[int64_t(i) * B.ld] * xv[int64_t(i) * B.ld];
+        for (int i = lane; i < n; i += 32) nrm += xv[i] * xv[i];
         nrm = warp_sum_c(nrm);
         const T scn = T(1) / sqrt_c(max(nrm, Tiny<T>::small));
-        for (int i = lane; i < n; i += 32) xv[int64_t(i) * B.ld] *= scn;
+        for (int i = lane; i < n; i += 32) xv[i] *= scn;
         __syncwarp();
       }
+      for (int i = lane; i < n; i += 32) V[int64_t(i) * B.ld + j] = xv[i];
+      __syncwarp();
     }
   }
   for (int k = tid; k < nown; k += kThreadsC) {

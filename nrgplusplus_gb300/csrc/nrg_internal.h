@@ -73,6 +73,9 @@ void launch_eig_bisect_f32(const EigBlock *blocks, int nblocks, int max_n, int m
 // fp64: the FP64 reflector solver's buffers (W64, V64) and tiles.
 bool reflect_config(int max_n, int *tw, int *panel, bool fp64 = false);
 int reflect_max_n(bool fp64 = false);
+// whether column tiles of width tw fit for blocks up to max_n (and the
+// largest reflector panel that does)
+bool reflect_fits(int max_n, int tw, int *panel, bool fp64 = false);
 void launch_reflect(const EigBlock *blocks, const int2 *tiles, int ntiles, int max_n, int tw, int panel,
                     cudaStream_t s, bool fp64 = false);
 // FP64 Householder tridiagonalisation + implicit QL, one CTA per block.

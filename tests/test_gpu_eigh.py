@@ -72,3 +72,24 @@ def test_cluster_and_one_cta_solvers_agree(monkeypatch, sizes):
         scale = max(1.0, np.abs(h).max())
         assert np.abs(w1 - w0).max() <= 1e-12 * scale * n ** 0.5
         assert np.abs(h @ U1 - U1 * w1).max() <= 1e-11 * scale * n ** 0.5
+
+
+def test_autotuned_back_transform_is_bit_identical():
+    """The autotuner times every reflector tile width on the first launch of
+    a block-size histogram; whichever it keeps, the eigenpairs are the same
+    bit for bit as with the autotuner off."""
+    from nrgplusplus_gb300 import api
+    mats = _blocks(5)[6:12]
+    out = {}
+    for on in (True, False):
+        eng = api.Engine(api.PREC_MIXED)
+        eng.set_autotune(on)
+        out[on] = [eng.eigh_batched(mats), eng.eigh_batched(mats)]
+        rep = eng.autotune_report()
+        eng.close()
+        if on:
+            assert rep and "tw=" in rep[0]
+        else:
+            assert rep == []
+    for a, b in zip(out[True][0] + out[True][1], out[False][0] + out[False][1]):
+        assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])

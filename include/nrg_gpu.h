@@ -135,6 +135,10 @@ int nrg_engine_work_counters(nrg_engine *eng, double *out, int cap, int *n, int 
  * candidates compute every column in the same order, so results are the
  * same bit for bit whichever is picked.  on = 0: the widest tile that fits. */
 int nrg_engine_set_autotune(nrg_engine *eng, int on);
+/* Blocks above one SM's shared memory: 0 = the one-CTA eigensolver only,
+ * 1 = the thread-block-cluster eigensolver when every cluster of the launch
+ * fits one wave of the device (default; env NRG_EIG_CLUSTER), 2 = always. */
+int nrg_engine_set_eig_cluster(nrg_engine *eng, int mode);
 /* The decisions so far, one line per histogram with the candidates' times;
  * len = bytes of the report (written up to cap, NUL-terminated). */
 int nrg_engine_autotune_report(nrg_engine *eng, char *buf, uint64_t cap, uint64_t *len);

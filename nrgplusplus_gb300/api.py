@@ -60,7 +60,7 @@ EXPORTS = [
     "nrg_last_error", "nrg_engine_create", "nrg_engine_destroy", "nrg_engine_phase_times",
     "nrg_engine_launch_count", "nrg_engine_get_opts", "nrg_engine_fallback_count", "nrg_engine_memory",
     "nrg_engine_set_profiling", "nrg_engine_kernel_times", "nrg_engine_work_counters",
-    "nrg_engine_set_autotune", "nrg_engine_autotune_report",
+    "nrg_engine_set_autotune", "nrg_engine_autotune_report", "nrg_engine_set_eig_cluster",
     "nrg_engine_sync", "nrg_run_create", "nrg_run_destroy",
     "nrg_run_set_parameters", "nrg_run_set_bath", "nrg_run_add_site", "nrg_run_update_state",
     "nrg_run_check_discarded", "nrg_run_get_info", "nrg_run_get_all_eigenvalues",
@@ -192,6 +192,12 @@ class Engine:
     def set_autotune(self, on=True):
         """Launch-shape autotuner on / off (nrg_engine_set_autotune)."""
         _call(lib().nrg_engine_set_autotune, self.h, 1 if on else 0)
+
+    def set_eig_cluster(self, mode):
+        """Cluster eigensolver for blocks above one SM's shared memory:
+        0 off, 1 when the launch's clusters fit one wave (default), 2 always
+        (nrg_engine_set_eig_cluster)."""
+        _call(lib().nrg_engine_set_eig_cluster, self.h, int(mode))
 
     def autotune_report(self):
         """The autotuner's decisions: one line per block-size histogram."""

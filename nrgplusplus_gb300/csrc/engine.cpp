@@ -621,6 +621,19 @@ OzContrib ozc(const OzOperand &A, const OzOperand &B, int K, int trans, double a
 // The block-size histogram of one launch, coarsened into a key: the largest
 // block in steps of 32 rows, the block count and the total n^2 in powers of
 // two, and the precision of the kernel.
+// Cluster solver or one-CTA solver for the blocks above one SM's shared
+// memory. The cluster solver finishes a block several times sooner but spends
+// about six times the SM-time of the one-CTA solver on it, so in the automatic
+// mode it takes a launch only when all its clusters run in one wave of the
+// device: the launch is then latency-bound and the idle SMs are free.
+static bool cluster_wanted(const nrg_engine *e, const std::vector<int> &eligible, bool fp64) {
+  if (eligible.empty() || e->eig_cluster == 0) return false;
+  if (e->eig_cluster == 2) return true;
+  int ctas = 0;
+  for (int n : eligible) ctas += eig_cluster_size_for(n, fp64);
+  return ctas <= e->sm_count;
+}
+
 static uint64_t hist_key(const std::vector<EigBlock> &b, bool fp64) {
   int mx = 0;
   double n2 = 0;
@@ -738,6 +751,123 @@ struct MixedStatus {
   int nb = 0;
 };
 
+struct F64Solve {
+  std::vector<EigBlock> order;  // the blocks in launch order (status index)
+  int *d_status = nullptr;      // per block: 1 = tred2 + QL did not converge
+};
+
+// Plain FP64 eigensolve of a list of blocks (largest first).  Blocks above
+// the one-CTA shared-memory limit (up to the reflector kernel's) go to the
+// reflector solver, the mixed path's first stage in FP64 (Householder
+// reduction, bisection, inverse iteration, then k_reflect<double>): the
+// cluster solver when its clusters fit one wave, else one CTA per block
+// streaming the matrix (k_eig_bi<double>).  They are moved to the end of the
+// list; the others go to k_eig<double> (tred2 + QL) in shared memory, on the
+// side stream.  The caller reads the status at its next synchronisation.
+static F64Solve fp64_eigensolve(nrg_engine *e, std::vector<EigBlock> eb, std::vector<DevPtr> &hold,
+                                cudaStream_t s) {
+  int n_f64 = int(eb.size()), max_r64 = 0, tw64 = 8, panel64 = 1;
+  bool cluster64 = false;
+  uint64_t key64 = 0;
+  std::vector<ReflectPlan> plans64;
+  std::vector<std::vector<int2>> tiles64;
+  {
+    std::vector<EigBlock> one, rs;
+    std::vector<int> eligible64;
+    int64_t wsz = 0;
+    for (auto &b : eb) {
+      if (b.n > e->eig_smem_f64 && reflect_config(b.n, &tw64, &panel64, true)) {
+        rs.push_back(b);
+        wsz += int64_t(b.n) * b.ld;
+        max_r64 = std::max(max_r64, b.n);
+        if (eig_cluster_size_for(b.n, true) > 0) eligible64.push_back(b.n);
+      } else {
+        one.push_back(b);
+      }
+    }
+    if (!rs.empty()) {
+      cluster64 = eligible64.size() == rs.size() && cluster_wanted(e, eligible64, true);
+      key64 = hist_key(rs, true);
+      plans64 = reflect_plans(e, key64, max_r64, true);
+      tiles64 = reflect_tiles(rs, plans64);
+      DevPtr w = dalloc(e, 3 * wsz * sizeof(double) + 16);
+      hold.push_back(w);
+      double *base = static_cast<double *>(w->ptr);
+      int64_t o = 0;
+      for (size_t k = 0; k < rs.size(); ++k) {
+        EigBlock &b = rs[k];
+        b.W64 = base + o;
+        b.V64 = base + wsz + o;
+        b.Bt64 = base + 2 * wsz + o;
+        o += int64_t(b.n) * b.ld;
+      }
+      n_f64 = int(one.size());
+      eb = one;
+      eb.insert(eb.end(), rs.begin(), rs.end());
+    }
+  }
+
+  Arena ar;
+  const size_t o_eb = ar.add(eb);
+  std::vector<size_t> o_t64(tiles64.size());
+  for (size_t p = 0; p < tiles64.size(); ++p) o_t64[p] = ar.add(tiles64[p]);
+  std::vector<int> st(eb.size() + 1, 0);
+  const size_t o_st = ar.add(st);
+  DevPtr desc;
+  char *d = ar.push(e, desc);
+  hold.push_back(desc);
+  {
+    const int nrs = int(eb.size()) - n_f64;
+    // the tred2 + QL blocks run on the side stream beside the reflector solver
+    const bool fork = nrs > 0 && n_f64 > 0;
+    if (fork) {
+      check_cuda(cudaEventRecord(e->fork_ev, s), "fork");
+      check_cuda(cudaStreamWaitEvent(e->side, e->fork_ev, 0), "fork");
+    }
+    if (nrs > 0) {
+      std::vector<EigBlock> rsb(eb.begin() + n_f64, eb.end());
+      if (cluster64) {
+        Prof pf(e, "k_eig_cluster_f64", eig_flops(rsb) * 0.4);  // tridiagonal reduction: 4/3 n^3
+        const int cs = eig_cluster_size_for(max_r64, true);
+        const std::string what = "eigensolve f64 (cluster of " + std::to_string(cs) + " CTAs, " +
+                                 std::to_string(nrs) + " blocks, largest " + std::to_string(max_r64) + ")";
+        check_cuda(launch_eig_cluster(at<EigBlock>(d, o_eb) + n_f64, nrs, max_r64, cs, true, s), what.c_str());
+        count_launch(e);
+        post_launch("eigensolve f64 (cluster)");
+      } else {
+        Prof pf(e, "k_eig_bi_f64", eig_flops(rsb) * 0.4);  // tridiagonal reduction: 4/3 n^3
+        launch_eig_bisect_f64(at<EigBlock>(d, o_eb) + n_f64, nrs, max_r64, e->eig_smem_f64, s);
+        count_launch(e);
+        post_launch("eigensolve f64 (reflector solver)");
+      }
+      double f = 0;  // applying the reflectors: 2 n^3 per block
+      for (auto &x : rsb) f += 2.0 * double(x.n) * x.n * x.n;
+      run_reflect(e, key64, plans64, "k_reflect_f64", f, [&](size_t p) {
+        launch_reflect(at<EigBlock>(d, o_eb) + n_f64, at<int2>(d, o_t64[p]), int(tiles64[p].size()), max_r64,
+                       plans64[p].tw, plans64[p].panel, s, true);
+      });
+    }
+    if (n_f64 > 0) {
+      cudaStream_t so = fork ? e->side : s;
+      int mx = 0;
+      for (int b = 0; b < n_f64; ++b) mx = std::max(mx, eb[b].n);
+      std::vector<EigBlock> oneb(eb.begin(), eb.begin() + n_f64);
+      Prof pf(e, "k_eig_f64", eig_flops(oneb), so);
+      launch_eig_f64(at<EigBlock>(d, o_eb), n_f64, mx, e->eig_smem_f64, at<int>(d, o_st), so);
+      count_launch(e);
+      post_launch("eigensolve");
+    }
+    if (fork) {
+      check_cuda(cudaEventRecord(e->join_ev, e->side), "join");
+      check_cuda(cudaStreamWaitEvent(s, e->join_ev, 0), "join");
+    }
+  }
+  F64Solve r;
+  r.order = eb;
+  r.d_status = at<int>(d, o_st);
+  return r;
+}
+
 static MixedStatus mixed_eigensolve(nrg_engine *e, std::vector<DevBlock *> &blks, int max_n,
                                     std::vector<DevPtr> &hold) {
   cudaStream_t s = e->stream;
@@ -791,8 +921,12 @@ static MixedStatus mixed_eigensolve(nrg_engine *e, std::vector<DevBlock *> &blks
   // shared memory holds go to k_eig_cluster, the others to k_eig_bi
   std::vector<EigBlock> eb_one, eb_cl;
   int max_one = 0, max_cl = 0;
+  std::vector<int> eligible;
+  for (size_t b = 0; b < nb; ++b)
+    if (eb[b].n > e->eig_smem_f32 && eig_cluster_size_for(eb[b].n, false) > 0) eligible.push_back(eb[b].n);
+  const bool cluster_on = cluster_wanted(e, eligible, false);
   for (size_t b = 0; b < nb; ++b) {
-    if (e->eig_cluster && eb[b].n > e->eig_smem_f32 && eig_cluster_size_for(eb[b].n, false) > 0) {
+    if (cluster_on && eb[b].n > e->eig_smem_f32 && eig_cluster_size_for(eb[b].n, false) > 0) {
       eb_cl.push_back(eb[b]);
       max_cl = std::max(max_cl, eb[b].n);
     } else {
@@ -1130,59 +1264,14 @@ static void batch_add_site(nrg_run *const *runs, int nruns, const double *t, int
   for (int o : order) eblk_sorted.push_back(eblk[o]);
   e->work[0] += eig_flops(eblk);
   elem_block.insert(elem_block.end(), block_run.begin(), block_run.end());
-  // FP64 path: blocks above the one-CTA shared-memory limit that a cluster
-  // holds are solved by the reflector solver (k_eig_cluster<double> +
-  // k_reflect<double>, the mixed path's first stage in FP64) and moved to the
-  // end of the list; the others by k_eig<double> (tred2 + QL)
-  int n_f64 = int(eblk_sorted.size()), max_cl64 = 0, tw64 = 8, panel64 = 1;
-  uint64_t key64 = 0;
-  std::vector<ReflectPlan> plans64;
-  std::vector<std::vector<int2>> tiles64;
-  if (e->precision == NRG_PREC_FP64 && e->eig_cluster) {
-    std::vector<EigBlock> one, cl;
-    int64_t wsz = 0;
-    for (auto &b : eblk_sorted) {
-      if (b.n > e->eig_smem_f64 && eig_cluster_size_for(b.n, true) > 0 && reflect_config(b.n, &tw64, &panel64, true)) {
-        cl.push_back(b);
-        wsz += int64_t(b.n) * b.ld;
-        max_cl64 = std::max(max_cl64, b.n);
-      } else {
-        one.push_back(b);
-      }
-    }
-    if (!cl.empty()) {
-      key64 = hist_key(cl, true);
-      plans64 = reflect_plans(e, key64, max_cl64, true);
-      tiles64 = reflect_tiles(cl, plans64);
-      DevPtr w = dalloc(e, 3 * wsz * sizeof(double) + 16);
-      hold.push_back(w);
-      double *base = static_cast<double *>(w->ptr);
-      int64_t o = 0;
-      for (size_t k = 0; k < cl.size(); ++k) {
-        EigBlock &b = cl[k];
-        b.W64 = base + o;
-        b.V64 = base + wsz + o;
-        b.Bt64 = base + 2 * wsz + o;
-        o += int64_t(b.n) * b.ld;
-      }
-      n_f64 = int(one.size());
-      eblk_sorted = one;
-      eblk_sorted.insert(eblk_sorted.end(), cl.begin(), cl.end());
-    }
-  }
-
   Arena ar;
   size_t o_ablk = ar.add(ablk), o_asub = ar.add(asub), o_apair = ar.add(apair),
-         o_aterm = ar.add(aterm), o_eblk = ar.add(eblk_sorted), o_trun = ar.add(trun),
+         o_aterm = ar.add(aterm), o_trun = ar.add(trun),
          o_tblk = ar.add(tblk), o_elem = ar.add(elem_block);
-  std::vector<size_t> o_t64(tiles64.size());
-  for (size_t p = 0; p < tiles64.size(); ++p) o_t64[p] = ar.add(tiles64[p]);
   std::vector<int> zeros(nblk_total + 1, 0);
   size_t o_kept = ar.add(zeros);
   std::vector<TruncResult> tres(nruns);
   size_t o_tres = ar.add(tres);
-  std::vector<int> stat(eblk_sorted.size() + 1, 0);
-  size_t o_stat = ar.add(stat);
   DevPtr desc;
   char *d = ar.push(e, desc);
   hold.push_back(desc);
@@ -1200,35 +1289,9 @@ static void batch_add_site(nrg_run *const *runs, int nruns, const double *t, int
     fail(NRG_E_ARG, "block dimension " + std::to_string(max_n) + " exceeds the solver limit " +
                         std::to_string(eig_max_n_f64()));
   MixedStatus mstat;
+  F64Solve f64;
   if (e->precision == NRG_PREC_FP64) {
-    const int ncl = int(eblk_sorted.size()) - n_f64;
-    if (ncl > 0) {
-      std::vector<EigBlock> clb(eblk_sorted.begin() + n_f64, eblk_sorted.end());
-      {
-        Prof pf(e, "k_eig_cluster_f64", eig_flops(clb) * 0.4);  // tridiagonal reduction: 4/3 n^3
-        const int cs = eig_cluster_size_for(max_cl64, true);
-        const std::string what = "eigensolve f64 (cluster of " + std::to_string(cs) + " CTAs, " +
-                                 std::to_string(ncl) + " blocks, largest " + std::to_string(max_cl64) + ")";
-        check_cuda(launch_eig_cluster(at<EigBlock>(d, o_eblk) + n_f64, ncl, max_cl64, cs, true, s), what.c_str());
-        count_launch(e);
-        post_launch("eigensolve f64 (cluster)");
-      }
-      double f = 0;  // applying the reflectors: 2 n^3 per block
-      for (auto &x : clb) f += 2.0 * double(x.n) * x.n * x.n;
-      run_reflect(e, key64, plans64, "k_reflect_f64", f, [&](size_t p) {
-        launch_reflect(at<EigBlock>(d, o_eblk) + n_f64, at<int2>(d, o_t64[p]), int(tiles64[p].size()), max_cl64,
-                       plans64[p].tw, plans64[p].panel, s, true);
-      });
-    }
-    if (n_f64 > 0) {
-      int mx = 0;
-      for (int b = 0; b < n_f64; ++b) mx = std::max(mx, eblk_sorted[b].n);
-      std::vector<EigBlock> oneb(eblk_sorted.begin(), eblk_sorted.begin() + n_f64);
-      Prof pf(e, "k_eig_f64", eig_flops(oneb));
-      launch_eig_f64(at<EigBlock>(d, o_eblk), n_f64, mx, e->eig_smem_f64, at<int>(d, o_stat), s);
-      count_launch(e);
-      post_launch("eigensolve");
-    }
+    f64 = fp64_eigensolve(e, eblk_sorted, hold, s);
   } else {
     if (max_n > refine_max_n())
       fail(NRG_E_ARG, "block dimension " + std::to_string(max_n) + " exceeds the refinement limit");
@@ -1268,8 +1331,10 @@ static void batch_add_site(nrg_run *const *runs, int nruns, const double *t, int
                              cudaMemcpyDeviceToHost, s), "kept D2H");
   check_cuda(cudaMemcpyAsync(tres.data(), d + o_tres, nruns * sizeof(TruncResult),
                              cudaMemcpyDeviceToHost, s), "result D2H");
-  check_cuda(cudaMemcpyAsync(stat.data(), d + o_stat, eblk_sorted.size() * sizeof(int),
-                             cudaMemcpyDeviceToHost, s), "status D2H");
+  std::vector<int> stat(f64.order.size() + 1, 0);
+  if (!f64.order.empty())
+    check_cuda(cudaMemcpyAsync(stat.data(), f64.d_status, f64.order.size() * sizeof(int),
+                               cudaMemcpyDeviceToHost, s), "status D2H");
   MixedCheck mcheck;
   mcheck.enqueue(mstat, s);
   std::vector<std::vector<double>> sorted(nruns), evals(nruns);
@@ -1287,9 +1352,9 @@ static void batch_add_site(nrg_run *const *runs, int nruns, const double *t, int
   check_cuda(cudaStreamSynchronize(s), "site step");
   check_kernel_error(e);
   mcheck.check(e);
-  for (size_t b = 0; b < eblk_sorted.size(); ++b)
+  for (size_t b = 0; b < f64.order.size(); ++b)
     if (stat[b]) fail(NRG_E_EIG, "block eigensolver did not converge (n = " +
-                                     std::to_string(eblk_sorted[b].n) + ")");
+                                     std::to_string(f64.order[b].n) + ")");
   // ---- pending truncation per run + rotation descriptors
   std::vector<GemmGroup> groups;
   std::vector<GemmContrib> contribs;
@@ -1507,19 +1572,12 @@ extern "C" int nrg_eigh_batched(nrg_engine *e, int nblk, const int *dims, const 
         eb[b].ld = blocks[b].ld;
         eb[b].ldu = blocks[b].ld;
       }
+      std::stable_sort(eb.begin(), eb.end(), [](const EigBlock &x, const EigBlock &y) { return x.n > y.n; });
+      F64Solve f = fp64_eigensolve(e, eb, hold, s);
       std::vector<int> st(nblk + 1, 0);
-      Arena a;
-      size_t o1 = a.add(eb), o2 = a.add(st);
-      DevPtr dd;
-      char *dp = a.push(e, dd);
-      {
-        Prof pf(e, "k_eig_f64", eig_flops(eb));
-        launch_eig_f64(at<EigBlock>(dp, o1), nblk, max_n, e->eig_smem_f64, at<int>(dp, o2), s);
-        count_launch(e);
-        post_launch("eigh f64");
-      }
-      check_cuda(cudaMemcpyAsync(st.data(), dp + o2, nblk * sizeof(int), cudaMemcpyDeviceToHost, s), "status");
+      check_cuda(cudaMemcpyAsync(st.data(), f.d_status, nblk * sizeof(int), cudaMemcpyDeviceToHost, s), "status");
       check_cuda(cudaStreamSynchronize(s), "eigh");
+      check_kernel_error(e);
       for (int b = 0; b < nblk; ++b)
         if (st[b]) fail(NRG_E_EIG, "block eigensolver did not converge");
     } else {

@@ -644,7 +644,12 @@ int nrg_engine_create(const nrg_engine_opts *opts, nrg_engine **out) {
     check_cuda(cudaMalloc(&e->d_kerr, sizeof(int)), "cudaMalloc (kernel error word)");
     check_cuda(cudaMemset(e->d_kerr, 0, sizeof(int)), "cudaMemset");
     if (const char *oz = std::getenv("NRG_OZAKI")) e->ozaki = std::atoi(oz) & 3;
-    if (const char *c = std::getenv("NRG_EIG_CLUSTER")) e->eig_cluster = std::atoi(c) != 0;
+    if (const char *c = std::getenv("NRG_EIG_CLUSTER")) e->eig_cluster = std::min(2, std::max(0, std::atoi(c)));
+    {
+      int dev = 0;
+      check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
+      check_cuda(cudaDeviceGetAttribute(&e->sm_count, cudaDevAttrMultiProcessorCount, dev), "SM count");
+    }
     if (const char *c = std::getenv("NRG_AUTOTUNE")) e->autotune = std::atoi(c) != 0;
     *out = e;
   });
@@ -774,6 +779,14 @@ int nrg_engine_set_autotune(nrg_engine *e, int on) {
   return guard([&] {
     if (!e) fail(NRG_E_ARG, "null engine");
     e->autotune = on != 0;
+  });
+}
+
+int nrg_engine_set_eig_cluster(nrg_engine *e, int mode) {
+  return guard([&] {
+    if (!e) fail(NRG_E_ARG, "null engine");
+    if (mode < 0 || mode > 2) fail(NRG_E_ARG, "cluster mode must be 0, 1 or 2");
+    e->eig_cluster = mode;
   });
 }
 

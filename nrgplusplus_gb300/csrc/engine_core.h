@@ -150,7 +150,11 @@ struct nrg_engine {
   int eig_smem_f64 = 0, eig_smem_f32 = 0;
   // blocks above the one-CTA shared-memory limit go to the cluster solver
   // (NRG_EIG_CLUSTER=0 turns it off)
-  bool eig_cluster = true;
+  // blocks above one SM's shared memory: 0 = one-CTA solver only, 1 = the
+  // cluster solver when every cluster of the launch fits one wave of the
+  // device (a latency-bound launch), 2 = the cluster solver always
+  int eig_cluster = 1;
+  int sm_count = 0;
   // launch-shape autotuner (nrg_engine_set_autotune): per block-size
   // histogram, the reflector back-transform's column-tile width and panel,
   // picked by timing every candidate on the first launch that shows the

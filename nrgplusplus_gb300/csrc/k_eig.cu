@@ -17,6 +17,7 @@
 // The matrix lives in shared memory when it fits, otherwise in the block's
 // own global buffer (L2 resident).  The QL sweep count per eigenvalue is
 // capped; a block that hits the cap sets status[b] = 1 and stops.
+#include "eig_tri.cuh"
 #include "nrg_internal.h"
 
 #include <algorithm>
@@ -486,16 +487,15 @@ k_eig(const EigBlock *__restrict__ blocks, int max_n_smem, int *status, const in
 //     multi-CTA kernel (k_reflect).
 // Accuracy is FP32 (~1e-6); the FP64-accurate refinement follows.
 
-constexpr float kClusterGap = 1e-5f;
 constexpr int kInvIter = 3;
 
-__device__ __forceinline__ float block_minf(float v, float *red) {
-  for (int o = 16; o > 0; o >>= 1) v = fminf(v, __shfl_xor_sync(0xffffffffu, v, o));
+template <typename T> __device__ __forceinline__ T block_min(T v, T *red) {
+  for (int o = 16; o > 0; o >>= 1) v = min(v, __shfl_xor_sync(0xffffffffu, v, o));
   __syncthreads();
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
   __syncthreads();
-  float m = red[0];
-  for (int w = 1; w < kWarps; ++w) m = fminf(m, red[w]);
+  T m = red[0];
+  for (int w = 1; w < kWarps; ++w) m = min(m, red[w]);
   __syncthreads();
   return m;
 }
@@ -564,6 +564,29 @@ __device__ float inv_solve(const float *d, const float *e, int n, float lam, flo
   return rsqrtf(fmaxf(nrm, 1e-37f));
 }
 
+// FP32 uses the forms above, FP64 the shared templates (eig_tri.cuh)
+__device__ __forceinline__ int sturm_t(const float *d, const float *e, int n, float x) {
+  return sturm_count(d, e, n, x);
+}
+__device__ __forceinline__ int sturm_t(const double *d, const double *e, int n, double x) {
+  return sturm_c<double>(d, e, n, x);
+}
+__device__ __forceinline__ float inv_t(const float *d, const float *e, int n, float lam, float pivmin, float s,
+                                       float *V, float *Bt, int ld, int j) {
+  return inv_solve(d, e, n, lam, pivmin, s, V, Bt, ld, j);
+}
+__device__ __forceinline__ double inv_t(const double *d, const double *e, int n, double lam, double pivmin,
+                                        double s, double *V, double *Bt, int ld, int j) {
+  return inv_solve_c<double>(d, e, n, lam, pivmin, s, V, Bt, ld, j);
+}
+__device__ __forceinline__ float rnorm_t(float x) { return rsqrtf(fmaxf(x, 1e-37f)); }
+__device__ __forceinline__ double rnorm_t(double x) { return 1.0 / sqrt(fmax(x, 1e-300)); }
+
+// One CTA per block.  T = float: the mixed path's first stage (outputs in
+// W, V, Bt).  T = double: the plain FP64 path's reflector solver for blocks
+// above the shared-memory limit (W64, V64, Bt64), the same work in FP64 with
+// no refinement after it.
+template <typename T>
 __global__ void __launch_bounds__(kThreads, 1)
 k_eig_bi(const EigBlock *__restrict__ blocks, int max_n_smem, int smem_total) {
   extern __shared__ __align__(16) char smem[];
@@ -571,23 +594,24 @@ k_eig_bi(const EigBlock *__restrict__ blocks, int max_n_smem, int smem_total) {
   const int n = B.n;
   if (n == 0) return;
   const bool in_smem = (n <= max_n_smem);
-  float *amat, *d, *e, *u, *p, *red;
+  T *amat, *d, *e, *u, *p, *red;
   int *rank;
   Ctl *ctl;
   char *scratch;
-  carve<float>(smem, n, in_smem, amat, d, e, u, p, red, rank, ctl, &scratch);
-  float *a = in_smem ? amat : B.W;
+  carve<T>(smem, n, in_smem, amat, d, e, u, p, red, rank, ctl, &scratch);
+  T *const Wg = Bufs<T>::W(B), *const Vg = Bufs<T>::V(B), *const Btg = Bufs<T>::Bt(B);
+  T *a = in_smem ? amat : Wg;
   const int lda = in_smem ? n + 1 : B.ld;
   for (int64_t idx = threadIdx.x; idx < int64_t(n) * n; idx += kThreads) {
     const int r = int(idx / n), c = int(idx - int64_t(r) * n);
-    a[int64_t(r) * lda + c] = float(B.H[int64_t(r) * B.ld + c]);
+    a[int64_t(r) * lda + c] = T(B.H[int64_t(r) * B.ld + c]);
   }
   __syncthreads();
-  tred2_reduce<float>(a, lda, n, d, e, u, p, red, false, !in_smem && (lda % 2 == 0));
+  tred2_reduce<T>(a, lda, n, d, e, u, p, red, false, sizeof(T) == sizeof(float) && !in_smem && (lda % 2 == 0));
   // T's diagonal into d; h_i (0: no reflector) onto the diagonal of the
   // reflector matrix, which k_reflect reads from the block's W buffer
   for (int i = threadIdx.x; i < n; i += kThreads) {
-    const float h = (i == 0) ? 0.f : d[i];
+    const T h = (i == 0) ? T(0) : d[i];
     d[i] = a[int64_t(i) * lda + i];
     a[int64_t(i) * lda + i] = h;
   }
@@ -595,48 +619,48 @@ k_eig_bi(const EigBlock *__restrict__ blocks, int max_n_smem, int smem_total) {
   if (in_smem) {  // reflectors (lower triangle and diagonal) out to W
     for (int64_t idx = threadIdx.x; idx < int64_t(n) * n; idx += kThreads) {
       const int r = int(idx / n), c = int(idx - int64_t(r) * n);
-      if (c <= r) B.W[int64_t(r) * B.ld + c] = a[int64_t(r) * lda + c];
+      if (c <= r) Wg[int64_t(r) * B.ld + c] = a[int64_t(r) * lda + c];
     }
   }
   // Gershgorin interval and the norm used for pivots and cluster gaps
-  float lo = 3e38f, hi = -3e38f, tn = 0.f;
+  T lo = T(3e38f), hi = T(-3e38f), tn = T(0);
   for (int i = threadIdx.x; i < n; i += kThreads) {
-    const float r = fabsf(e[i]) + (i + 1 < n ? fabsf(e[i + 1]) : 0.f);
-    lo = fminf(lo, d[i] - r);
-    hi = fmaxf(hi, d[i] + r);
-    tn = fmaxf(tn, fabsf(d[i]) + r);
+    const T r = abs_c(e[i]) + (i + 1 < n ? abs_c(e[i + 1]) : T(0));
+    lo = min(lo, d[i] - r);
+    hi = max(hi, d[i] + r);
+    tn = max(tn, abs_c(d[i]) + r);
   }
-  lo = block_minf(lo, red);
-  hi = -block_minf(-hi, red);
-  tn = -block_minf(-tn, red);
-  const float span = fmaxf(hi - lo, 1e-30f);
-  lo -= 1e-6f * span;
-  hi += 1e-6f * span;
-  float *lam = u;                           // eigenvalues, ascending
+  lo = block_min<T>(lo, red);
+  hi = -block_min<T>(-hi, red);
+  tn = -block_min<T>(-tn, red);
+  const T span = max(hi - lo, T(1e-30f));
+  lo -= T(1e-6f) * span;
+  hi += T(1e-6f) * span;
+  T *lam = u;                               // eigenvalues, ascending
   int *cl = reinterpret_cast<int *>(p);     // cluster [start, end) pairs
   for (int j = threadIdx.x; j < n; j += kThreads) {
-    float a0 = lo, b0 = hi;
+    T a0 = lo, b0 = hi;
     for (int it = 0; it < 80; ++it) {
-      const float mid = 0.5f * (a0 + b0);
+      const T mid = T(0.5f) * (a0 + b0);
       if (mid <= a0 || mid >= b0) break;
-      if (sturm_count(d, e, n, mid) > j) b0 = mid; else a0 = mid;
+      if (sturm_t(d, e, n, mid) > j) b0 = mid; else a0 = mid;
     }
-    lam[j] = 0.5f * (a0 + b0);
+    lam[j] = T(0.5f) * (a0 + b0);
   }
   __syncthreads();
-  const float pivmin = fmaxf(tn * 1.2e-7f, 1e-20f);
+  const T pivmin = Tiny<T>::pivmin(tn);
   // inverse iteration for every eigenvalue in parallel
   for (int j = threadIdx.x; j < n; j += kThreads) {
     for (int i = 0; i < n; ++i)
-      B.V[int64_t(i) * B.ld + j] = 1.0f + 0.25f * float((i * 7919 + j * 104729) % 97) / 97.f;
-    float s = 1.f;
-    for (int it = 0; it < kInvIter; ++it) s = inv_solve(d, e, n, lam[j], pivmin, s, B.V, B.Bt, B.ld, j);
-    for (int i = 0; i < n; ++i) B.V[int64_t(i) * B.ld + j] *= s;
+      Vg[int64_t(i) * B.ld + j] = T(1.0f + 0.25f * float((i * 7919 + j * 104729) % 97) / 97.f);
+    T sc = T(1);
+    for (int it = 0; it < kInvIter; ++it) sc = inv_t(d, e, n, lam[j], pivmin, sc, Vg, Btg, B.ld, j);
+    for (int i = 0; i < n; ++i) Vg[int64_t(i) * B.ld + j] *= sc;
   }
   // clusters of near-degenerate eigenvalues
   if (threadIdx.x == 0) {
     int c = 0, k = 0;
-    const float gap = kClusterGap * fmaxf(tn, 1e-30f);
+    const T gap = Tiny<T>::gap * max(tn, T(1e-30f));
     while (k < n) {
       int q = k + 1;
       while (q < n && lam[q] - lam[q - 1] <= gap) ++q;
@@ -653,49 +677,49 @@ k_eig_bi(const EigBlock *__restrict__ blocks, int max_n_smem, int smem_total) {
   const int ncl = ctl->m;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   // Each warp iterates its clusters' members in shared memory (the member x
-  // and its LU pivots b: 2n floats per warp, in the area the matrix used),
+  // and its LU pivots b: 2n values per warp, in the area the matrix used),
   // so the sequential solves run at shared-memory latency.  Without room for
   // one warp's pair the member is iterated in place in V / Bt.
   const size_t avail = size_t(smem_total) - size_t(scratch - smem);
-  int nw = int(avail / (sizeof(float) * 2 * size_t(n)));
+  int nw = int(avail / (sizeof(T) * 2 * size_t(n)));
   const bool staged = nw > 0;
   if (nw > kWarps || !staged) nw = kWarps;
   if (warp < nw) {
     for (int q = warp; q < ncl; q += nw) {
       const int c0 = cl[2 * q], c1 = cl[2 * q + 1];
       for (int j = c0; j < c1; ++j) {
-        float *xv, *bv;
+        T *xv, *bv;
         int xs;
         if (staged) {
-          xv = reinterpret_cast<float *>(scratch) + size_t(warp) * 2 * n;
+          xv = reinterpret_cast<T *>(scratch) + size_t(warp) * 2 * n;
           bv = xv + n;
           xs = 1;
-          for (int i = lane; i < n; i += 32) xv[i] = B.V[int64_t(i) * B.ld + j];
+          for (int i = lane; i < n; i += 32) xv[i] = Vg[int64_t(i) * B.ld + j];
         } else {
-          xv = B.V + j;
-          bv = B.Bt + j;
+          xv = Vg + j;
+          bv = Btg + j;
           xs = B.ld;
         }
         __syncwarp();
         for (int rep = 0; rep < 2; ++rep) {
-          if (lane == 0) inv_solve(d, e, n, lam[j], pivmin, 1.f, xv, bv, xs, 0);
+          if (lane == 0) inv_t(d, e, n, lam[j], pivmin, T(1), xv, bv, xs, 0);
           __syncwarp();
           for (int k = c0; k < j; ++k) {  // earlier members are final in V
-            float dot = 0.f;
-            for (int i = lane; i < n; i += 32) dot += B.V[int64_t(i) * B.ld + k] * xv[int64_t(i) * xs];
+            T dot = T(0);
+            for (int i = lane; i < n; i += 32) dot += Vg[int64_t(i) * B.ld + k] * xv[int64_t(i) * xs];
             dot = warp_sum(dot);
-            for (int i = lane; i < n; i += 32) xv[int64_t(i) * xs] -= dot * B.V[int64_t(i) * B.ld + k];
+            for (int i = lane; i < n; i += 32) xv[int64_t(i) * xs] -= dot * Vg[int64_t(i) * B.ld + k];
             __syncwarp();
           }
-          float nrm = 0.f;
+          T nrm = T(0);
           for (int i = lane; i < n; i += 32) nrm += xv[int64_t(i) * xs] * xv[int64_t(i) * xs];
           nrm = warp_sum(nrm);
-          const float sc = rsqrtf(fmaxf(nrm, 1e-37f));
-          for (int i = lane; i < n; i += 32) xv[int64_t(i) * xs] *= sc;
+          const T scn = rnorm_t(nrm);
+          for (int i = lane; i < n; i += 32) xv[int64_t(i) * xs] *= scn;
           __syncwarp();
         }
         if (staged)
-          for (int i = lane; i < n; i += 32) B.V[int64_t(i) * B.ld + j] = xv[i];
+          for (int i = lane; i < n; i += 32) Vg[int64_t(i) * B.ld + j] = xv[i];
         __syncwarp();
       }
     }
@@ -829,14 +853,24 @@ void launch_eig_f64(const EigBlock *blocks, int nblocks, int max_n, int max_n_sm
   launch<double>(blocks, nblocks, max_n, max_n_smem, status, s, gate);
 }
 
+template <typename T>
+static void launch_bisect(const EigBlock *blocks, int nblocks, int max_n, int max_n_smem, cudaStream_t s) {
+  if (nblocks == 0) return;
+  ensure_smem_limit(reinterpret_cast<const void *>(k_eig_bi<T>), kSmemBytes);
+  size_t bytes = smem_bytes<T>(max_n, max_n <= max_n_smem);
+  if (max_n > max_n_smem) bytes = std::max(bytes, smem_bytes<T>(max_n_smem, true));
+  if (bytes > size_t(kSmemBytes)) bytes = kSmemBytes;
+  k_eig_bi<T><<<nblocks, kThreads, bytes, s>>>(blocks, max_n_smem, int(bytes));
+}
+
 void launch_eig_bisect_f32(const EigBlock *blocks, int nblocks, int max_n, int max_n_smem,
                            cudaStream_t s) {
-  if (nblocks == 0) return;
-  ensure_smem_limit(reinterpret_cast<const void *>(k_eig_bi), kSmemBytes);
-  size_t bytes = smem_bytes<float>(max_n, max_n <= max_n_smem);
-  if (max_n > max_n_smem) bytes = std::max(bytes, smem_bytes<float>(max_n_smem, true));
-  if (bytes > size_t(kSmemBytes)) bytes = kSmemBytes;
-  k_eig_bi<<<nblocks, kThreads, bytes, s>>>(blocks, max_n_smem, int(bytes));
+  launch_bisect<float>(blocks, nblocks, max_n, max_n_smem, s);
+}
+
+void launch_eig_bisect_f64(const EigBlock *blocks, int nblocks, int max_n, int max_n_smem,
+                           cudaStream_t s) {
+  launch_bisect<double>(blocks, nblocks, max_n, max_n_smem, s);
 }
 
 bool reflect_config(int max_n, int *tw, int *panel, bool fp64) {

@@ -70,6 +70,10 @@ struct EigBlock {
 // tiles: (block, column tile of width tw).
 void launch_eig_bisect_f32(const EigBlock *blocks, int nblocks, int max_n, int max_n_smem,
                            cudaStream_t s);
+// The same solver in FP64 (W64, V64, Bt64): the plain path's blocks above the
+// shared-memory limit.
+void launch_eig_bisect_f64(const EigBlock *blocks, int nblocks, int max_n, int max_n_smem,
+                           cudaStream_t s);
 // fp64: the FP64 reflector solver's buffers (W64, V64) and tiles.
 bool reflect_config(int max_n, int *tw, int *panel, bool fp64 = false);
 int reflect_max_n(bool fp64 = false);

@@ -60,18 +60,19 @@ def test_cluster_and_one_cta_solvers_agree(monkeypatch, sizes):
         a = rng.standard_normal((n, n))
         mats.append((a + a.T) * 0.5)
     out = {}
-    for flag in ("1", "0"):
+    for flag in ("2", "1", "0"):
         monkeypatch.setenv("NRG_EIG_CLUSTER", flag)
         eng = api.Engine(api.PREC_MIXED)
         eng.eigh_batched(mats)        # the largest launch first,
         eng.eigh_batched(mats[:1])    # a smaller one,
         out[flag] = eng.eigh_batched(mats)  # and the largest again
         eng.close()
-    for h, (w1, U1), (w0, U0) in zip(mats, out["1"], out["0"]):
+    for h, (w2, U2), (w1, U1), (w0, U0) in zip(mats, out["2"], out["1"], out["0"]):
         n = h.shape[0]
         scale = max(1.0, np.abs(h).max())
-        assert np.abs(w1 - w0).max() <= 1e-12 * scale * n ** 0.5
-        assert np.abs(h @ U1 - U1 * w1).max() <= 1e-11 * scale * n ** 0.5
+        for w, U in ((w2, U2), (w1, U1)):
+            assert np.abs(w - w0).max() <= 1e-12 * scale * n ** 0.5
+            assert np.abs(h @ U - U * w).max() <= 1e-11 * scale * n ** 0.5
 
 
 def test_autotuned_back_transform_is_bit_identical():

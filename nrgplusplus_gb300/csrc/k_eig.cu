@@ -29,6 +29,7 @@ constexpr int kThreads = 512;
 constexpr int kWarps = kThreads / 32;
 constexpr int kMaxQlIter = 60;
 constexpr int kSmemBytes = 225 * 1024;
+constexpr int kBiVecs = 6;  // k_eig_bi's shared vectors of n: d, e, two u and two p / q
 
 template <typename T> __device__ __forceinline__ T tabs(T x) { return x < T(0) ? -x : x; }
 __device__ __forceinline__ double thypot(double a, double b) { return hypot(a, b); }
@@ -246,6 +247,173 @@ __device__ void tred2_reduce(T *a, int lda, int n, T *d, T *e, T *u, T *p, T *re
 #undef A
 }
 
+// The reflector solver's reduction (k_eig_bi): the same Householder steps as
+// tred2_reduce without store_uh, with each step's rank-2 update deferred
+// into the next step's matrix-vector product, so a step makes one pass over
+// the active rows (read and write) instead of two reads and a write:
+//   step i: row i takes the pending update (u, q of step i + 1), forms
+//           u' / h' / e_i; then rows 0..i-1 take the pending update and
+//           p'_j = (A u')_j / h' from the updated values in the same pass;
+//           q' = p' - (u'.p' / 2h') u' becomes the pending update.
+// The values are those of the separate passes.  ua / pa, ub / pb: two pairs
+// of shared vectors of n, swapped every step.  wide: global memory, even
+// lda, 8- or 16-byte column pairs; otherwise one column per lane.
+template <typename T> struct Pair;
+template <> struct Pair<float> { using type = float2; };
+template <> struct Pair<double> { using type = double2; };
+
+// Rows 0..jn-1: the pending update over ncol columns (UPD) and/or the dot
+// products with un (DOT, pn[j] = dot / hn).  Four rows per warp at a time, so
+// each lane keeps several independent loads in flight.
+template <typename T, bool WIDE, bool UPD, bool DOT>
+__device__ void fused_rows(T *a, int lda, int jn, int ncol, const T *u, const T *q, const T *un, T *pn, T hn) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  using P = typename Pair<T>::type;
+  const int nc = WIDE ? (ncol + 1) >> 1 : ncol;
+  for (int j0 = warp; j0 < jn; j0 += 4 * kWarps) {
+    T *row[4];
+    T uj[4], qj[4], sd[4];
+    bool ok[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      const int j = j0 + r * kWarps;
+      ok[r] = j < jn;
+      row[r] = a + int64_t(ok[r] ? j : j0) * lda;
+      uj[r] = (UPD && ok[r]) ? u[j] : T(0);
+      qj[r] = (UPD && ok[r]) ? q[j] : T(0);
+      sd[r] = T(0);
+    }
+    if constexpr (WIDE) {
+      const P *u2 = reinterpret_cast<const P *>(u), *q2 = reinterpret_cast<const P *>(q);
+      const P *n2 = reinterpret_cast<const P *>(un);
+#pragma unroll 2
+      for (int c = lane; c < nc; c += 32) {
+        P v[4];
+#pragma unroll
+        for (int r = 0; r < 4; ++r) v[r] = reinterpret_cast<const P *>(row[r])[c];
+        if constexpr (UPD) {
+          const P uu = u2[c], qq = q2[c];
+#pragma unroll
+          for (int r = 0; r < 4; ++r) {
+            v[r].x -= uj[r] * qq.x + qj[r] * uu.x;
+            v[r].y -= uj[r] * qq.y + qj[r] * uu.y;
+          }
+#pragma unroll
+          for (int r = 0; r < 4; ++r)
+            if (ok[r]) reinterpret_cast<P *>(row[r])[c] = v[r];
+        }
+        if constexpr (DOT) {
+          const P w = n2[c];
+#pragma unroll
+          for (int r = 0; r < 4; ++r) sd[r] = fma(v[r].x, w.x, fma(v[r].y, w.y, sd[r]));
+        }
+      }
+    } else {
+      for (int c = lane; c < nc; c += 32) {
+        T v[4];
+#pragma unroll
+        for (int r = 0; r < 4; ++r) v[r] = row[r][c];
+        if constexpr (UPD) {
+          const T uu = u[c], qq = q[c];
+#pragma unroll
+          for (int r = 0; r < 4; ++r) v[r] -= uj[r] * qq + qj[r] * uu;
+#pragma unroll
+          for (int r = 0; r < 4; ++r)
+            if (ok[r]) row[r][c] = v[r];
+        }
+        if constexpr (DOT) {
+          const T w = un[c];
+#pragma unroll
+          for (int r = 0; r < 4; ++r) sd[r] += v[r] * w;
+        }
+      }
+    }
+    if constexpr (DOT) {
+#pragma unroll
+      for (int r = 0; r < 4; ++r) sd[r] = warp_sum(sd[r]);
+      if (lane == 0)
+#pragma unroll
+        for (int r = 0; r < 4; ++r)
+          if (ok[r]) pn[j0 + r * kWarps] = sd[r] / hn;
+    }
+  }
+}
+
+template <typename T, bool WIDE>
+__device__ void tred2_fused(T *a, int lda, int n, T *d, T *e, T *ua, T *pa, T *ub, T *pb, T *red) {
+  const int tid = threadIdx.x;
+  T *u = ua, *q = pa, *un = ub, *pn = pb;
+  bool pending = false;
+  for (int i = n - 1; i >= 1; --i) {
+    const int l = i - 1;
+    T *ai = a + int64_t(i) * lda;
+    if (pending) {  // row i first: it holds the next reflector
+      const T ui = u[i], qi = q[i];
+      for (int c = tid; c <= i; c += kThreads) ai[c] -= ui * q[c] + qi * u[c];
+      __syncthreads();
+    }
+    // the pending update spans columns 0..i, the new product 0..l; in the
+    // wide form the last pair may reach one column further, which u, q and
+    // un hold at zero there
+    const int ncol = pending ? i + 1 : l + 1;
+    T scale = T(0);
+    for (int k = tid; k <= l; k += kThreads) scale += tabs(ai[k]);
+    scale = block_sum(scale, red);
+    if (l == 0 || scale == T(0)) {
+      if (tid == 0) { e[i] = ai[l]; d[i] = T(0); }
+      if (pending) fused_rows<T, WIDE, true, false>(a, lda, i, ncol, u, q, nullptr, nullptr, T(1));
+      __syncthreads();
+      pending = false;
+      continue;
+    }
+    T hs = T(0);
+    for (int k = tid; k <= l; k += kThreads) {
+      const T x = ai[k] / scale;
+      ai[k] = x;
+      un[k] = x;
+      hs += x * x;
+    }
+    T h = block_sum(hs, red);
+    if (tid == 0) {
+      const T f = ai[l];
+      const T g = (f >= T(0)) ? -tsqrt(h) : tsqrt(h);
+      e[i] = scale * g;
+      h -= f * g;
+      ai[l] = f - g;
+      un[l] = f - g;
+      un[i] = T(0);
+      pn[i] = T(0);
+      if (i + 1 < n) {
+        un[i + 1] = T(0);
+        pn[i + 1] = T(0);
+      }
+      red[kWarps] = h;
+    }
+    __syncthreads();
+    h = red[kWarps];
+    __syncthreads();
+    if (pending) fused_rows<T, WIDE, true, true>(a, lda, i, ncol, u, q, un, pn, h);
+    else fused_rows<T, WIDE, false, true>(a, lda, i, ncol, u, q, un, pn, h);
+    __syncthreads();
+    T fs = T(0);
+    for (int j = tid; j <= l; j += kThreads) fs += pn[j] * un[j];
+    const T f = block_sum(fs, red);
+    const T hh = f / (h + h);
+    for (int j = tid; j <= l; j += kThreads) pn[j] = pn[j] - hh * un[j];  // q'
+    if (tid == 0) d[i] = h;
+    __syncthreads();
+    T *t = u;
+    u = un;
+    un = t;
+    t = q;
+    q = pn;
+    pn = t;
+    pending = true;
+  }
+  if (tid == 0) { d[0] = T(0); e[0] = T(0); }
+  __syncthreads();
+}
+
 // Accumulation of Q from the reflectors left by tred2_reduce(store_uh):
 // on return a = Q and d = the diagonal of T.
 template <typename T>
@@ -408,7 +576,8 @@ __device__ void write_sorted(const T *a, int lda, int n, const T *d, int *rank, 
 
 template <typename T>
 __device__ void carve(char *smem, int n, bool matrix_in_smem, T *&amat, T *&d, T *&e, T *&u, T *&p,
-                      T *&red, int *&rank, Ctl *&ctl, char **scratch = nullptr) {
+                      T *&red, int *&rank, Ctl *&ctl, char **scratch = nullptr, T **ub = nullptr,
+                      T **pb = nullptr) {
   size_t off = 0;
   auto take = [&](size_t bytes) {
     char *q = smem + off;
@@ -422,6 +591,10 @@ __device__ void carve(char *smem, int n, bool matrix_in_smem, T *&amat, T *&d, T
   u = reinterpret_cast<T *>(take(sizeof(T) * n));
   p = reinterpret_cast<T *>(take(sizeof(T) * n));
   rank = reinterpret_cast<int *>(u);  // reused after the solve
+  if (ub) {  // the second u / q pair of the fused reduction
+    *ub = reinterpret_cast<T *>(take(sizeof(T) * n));
+    *pb = reinterpret_cast<T *>(take(sizeof(T) * n));
+  }
   if (scratch) *scratch = smem + off;  // the matrix area (free once it is reduced) and beyond
   amat = matrix_in_smem ? reinterpret_cast<T *>(take(sizeof(T) * size_t(n) * (n + 1))) : nullptr;
 }
@@ -598,7 +771,8 @@ k_eig_bi(const EigBlock *__restrict__ blocks, int max_n_smem, int smem_total) {
   int *rank;
   Ctl *ctl;
   char *scratch;
-  carve<T>(smem, n, in_smem, amat, d, e, u, p, red, rank, ctl, &scratch);
+  T *ub, *pb;
+  carve<T>(smem, n, in_smem, amat, d, e, u, p, red, rank, ctl, &scratch, &ub, &pb);
   T *const Wg = Bufs<T>::W(B), *const Vg = Bufs<T>::V(B), *const Btg = Bufs<T>::Bt(B);
   T *a = in_smem ? amat : Wg;
   const int lda = in_smem ? n + 1 : B.ld;
@@ -607,7 +781,8 @@ k_eig_bi(const EigBlock *__restrict__ blocks, int max_n_smem, int smem_total) {
     a[int64_t(r) * lda + c] = T(B.H[int64_t(r) * B.ld + c]);
   }
   __syncthreads();
-  tred2_reduce<T>(a, lda, n, d, e, u, p, red, false, sizeof(T) == sizeof(float) && !in_smem && (lda % 2 == 0));
+  if (!in_smem && lda % 2 == 0) tred2_fused<T, true>(a, lda, n, d, e, u, p, ub, pb, red);
+  else tred2_fused<T, false>(a, lda, n, d, e, u, p, ub, pb, red);
   // T's diagonal into d; h_i (0: no reflector) onto the diagonal of the
   // reflector matrix, which k_reflect reads from the block's W buffer
   for (int i = threadIdx.x; i < n; i += kThreads) {
@@ -809,15 +984,15 @@ size_t reflect_bytes(int n, int tw, int panel, size_t elem = sizeof(float)) {
   return elem * (size_t(n) * (tw + 1) + size_t(panel) * (n + 1)) + 64;
 }
 
-template <typename T> size_t smem_bytes(int n, bool in_smem) {
-  size_t b = 16 + 16 * ((sizeof(T) * (kWarps + 1) + 15) / 16) + 4 * ((sizeof(T) * n + 15) & ~15);
+template <typename T> size_t smem_bytes(int n, bool in_smem, int nvec = 4) {
+  size_t b = 16 + 16 * ((sizeof(T) * (kWarps + 1) + 15) / 16) + nvec * ((sizeof(T) * n + 15) & ~15);
   if (in_smem) b += (sizeof(T) * size_t(n) * (n + 1) + 15) & ~size_t(15);
   return b + 64;
 }
 
-template <typename T> int smem_limit() {
+template <typename T> int smem_limit(int nvec = 4) {
   int n = 8;
-  while (smem_bytes<T>(n + 1, true) <= size_t(kSmemBytes)) ++n;
+  while (smem_bytes<T>(n + 1, true, nvec) <= size_t(kSmemBytes)) ++n;
   return n;
 }
 
@@ -836,7 +1011,7 @@ void launch(const EigBlock *blocks, int nblocks, int max_n, int max_n_smem, int 
 }  // namespace
 
 int eig_smem_limit_f64() { return smem_limit<double>(); }
-int eig_smem_limit_f32() { return smem_limit<float>(); }
+int eig_smem_limit_f32() { return smem_limit<float>(kBiVecs); }
 
 // Largest block the solver accepts: its d, e, u, p vectors must fit in shared
 // memory even when the matrix itself stays in global memory.
@@ -857,8 +1032,8 @@ template <typename T>
 static void launch_bisect(const EigBlock *blocks, int nblocks, int max_n, int max_n_smem, cudaStream_t s) {
   if (nblocks == 0) return;
   ensure_smem_limit(reinterpret_cast<const void *>(k_eig_bi<T>), kSmemBytes);
-  size_t bytes = smem_bytes<T>(max_n, max_n <= max_n_smem);
-  if (max_n > max_n_smem) bytes = std::max(bytes, smem_bytes<T>(max_n_smem, true));
+  size_t bytes = smem_bytes<T>(max_n, max_n <= max_n_smem, kBiVecs);
+  if (max_n > max_n_smem) bytes = std::max(bytes, smem_bytes<T>(max_n_smem, true, kBiVecs));
   if (bytes > size_t(kSmemBytes)) bytes = kSmemBytes;
   k_eig_bi<T><<<nblocks, kThreads, bytes, s>>>(blocks, max_n_smem, int(bytes));
 }

@@ -664,8 +664,15 @@ def output_errors(engine, got_mixed, got_fp64):
 def sweep_pass(engines, count):
     """The first `count` instances of the seeded 512-instance sweep, spread
     over the engines (greedy by Nkeep^2 x sites), each engine stepping its
-    share as one heterogeneous batch in its own host thread.  Returns the
-    wall time in seconds."""
+    share as one heterogeneous batch in its own host thread.  Two passes:
+    the first warms the engines on the sweep's block-size histograms (the
+    autotuner times its candidates on the first launch of each); the second
+    is timed.  Returns its wall time in seconds."""
+    _sweep_once(engines, count)
+    return _sweep_once(engines, count)
+
+
+def _sweep_once(engines, count):
     import threading
     from nrgplusplus_gb300 import workloads
     inst = workloads.sweep_instances()[:count]
@@ -815,7 +822,7 @@ def main():
     if args.sweep_runs > 0 and not reduced:
         sweep = {"instances": args.sweep_runs, "of": 512, "seed": "workloads.SWEEP_SEED",
                  "what": "RG flows (all eigenvalues per site) of the first instances of the seeded sweep, "
-                         "one heterogeneous batch per engine, one pass after the workload warmed the engines"}
+                         "one heterogeneous batch per engine; the second of two passes is timed"}
         t = sweep_pass(engines, args.sweep_runs)
         sweep["mixed_runs_per_s"] = args.sweep_runs / t
         log("sweep mixed: %.3f runs/s" % sweep["mixed_runs_per_s"])

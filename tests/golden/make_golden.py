@@ -149,6 +149,10 @@ CASES = [
      dict(eps=-0.3, U=0.6, V=0.12, **{"lambda": 2.0}, nkeep=256, nsites=20, delta=0.001), {}),
     ("ref_twochannel_nk256", "twochannel",
      dict(eps=-0.3, U=0.6, V=0.12, **{"lambda": 4.0}, nkeep=256, nsites=8), {}),
+    # the two-channel workload at its own size (Nkeep=4096, blocks up to ~4300)
+    # over its first sites
+    ("ref_c3_twochannel_nk4096", "twochannel",
+     dict(eps=-0.3, U=0.6, V=0.12, **{"lambda": 4.0}, nkeep=4096, nsites=5), {}),
 ]
 
 

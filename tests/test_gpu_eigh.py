@@ -48,6 +48,33 @@ def test_eigh_batched(gpu_engine, mixed_engine, mode):
         assert np.abs(h @ U - U * w).max() <= 1e-11 * scale * max(1, n) ** 0.5, (mode, n)
 
 
+@pytest.mark.parametrize("mode,n", [("fp64", 1500), ("mixed", 1500), ("mixed", 4300)])
+def test_eigh_large_blocks(gpu_engine, mixed_engine, mode, n):
+    """Blocks of the two-channel workload's size (up to ~4300 rows): the
+    one-CTA reflector solver streaming the matrix from global memory, with
+    its bisection and inverse iteration, in FP64 (no refinement) and FP32
+    followed by the FP64-accurate refinement.  (The plain FP64 path solves
+    blocks above its reflector kernel's limit, about 2880 rows, with tred2 +
+    QL in global memory, minutes per block: not run here.)"""
+    eng = gpu_engine if mode == "fp64" else mixed_engine
+    rng = np.random.default_rng(n)
+    a = rng.standard_normal((n, n))
+    h = 0.5 * (a + a.T)
+    # an NRG-like spectrum: a dense low part and exact pairs
+    d = np.sort(rng.uniform(-2, 6, n // 2))
+    d = np.concatenate([d, d[: n - n // 2]])
+    q, _ = np.linalg.qr(rng.standard_normal((n, n)))
+    g = (q * d) @ q.T
+    g = 0.5 * (g + g.T)
+    for m in (h, g):
+        (w, U), = eng.eigh_batched([m])
+        scale = max(1.0, np.abs(m).max())
+        wr = np.linalg.eigvalsh(m)
+        assert np.abs(w - wr).max() <= 1e-12 * scale * n ** 0.5, (mode, n)
+        assert np.abs(U.T @ U - np.eye(n)).max() <= 1e-12 * n ** 0.5, (mode, n)
+        assert np.abs(m @ U - U * w).max() <= 1e-11 * scale * n ** 0.5, (mode, n)
+
+
 @pytest.mark.parametrize("sizes", [[240, 300, 420], [480, 640], [706]])
 def test_cluster_and_one_cta_solvers_agree(monkeypatch, sizes):
     """The thread-block-cluster solver (blocks above one SM's shared memory;

@@ -4,6 +4,9 @@
   50 sites and at Nkeep=2048 / 40 sites, d-dagger-chi tracked, T=0 FDM
   spectrum, entropy and specific heat, against the reference's own outputs
   (tests/golden/ref_c2_siam_*_nk1024, ref_siam_*_nk2048);
+* the two-channel workload at its own size (Lambda=4, Nkeep=4096, blocks up
+  to 4279 rows), mixed path, over its first five sites, against the
+  reference's run (tests/golden/ref_c3_twochannel_nk4096);
 * instances of the seeded parameter sweep stepped together in one batch
   (different Lambda, Nkeep and lengths), against the reference's outputs for
   each instance (tests/golden/ref_sweep_*), over the sites where the
@@ -110,6 +113,22 @@ def test_superconducting_bath_against_reference(gpu_engine, mixed_engine, path):
     try:
         check_eigs(fx, out["eig"], 2.0)
         for i in range(20):
+            assert np.array_equal(np.array(out["kept"][i]), fx["kept%d" % i]), i
+    finally:
+        out["run"].close()
+
+
+def test_two_channel_workload_nk4096_mixed(mixed_engine):
+    """Blocks of up to 4279 rows (four per site above 4100): the FP32
+    reflector solver streaming them from global memory, then the
+    FP64-accurate refinement.  The plain FP64 path would solve the blocks
+    above its reflector kernel's limit (about 2880 rows) with tred2 + QL in
+    global memory, minutes per block, so it is not run at this size."""
+    fx = golden("ref_c3_twochannel_nk4096")
+    out = workloads.run_nrg(mixed_engine, "twochannel", 4096, 5, 4.0, V=0.12, eps=-0.3, U=0.6)
+    try:
+        check_eigs(fx, out["eig"], 4.0)
+        for i in range(5):
             assert np.array_equal(np.array(out["kept"][i]), fx["kept%d" % i]), i
     finally:
         out["run"].close()

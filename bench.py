@@ -553,8 +553,10 @@ def kernel_models(fp64_peak):
 
 
 # DRAM bytes (read + write) per launch measured with ncu on one engine's
-# batch (mean over its launches; summary and command under profiles/)
-MEASURED_TRAFFIC = {"k_gemm_oz": 221.0e6}
+# 4-run batch of the Nkeep = 2048 workload, cold cache (mean over the
+# batch's launches; profiles/launches_siam_fdm_nk2048_engine.md)
+MEASURED_TRAFFIC = {"k_gemm_oz": 435.5e6, "k_eig_bi_f32": 177.1e6, "k_oa_update": 156.3e6,
+                    "k_reflect": 101.0e6, "k_split": 300.8e6}
 
 
 def kernel_profile(engine, batch=None):
@@ -587,7 +589,7 @@ def roofline_from(kt, wc, fp64_peak):
     top = max(known.items(), key=lambda kv: kv[1][0])
     rf = _roofline(top[0], *top[1], models)
     rf["all"] = {k: {"achieved": round(r["achieved"], 3), "unit": r["unit"], "frac": round(r["frac"], 5),
-                     "bound": r["bound"], "ms": round(v[0], 3)}
+                     "bound": r["bound"], "ms": round(v[0], 3), "traffic": r["traffic"]}
                  for k, v in known.items() for r in [_roofline(k, *v, models)]}
     if "k_gemm_oz" in kt and kt["k_gemm_oz"][0] > 0 and wc.get("tc_useful"):
         ms = kt["k_gemm_oz"][0]

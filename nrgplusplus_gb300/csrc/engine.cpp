@@ -939,6 +939,10 @@ static MixedStatus mixed_eigensolve(nrg_engine *e, std::vector<DevBlock *> &blks
   std::vector<size_t> obt(rplans.size());
   for (size_t p = 0; p < rplans.size(); ++p) obt[p] = a.add(rtiles[p]);
   const size_t orb = a.add(rb);  // filled per step below (host copy re-uploaded)
+  std::vector<int2> strips;      // (block, first row) of the refinement's row-strip passes
+  for (size_t b = 0; b < nb; ++b)
+    for (int r0 = 0; r0 < blks[b]->n; r0 += oa_strip_rows()) strips.push_back(make_int2(int(b), r0));
+  const size_t ostrip = a.add(strips), oflag = a.add(stat);
   const size_t oone = a.add(eb_one), ocl = a.add(eb_cl);
   DevPtr dd;
   char *dp = a.push(e, dd);
@@ -1038,8 +1042,16 @@ static MixedStatus mixed_eigensolve(nrg_engine *e, std::vector<DevBlock *> &blks
     g2.launch(e, hold);
     upload_async(e, dp + orb, rb.data(), nb * sizeof(RefineBlock));
     if (final) {
+      {
+        Prof pf(e, "k_oa_check");
+        launch_oa_check(at<RefineBlock>(dp, orb), at<int2>(dp, ostrip), int(strips.size()), max_n, kClusterTau,
+                        at<int>(dp, oflag), s);
+        count_launch(e);
+        post_launch("refine check");
+      }
       Prof pf(e, "k_oa_final");
-      launch_oa_final(at<RefineBlock>(dp, orb), int(nb), max_n, kClusterTau, at<int>(dp, ost), s);
+      launch_oa_final(at<RefineBlock>(dp, orb), int(nb), max_n, kClusterTau, at<int>(dp, ost),
+                      at<int>(dp, oflag), s);
       count_launch(e);
       post_launch("refine final");
       break;
@@ -1048,7 +1060,7 @@ static MixedStatus mixed_eigensolve(nrg_engine *e, std::vector<DevBlock *> &blks
       double bytes = 0;  // S, G read and E written
       for (size_t b = 0; b < nb; ++b) bytes += 24.0 * blks[b]->n * blks[b]->n;
       Prof pf(e, "k_oa_update", bytes);
-      launch_oa_update(at<RefineBlock>(dp, orb), int(nb), max_n, kClusterTau, s);
+      launch_oa_update(at<RefineBlock>(dp, orb), at<int2>(dp, ostrip), int(strips.size()), max_n, kClusterTau, s);
       count_launch(e);
       post_launch("refine update");
     }

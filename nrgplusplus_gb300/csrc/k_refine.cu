@@ -48,32 +48,101 @@ __device__ double block_max(double v, double *red) {
   return m;
 }
 
-__global__ void __launch_bounds__(kThreads)
-k_oa_update(const RefineBlock *__restrict__ blocks, double tau_rel) {
-  extern __shared__ __align__(16) double sm[];
-  __shared__ double red[kWarps];
-  const RefineBlock B = blocks[blockIdx.x];
+// The element-wise passes over S and G (the Newton correction, the
+// convergence check) run on row strips: one CTA per kStripRows rows of one
+// block, one warp per row and lanes along it, so a large block spreads over
+// many SMs.  Every CTA recomputes the block's Rayleigh quotients
+// lam_i = S_ii / G_ii and tau (n values) in shared memory.
+constexpr int kStripRows = 16;
+constexpr int kStripThreads = 256;
+constexpr int kStripWarps = kStripThreads / 32;
+
+__device__ double strip_max(double v, double *red) {
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double m = red[0];
+  for (int w = 1; w < kStripWarps; ++w) m = fmax(m, red[w]);
+  __syncthreads();
+  return m;
+}
+
+// lam into shared memory; returns tau (0 < tau) and sets *bad when a
+// Rayleigh quotient is not finite
+__device__ double strip_lambdas(const RefineBlock &B, double *lam, double tau_rel, double *red, bool *bad) {
   const int n = B.n;
-  double *lam = sm;
-  double local = 0.0;
-  for (int i = threadIdx.x; i < n; i += kThreads) {
+  double local = 0.0, nf = 0.0;
+  for (int i = threadIdx.x; i < n; i += kStripThreads) {
     const double l = B.S[int64_t(i) * B.ld + i] / B.G[int64_t(i) * B.ld + i];
     lam[i] = l;
     if (isfinite(l)) local = fmax(local, fabs(l));
+    else nf = 1.0;
   }
-  const double tau = tau_rel * fmax(1.0, block_max(local, red));
-  for (int64_t idx = threadIdx.x; idx < int64_t(n) * n; idx += kThreads) {
-    const int i = int(idx / n), j = int(idx - int64_t(i) * n);
-    const double g = sym(B.G, B.ld, i, j);
-    double e;
-    if (i == j) {
-      e = 0.5 * (1.0 - g);
-    } else {
-      const double d = lam[j] - lam[i];
-      e = (fabs(d) > tau) ? (sym(B.S, B.ld, i, j) - lam[j] * g) / d : -0.5 * g;
+  const double m = strip_max(local, red);
+  *bad = strip_max(nf, red) > 0.0;
+  return tau_rel * fmax(1.0, m);
+}
+
+__global__ void __launch_bounds__(kStripThreads)
+k_oa_update(const RefineBlock *__restrict__ blocks, const int2 *__restrict__ tiles, double tau_rel) {
+  extern __shared__ __align__(16) double lam[];
+  __shared__ double red[kStripWarps];
+  const int2 t = tiles[blockIdx.x];
+  const RefineBlock B = blocks[t.x];
+  const int n = B.n;
+  bool nf;
+  const double tau = strip_lambdas(B, lam, tau_rel, red, &nf);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int r1 = min(n, t.y + kStripRows);
+  for (int i = t.y + warp; i < r1; i += kStripWarps) {
+    const double li = lam[i];
+    double *out = B.E2 + int64_t(i) * B.ld;
+    for (int j = lane; j < n; j += 32) {
+      const double g = sym(B.G, B.ld, i, j);
+      double e;
+      if (i == j) {
+        e = 0.5 * (1.0 - g);
+      } else {
+        const double d = lam[j] - li;
+        e = (fabs(d) > tau) ? (sym(B.S, B.ld, i, j) - lam[j] * g) / d : -0.5 * g;
+      }
+      out[j] = e;
     }
-    B.E2[int64_t(i) * B.ld + j] = e;
   }
+}
+
+// Convergence: every entry of the correction one more Newton step would
+// apply (the k_oa_update formulas; within a cluster only the orthogonality
+// part) must be below kConvTol and every Rayleigh quotient finite, otherwise
+// flag[b] = 1 and the block is re-solved in FP64.
+__global__ void __launch_bounds__(kStripThreads)
+k_oa_check(const RefineBlock *__restrict__ blocks, const int2 *__restrict__ tiles, double tau_rel, int *flag) {
+  extern __shared__ __align__(16) double lam[];
+  __shared__ double red[kStripWarps];
+  const int2 t = tiles[blockIdx.x];
+  const RefineBlock B = blocks[t.x];
+  const int n = B.n;
+  bool nf;
+  const double tau = strip_lambdas(B, lam, tau_rel, red, &nf);
+  double bad = nf ? 1.0 : 0.0;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int r1 = min(n, t.y + kStripRows);
+  for (int i = t.y + warp; i < r1 && bad == 0.0; i += kStripWarps) {
+    const double li = lam[i];
+    for (int j = lane; j < n; j += 32) {
+      const double g = sym(B.G, B.ld, i, j);
+      double r;
+      if (i == j) {
+        r = 1.0 - g;
+      } else {
+        const double d = lam[j] - li;
+        r = (fabs(d) > tau) ? (sym(B.S, B.ld, i, j) - lam[j] * g) / d : g;
+      }
+      if (!(fabs(r) <= kConvTol)) bad = 1.0;
+    }
+  }
+  if (strip_max(bad, red) > 0.0 && threadIdx.x == 0) flag[t.x] = 1;
 }
 
 // Final Rayleigh-Ritz pass: eigenvalues, cluster diagonalisation, sorted
@@ -82,12 +151,16 @@ k_oa_update(const RefineBlock *__restrict__ blocks, double tau_rel) {
 // remaining correction above kConvTol) or a cluster exceeds kMaxCluster; the
 // host then re-solves the block in FP64.
 __global__ void __launch_bounds__(kThreads)
-k_oa_final(const RefineBlock *__restrict__ blocks, double tau_rel, int *status) {
+k_oa_final(const RefineBlock *__restrict__ blocks, double tau_rel, int *status, const int *flag) {
   extern __shared__ __align__(16) double sm[];
   __shared__ double red[kWarps];
   __shared__ int ncl, jac_flag;
   const RefineBlock B = blocks[blockIdx.x];
   const int n = B.n;
+  if (flag[blockIdx.x]) {  // k_oa_check: refinement broke down, re-solve in FP64
+    if (threadIdx.x == 0) status[blockIdx.x] = 2;
+    return;
+  }
   double *lam = sm;                                   // n
   double *lams = lam + n;                             // n (sorted)
   double *Sc = lams + n;                              // kMaxCluster^2
@@ -95,34 +168,14 @@ k_oa_final(const RefineBlock *__restrict__ blocks, double tau_rel, int *status) 
   int *perm = reinterpret_cast<int *>(Qc + kMaxCluster * kMaxCluster);  // n
   int *cl = perm + n;                                 // up to n/2 + 1 cluster starts/ends
   int *order = cl + n + 2;                            // kMaxCluster
-  double local = 0.0, bad = 0.0;
+  double local = 0.0;
   for (int i = threadIdx.x; i < n; i += kThreads) {
     const double l = B.S[int64_t(i) * B.ld + i] / B.G[int64_t(i) * B.ld + i];
     lam[i] = l;
     local = fmax(local, fabs(l));
-    if (!isfinite(l)) bad = 1.0;
   }
   const double tau = tau_rel * fmax(1.0, block_max(local, red));
   __syncthreads();  // lam complete
-  // convergence: every entry of the correction one more Newton step would
-  // apply (the k_oa_update formulas; within a cluster only the orthogonality
-  // part) must be below kConvTol, otherwise the block is re-solved in FP64
-  for (int64_t idx = threadIdx.x; idx < int64_t(n) * n && bad == 0.0; idx += kThreads) {
-    const int i = int(idx / n), j = int(idx - int64_t(i) * n);
-    const double g = sym(B.G, B.ld, i, j);
-    double r;
-    if (i == j) {
-      r = 1.0 - g;
-    } else {
-      const double d = lam[j] - lam[i];
-      r = (fabs(d) > tau) ? (sym(B.S, B.ld, i, j) - lam[j] * g) / d : g;
-    }
-    if (!(fabs(r) <= kConvTol)) bad = 1.0;
-  }
-  if (block_max(bad, red) > 0.0) {  // refinement broke down: re-solve in FP64
-    if (threadIdx.x == 0) status[blockIdx.x] = 2;
-    return;
-  }
   for (int i = threadIdx.x; i < n; i += kThreads) {
     const double x = lam[i];
     int r = 0;
@@ -151,9 +204,10 @@ k_oa_final(const RefineBlock *__restrict__ blocks, double tau_rel, int *status) 
   __syncthreads();
   // plain columns: U[:, k] = X[:, perm[k]], E[k] = lams[k]
   for (int k = threadIdx.x; k < n; k += kThreads) B.Eout[k] = lams[k];
-  for (int64_t idx = threadIdx.x; idx < int64_t(n) * n; idx += kThreads) {
-    const int r = int(idx / n), k = int(idx - int64_t(r) * n);
-    B.U[int64_t(r) * B.ldu + k] = B.X[int64_t(r) * B.ld + perm[k]];
+  {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int r = warp; r < n; r += kWarps)
+      for (int k = lane; k < n; k += 32) B.U[int64_t(r) * B.ldu + k] = B.X[int64_t(r) * B.ld + perm[k]];
   }
   __syncthreads();
   for (int q = 0; q < ncl; ++q) {
@@ -242,18 +296,27 @@ int refine_max_n() {
   return n;
 }
 
-void launch_oa_update(const RefineBlock *blocks, int nblocks, int max_n, double tau_rel,
+void launch_oa_update(const RefineBlock *blocks, const int2 *tiles, int ntiles, int max_n, double tau_rel,
                       cudaStream_t s) {
-  if (nblocks == 0) return;
+  if (ntiles == 0) return;
   ensure_smem_limit(reinterpret_cast<const void *>(k_oa_update), 225 * 1024);
-  k_oa_update<<<nblocks, kThreads, sizeof(double) * size_t(max_n) + 16, s>>>(blocks, tau_rel);
+  k_oa_update<<<ntiles, kStripThreads, sizeof(double) * size_t(max_n) + 16, s>>>(blocks, tiles, tau_rel);
 }
 
+void launch_oa_check(const RefineBlock *blocks, const int2 *tiles, int ntiles, int max_n, double tau_rel,
+                     int *flag, cudaStream_t s) {
+  if (ntiles == 0) return;
+  ensure_smem_limit(reinterpret_cast<const void *>(k_oa_check), 225 * 1024);
+  k_oa_check<<<ntiles, kStripThreads, sizeof(double) * size_t(max_n) + 16, s>>>(blocks, tiles, tau_rel, flag);
+}
+
+int oa_strip_rows() { return kStripRows; }
+
 void launch_oa_final(const RefineBlock *blocks, int nblocks, int max_n, double tau_rel, int *status,
-                     cudaStream_t s) {
+                     const int *flag, cudaStream_t s) {
   if (nblocks == 0) return;
   ensure_smem_limit(reinterpret_cast<const void *>(k_oa_final), 225 * 1024);
-  k_oa_final<<<nblocks, kThreads, final_smem(max_n), s>>>(blocks, tau_rel, status);
+  k_oa_final<<<nblocks, kThreads, final_smem(max_n), s>>>(blocks, tau_rel, status, flag);
 }
 
 }  // namespace nrg

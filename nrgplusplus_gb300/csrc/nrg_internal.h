@@ -113,12 +113,20 @@ struct RefineBlock {
   double *Eout;         // final eigenvalues, ascending
   int n, ld, ldu, pad;
 };
-void launch_oa_update(const RefineBlock *blocks, int nblocks, int max_n, double tau_rel,
+// The element-wise passes run on row strips: tiles = (block, first row), one
+// per oa_strip_rows() rows of each block.
+int oa_strip_rows();
+void launch_oa_update(const RefineBlock *blocks, const int2 *tiles, int ntiles, int max_n, double tau_rel,
                       cudaStream_t s);
-// status[b] = 2: a near-degenerate cluster is too large for the in-kernel
-// Jacobi; the host re-solves that block with the FP64 solver.
+// flag[b] = 1 (zeroed by the caller): the refinement of block b has not
+// converged or a Rayleigh quotient is not finite.
+void launch_oa_check(const RefineBlock *blocks, const int2 *tiles, int ntiles, int max_n, double tau_rel,
+                     int *flag, cudaStream_t s);
+// status[b] = 2: flagged by launch_oa_check, or a near-degenerate cluster
+// too large for the in-kernel Jacobi; the block is re-solved with the FP64
+// solver.
 void launch_oa_final(const RefineBlock *blocks, int nblocks, int max_n, double tau_rel, int *status,
-                     cudaStream_t s);
+                     const int *flag, cudaStream_t s);
 int refine_max_n();
 
 // ----------------------------------------------------------- grouped GEMM

@@ -339,137 +339,8 @@ __device__ void fused_rows(T *a, int lda, int jn, int ncol, const T *u, const T 
   }
 }
 
-// 8-byte cp.async (global -> shared through L1: the rows are written back by
-// this CTA's own stores, ordered before the next step's loads by the step's
-// CTA barriers)
-__device__ __forceinline__ void cp_async8(void *sdst, const void *gsrc) {
-  const unsigned sa = static_cast<unsigned>(__cvta_generic_to_shared(sdst));
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gsrc) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-template <int N> __device__ __forceinline__ void cp_async_wait() {
-  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
-}
-
-constexpr int kPipe = 3;  // stages of a warp's ring
-
-// The streaming pass of tred2_fused for a matrix in global memory (even
-// lda): a warp's rows (four at a time, j0 = warp + 64 g + 16 r) go through
-// the warp's ring of kPipe shared-memory stages, each 4 rows x cwu 8-byte
-// units (a unit: two FP32 or one FP64 value), filled by cp.async kPipe - 1
-// tiles ahead, so every lane keeps its next tiles' loads in flight while it
-// updates the current one; updated values go straight back to global
-// memory.  begin() issues the first tiles (before the step's row-i work, so
-// their latency overlaps it); run() consumes them.  No CTA barrier inside.
-template <typename T>
-struct RowStream {
-  static constexpr int EPU = 8 / int(sizeof(T));  // elements per unit
-  T *a;
-  int lda, jn, nunit, cwu, nk, ntile;
-  T *ring;  // this warp's kPipe x 4 x cwu units
-
-  __device__ RowStream(T *a_, int lda_, int jn_, int ncol, T *ring_base, int cwu_) : a(a_), lda(lda_), jn(jn_) {
-    const int warp = threadIdx.x >> 5;
-    cwu = cwu_;
-    nunit = (ncol + EPU - 1) / EPU;
-    nk = (nunit + cwu - 1) / cwu;
-    const int ng = warp < jn ? (jn - warp + 63) / 64 : 0;
-    ntile = ng * nk;
-    ring = ring_base + size_t(warp) * kPipe * 4 * cwu * EPU;
-  }
-  __device__ void issue(int t) {
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    if (t < ntile) {
-      const int g = t / nk, k = t - g * nk;
-      T *st = ring + size_t(t % kPipe) * 4 * cwu * EPU;
-#pragma unroll
-      for (int r = 0; r < 4; ++r) {
-        const int j = warp + 64 * g + 16 * r;
-        if (j >= jn) continue;
-        const T *src = a + int64_t(j) * lda;
-        for (int x = lane; x < cwu; x += 32) {
-          const int cu = k * cwu + x;
-          if (cu < nunit) cp_async8(st + (r * cwu + x) * EPU, src + cu * EPU);
-        }
-      }
-    }
-    cp_async_commit();  // one group per tile slot, empty past the end
-  }
-  __device__ void begin() {
-#pragma unroll
-    for (int t = 0; t < kPipe - 1; ++t) issue(t);
-  }
-  template <bool UPD, bool DOT>
-  __device__ void run(const T *u, const T *q, const T *un, T *pn, T hn) {
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    T uj[4], qj[4], sd[4];
-    bool ok[4];
-    for (int t = 0; t < ntile; ++t) {
-      issue(t + kPipe - 1);
-      cp_async_wait<kPipe - 1>();
-      __syncwarp();
-      const int g = t / nk, k = t - g * nk;
-      if (k == 0) {
-#pragma unroll
-        for (int r = 0; r < 4; ++r) {
-          const int j = warp + 64 * g + 16 * r;
-          ok[r] = j < jn;
-          uj[r] = (UPD && ok[r]) ? u[j] : T(0);
-          qj[r] = (UPD && ok[r]) ? q[j] : T(0);
-          sd[r] = T(0);
-        }
-      }
-      const T *st = ring + size_t(t % kPipe) * 4 * cwu * EPU;
-      for (int x = lane; x < cwu; x += 32) {
-        const int cu = k * cwu + x;
-        if (cu >= nunit) break;
-        if constexpr (EPU == 2) {
-          const float2 uu = reinterpret_cast<const float2 *>(u)[cu], qq = reinterpret_cast<const float2 *>(q)[cu];
-          const float2 w = DOT ? reinterpret_cast<const float2 *>(un)[cu] : make_float2(0.f, 0.f);
-#pragma unroll
-          for (int r = 0; r < 4; ++r) {
-            if (!ok[r]) continue;
-            float2 v = reinterpret_cast<const float2 *>(st)[r * cwu + x];
-            if constexpr (UPD) {
-              v.x -= uj[r] * qq.x + qj[r] * uu.x;
-              v.y -= uj[r] * qq.y + qj[r] * uu.y;
-              reinterpret_cast<float2 *>(a + int64_t(warp + 64 * g + 16 * r) * lda)[cu] = v;
-            }
-            if constexpr (DOT) sd[r] = fmaf(v.x, w.x, fmaf(v.y, w.y, sd[r]));
-          }
-        } else {
-          const T uu = u[cu], qq = q[cu], w = DOT ? un[cu] : T(0);
-#pragma unroll
-          for (int r = 0; r < 4; ++r) {
-            if (!ok[r]) continue;
-            T v = st[r * cwu + x];
-            if constexpr (UPD) {
-              v -= uj[r] * qq + qj[r] * uu;
-              a[int64_t(warp + 64 * g + 16 * r) * lda + cu] = v;
-            }
-            if constexpr (DOT) sd[r] += v * w;
-          }
-        }
-      }
-      __syncwarp();  // the stage is refilled by the next iteration's issue
-      if (DOT && k == nk - 1) {
-#pragma unroll
-        for (int r = 0; r < 4; ++r) sd[r] = warp_sum(sd[r]);
-        if (lane == 0)
-#pragma unroll
-          for (int r = 0; r < 4; ++r)
-            if (ok[r]) pn[warp + 64 * g + 16 * r] = sd[r] / hn;
-      }
-    }
-    cp_async_wait<0>();  // the empty tail groups
-  }
-};
-
-// ring: kWarps rings of kPipe x 4 x cwu units for the streaming form (wide
-// with cwu > 0); cwu = 0 streams without the ring (fused_rows).
 template <typename T, bool WIDE>
-__device__ void tred2_fused(T *a, int lda, int n, T *d, T *e, T *ua, T *pa, T *ub, T *pb, T *red,
-                            T *ring = nullptr, int cwu = 0) {
+__device__ void tred2_fused(T *a, int lda, int n, T *d, T *e, T *ua, T *pa, T *ub, T *pb, T *red) {
   const int tid = threadIdx.x;
   T *u = ua, *q = pa, *un = ub, *pn = pb;
   bool pending = false;
@@ -480,8 +351,6 @@ __device__ void tred2_fused(T *a, int lda, int n, T *d, T *e, T *ua, T *pa, T *u
     // wide form the last pair may reach one column further, which u, q and
     // un hold at zero there
     const int ncol = pending ? i + 1 : l + 1;
-    RowStream<T> rs(a, lda, i, ncol, ring, cwu > 0 ? cwu : 32);
-    if (WIDE && cwu > 0) rs.begin();  // rows 0..l, written by the previous step before its last barrier
     // row i (the next reflector): the pending update, staged in un, and its
     // |.| sum over columns 0..l
     T scale = T(0);
@@ -502,12 +371,7 @@ __device__ void tred2_fused(T *a, int lda, int n, T *d, T *e, T *ua, T *pa, T *u
     scale = block_sum(scale, red);
     if (l == 0 || scale == T(0)) {
       if (tid == 0) { e[i] = un[l]; d[i] = T(0); }
-      if (WIDE && cwu > 0) {
-        if (pending) rs.template run<true, false>(u, q, nullptr, nullptr, T(1));
-        else cp_async_wait<0>();
-      } else if (pending) {
-        fused_rows<T, WIDE, true, false>(a, lda, i, ncol, u, q, nullptr, nullptr, T(1));
-      }
+      if (pending) fused_rows<T, WIDE, true, false>(a, lda, i, ncol, u, q, nullptr, nullptr, T(1));
       __syncthreads();
       pending = false;
       continue;
@@ -538,13 +402,8 @@ __device__ void tred2_fused(T *a, int lda, int n, T *d, T *e, T *ua, T *pa, T *u
     __syncthreads();
     h = red[kWarps];
     __syncthreads();
-    if (WIDE && cwu > 0) {
-      if (pending) rs.template run<true, true>(u, q, un, pn, h);
-      else rs.template run<false, true>(u, q, un, pn, h);
-    } else {
-      if (pending) fused_rows<T, WIDE, true, true>(a, lda, i, ncol, u, q, un, pn, h);
-      else fused_rows<T, WIDE, false, true>(a, lda, i, ncol, u, q, un, pn, h);
-    }
+    if (pending) fused_rows<T, WIDE, true, true>(a, lda, i, ncol, u, q, un, pn, h);
+    else fused_rows<T, WIDE, false, true>(a, lda, i, ncol, u, q, un, pn, h);
     __syncthreads();
     T fs = T(0);
     for (int j = tid; j <= l; j += kThreads) fs += pn[j] * un[j];
@@ -932,17 +791,8 @@ k_eig_bi(const EigBlock *__restrict__ blocks, int max_n_smem, int smem_total) {
     a[int64_t(r) * lda + c] = T(B.H[int64_t(r) * B.ld + c]);
   }
   __syncthreads();
-  if (!in_smem && lda % 2 == 0) {
-    // the widest ring (units of 8 bytes per row per tile) that fits beside
-    // the vectors; none: stream without it
-    const size_t avail = size_t(smem_total) - size_t(scratch - smem);
-    int cwu = 128;
-    while (cwu >= 32 && size_t(kWarps) * kPipe * 4 * cwu * 8 > avail) cwu /= 2;
-    if (cwu < 32) cwu = 0;
-    tred2_fused<T, true>(a, lda, n, d, e, u, p, ub, pb, red, reinterpret_cast<T *>(scratch), cwu);
-  } else {
-    tred2_fused<T, false>(a, lda, n, d, e, u, p, ub, pb, red);
-  }
+  if (!in_smem && lda % 2 == 0) tred2_fused<T, true>(a, lda, n, d, e, u, p, ub, pb, red);
+  else tred2_fused<T, false>(a, lda, n, d, e, u, p, ub, pb, red);
   // T's diagonal into d; h_i (0: no reflector) onto the diagonal of the
   // reflector matrix, which k_reflect reads from the block's W buffer
   for (int i = threadIdx.x; i < n; i += kThreads) {

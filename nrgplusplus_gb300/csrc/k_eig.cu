@@ -17,6 +17,12 @@
 // The matrix lives in shared memory when it fits, otherwise in the block's
 // own global buffer (L2 resident).  The QL sweep count per eigenvalue is
 // capped; a block that hits the cap sets status[b] = 1 and stops.
+// Published algorithms restated here: the Householder tridiagonalisation and
+// implicit QL of EISPACK's tred2 / tql2 (Martin, Reinsch and Wilkinson, Numer.
+// Math. 11 (1968) 181; Bowdler, Martin, Reinsch and Wilkinson, Numer. Math. 11
+// (1968) 293); Sturm-sequence bisection (Barth, Martin and Wilkinson, Numer.
+// Math. 9 (1967) 386); inverse iteration with re-orthogonalisation of close
+// eigenvalues (Peters and Wilkinson, Linear Algebra (Handbook II/18), 1971).
 #include "eig_tri.cuh"
 #include "nrg_internal.h"
 

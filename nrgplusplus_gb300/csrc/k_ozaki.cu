@@ -188,24 +188,27 @@ constexpr int kConsumers = 256;
 constexpr int kATile = TM * TK * 2, kBTile = TN * TK * 2;  // bytes per plane
 constexpr int kAStage = kPlanes * kATile;                  // 32 KB
 constexpr int kStageBytes = kPlanes * (kATile + kBTile);   // 48 KB
-constexpr int kOctetBox = kPlanes * TK * 16;               // 2 KB: 8 planes x 16 k x 8 elements
+constexpr int kChunkBox = kPlanes * TK * 32;               // 4 KB: 8 planes x 16 k x 16 elements
 constexpr int kWaitLimit = 1 << 24;                        // bounded mbarrier polls
 
-// Stage layouts.  Every operand tile of a stage is written by TMA boxes (no
-// swizzle) straight into canonical core-matrix layouts (8 rows of 16 bytes
-// each, contiguous):
-//   K-major (rows of k):  two boxes {8 k, R rows, 8 planes}, one per k-half:
-//     [k-half][plane][row][8 k]; plane p at p * R * 16, row groups 128 bytes
-//     apart (SBO), k-halves R * 16 * 8 bytes apart (LBO);
-//   MN-major (rows of m or n): R / 8 boxes {8 m, 16 k, 8 planes}, one per
-//     m-octet: [octet][plane][k][8 m]; plane p at p * 256, k-groups 128
-//     bytes apart (LBO), octets 2 KB apart (SBO).
+// Stage layouts.  Every operand tile of a stage is written by TMA boxes with
+// the 32-byte swizzle straight into the canonical 32-byte-swizzled layouts
+// (rows of 32 bytes, the two 16-byte halves of a row exchanged in every
+// other group of four rows; atoms of 8 rows = 256 bytes, 256-byte aligned):
+//   K-major (rows of m or n, 16 k each):  one box {16 k, R rows, 8 planes}:
+//     [plane][row][16 k]; plane p at p * R * 32, 8-row groups 256 bytes apart
+//     (SBO; the k extent is one atom wide, LBO unused);
+//   MN-major (rows of k, 16 m or n each): R / 16 boxes {16 m, 16 k, 8 planes},
+//     one per 16-wide chunk: [chunk][plane][k][16 m]; plane p at p * 512,
+//     8-k groups 256 bytes apart (SBO), chunks 4 KB apart (LBO).
+// A box row is 32 bytes (16-byte rows halve the TMA unit's throughput).
 // The boxes of a stage always total kStageBytes (rows, k and planes beyond
 // the operand view are zero-filled by the TMA unit), which the producer
 // announces with one expect_tx on the stage's full barrier.
 __device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
   return uint64_t((addr >> 4) & 0x3FFF) | (uint64_t((lbo >> 4) & 0x3FFF) << 16) |
-         (uint64_t((sbo >> 4) & 0x3FFF) << 32) | (uint64_t(1) << 46);  // version 1; no swizzle
+         (uint64_t((sbo >> 4) & 0x3FFF) << 32) | (uint64_t(1) << 46) |  // version 1
+         (uint64_t(6) << 61);                                            // 32-byte swizzle
 }
 
 __device__ __forceinline__ void tma_load_3d(uint32_t dst, const OzTensorMap *map, int x, int y, int z, uint32_t bar) {
@@ -230,24 +233,22 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
 
 // The boxes of the k-step [k0, k0 + 16) of all 8 planes of op(A) (128 x 16)
 // and op(B) (64 x 16) into stage `st` (shared address), completing on `bar`.
-// x coordinates (k0, k0 + 8, m0 + 8 o, n0 + 8 o) are multiples of 8
-// elements: 16-byte aligned, as TMA requires.
+// x coordinates (k0, m0 + 16 o, n0 + 16 o) are multiples of 16 elements:
+// 32-byte aligned (TMA needs 16).
 __device__ __forceinline__ void stage_tma(const OzContrib &q, const OzTensorMap *maps, int m0, int n0, int k0,
                                           uint32_t st, uint32_t bar) {
   const bool ta = q.trans & 1, tb = (q.trans >> 1) & 1;
   const OzTensorMap *ma = maps + q.tmA, *mb = maps + q.tmB;
   if (!ta) {
     tma_load_3d(st, ma, k0, m0, 0, bar);
-    tma_load_3d(st + kAStage / 2, ma, k0 + 8, m0, 0, bar);
   } else {
-    for (int o = 0; o < TM / 8; ++o) tma_load_3d(st + o * kOctetBox, ma, m0 + 8 * o, k0, 0, bar);
+    for (int o = 0; o < TM / 16; ++o) tma_load_3d(st + o * kChunkBox, ma, m0 + 16 * o, k0, 0, bar);
   }
   const uint32_t sb = st + kAStage;
   if (tb) {
     tma_load_3d(sb, mb, k0, n0, 0, bar);
-    tma_load_3d(sb + (kStageBytes - kAStage) / 2, mb, k0 + 8, n0, 0, bar);
   } else {
-    for (int o = 0; o < TN / 8; ++o) tma_load_3d(sb + o * kOctetBox, mb, n0 + 8 * o, k0, 0, bar);
+    for (int o = 0; o < TN / 16; ++o) tma_load_3d(sb + o * kChunkBox, mb, n0 + 16 * o, k0, 0, bar);
   }
 }
 
@@ -440,9 +441,9 @@ k_gemm_oz(const GemmTile *__restrict__ tiles, const OzGroup *__restrict__ groups
           const uint32_t sa = ring0 + uint32_t(st * kStageBytes), sb = sa + kAStage;
           // plane p of A at a0 + p * astep, plane q of B at b0 + q * bstep
           // (the stage layouts above)
-          const uint64_t a0 = ta ? smem_desc(sa, 128, kOctetBox) : smem_desc(sa, kAStage / 2, 128);
-          const uint64_t b0 = tb ? smem_desc(sb, (kStageBytes - kAStage) / 2, 128) : smem_desc(sb, 128, kOctetBox);
-          const uint32_t astep = ta ? 256 : TM * 16, bstep = tb ? TN * 16 : 256;
+          const uint64_t a0 = ta ? smem_desc(sa, kChunkBox, 256) : smem_desc(sa, 16, 256);
+          const uint64_t b0 = tb ? smem_desc(sb, 16, 256) : smem_desc(sb, kChunkBox, 256);
+          const uint32_t astep = ta ? TK * 32 : TM * 32, bstep = tb ? TN * 32 : TK * 32;
           const uint32_t first = kacc == 0 ? 0u : 1u;
 #pragma unroll
           for (int p = 0; p < kPlanes; ++p) {
@@ -520,14 +521,14 @@ bool encode_oz_map(OzTensorMap *out, const OzOperand &o, int inner, int outer, i
   static_assert(sizeof(CUtensorMap) == sizeof(OzTensorMap), "tensor map size");
   if (!enc || inner <= 0 || outer <= 0 || planes <= 0 || planes > kPlanes) return false;
   const cuuint64_t strides[2] = {cuuint64_t(o.ld) * 2, cuuint64_t(o.pstride) * 2};
-  const cuuint32_t box[3] = {8, cuuint32_t(box_outer), cuuint32_t(kPlanes)}, es[3] = {1, 1, 1};
+  const cuuint32_t box[3] = {16, cuuint32_t(box_outer), cuuint32_t(kPlanes)}, es[3] = {1, 1, 1};
   // planes beyond `planes` are zero-filled (no bytes read) when the driver
   // takes a box deeper than the tensor; otherwise all 8 (always allocated)
   for (const int np : {planes, kPlanes}) {
     const cuuint64_t dims[3] = {cuuint64_t(inner), cuuint64_t(outer), cuuint64_t(np)};
     if (enc(reinterpret_cast<CUtensorMap *>(out), CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3,
             const_cast<__nv_bfloat16 *>(o.p), dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
-            CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+            CU_TENSOR_MAP_SWIZZLE_32B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS)
       return true;
   }

@@ -996,13 +996,22 @@ static MixedStatus mixed_eigensolve(nrg_engine *e, std::vector<DevBlock *> &blks
     pH = split_matrices(e, hm, hold);
   }
   auto splitv = [&](PlaneBuf &pl, double *base) { pl = split_blocks(e, base, off, dims, lds, hold); };
-  for (int step = 0; step <= kRefineSteps; ++step) {
-    const bool final = (step == kRefineSteps);
+  // Newton steps per block: the FP32 start's error grows with n (about
+  // sqrt(n) eps32 |H| / gap) and each step squares it, so blocks above 1536
+  // rows take one more step and above 3072 two more; a block whose steps are
+  // done sits out the later ones until the final pass
+  auto steps_of = [](int n) { return kRefineSteps + (n > 1536 ? 1 : 0) + (n > 3072 ? 1 : 0); };
+  int max_steps = 0;
+  for (size_t b = 0; b < nb; ++b) max_steps = std::max(max_steps, steps_of(blks[b]->n));
+  for (int step = 0; step <= max_steps; ++step) {
+    const bool final = (step == max_steps);
+    auto active = [&](size_t b) { return final || step < steps_of(blks[b]->n); };
     if (oz) {
       splitv(pX, X[cur]);
       OzList y;
       y.planes = step == 0 ? kFirstStepPlanes : kDigitPlanes;
       for (size_t b = 0; b < nb; ++b) {  // Y = H X
+        if (!active(b)) continue;
         const int n = blks[b]->n;
         y.out(P(my, off[b]), lds[b], n, n, false, {ozc(pH.op(b), pX.op(b), n, 0)});
       }
@@ -1011,6 +1020,7 @@ static MixedStatus mixed_eigensolve(nrg_engine *e, std::vector<DevBlock *> &blks
       OzList sg;
       sg.planes = y.planes;
       for (size_t b = 0; b < nb; ++b) {  // S = X^T Y, G = X^T X
+        if (!active(b)) continue;
         const int n = blks[b]->n;
         // symmetric: only the tiles that meet the upper triangle (the refinement
         // kernels read S and G there)
@@ -1023,7 +1033,7 @@ static MixedStatus mixed_eigensolve(nrg_engine *e, std::vector<DevBlock *> &blks
     for (size_t b = 0; b < nb; ++b) {
       const int n = blks[b]->n, ld = blks[b]->ld;
       double *x = X[cur] + off[b];
-      if (!oz) {
+      if (!oz && active(b)) {
         g1.out(P(my, off[b]), ld, n, n, false, {contrib(blks[b]->H, ld, x, ld, n, 0)});     // Y = H X
         g2.out(P(ms, off[b]), ld, n, n, false, {contrib(x, ld, P(my, off[b]), ld, n, 1)});  // S = X^T Y
         g2.out(P(mg, off[b]), ld, n, n, false, {contrib(x, ld, x, ld, n, 1)});              // G = X^T X
@@ -1071,6 +1081,7 @@ static MixedStatus mixed_eigensolve(nrg_engine *e, std::vector<DevBlock *> &blks
       OzList g3;
       g3.planes = step == 0 ? kFirstStepPlanes : kDigitPlanes;
       for (size_t b = 0; b < nb; ++b) {
+        if (!active(b)) continue;
         const int n = blks[b]->n;
         g3.out(X[1 - cur] + off[b], lds[b], n, n, true, {ozc(pX.op(b), pE.op(b), n, 0)});
       }
@@ -1078,6 +1089,7 @@ static MixedStatus mixed_eigensolve(nrg_engine *e, std::vector<DevBlock *> &blks
     } else {
       GemmList g3;
       for (size_t b = 0; b < nb; ++b) {
+        if (!active(b)) continue;
         const int n = blks[b]->n, ld = blks[b]->ld;
         g3.out(X[1 - cur] + off[b], ld, n, n, true, {contrib(X[cur] + off[b], ld, P(me2, off[b]), ld, n, 0)});
       }

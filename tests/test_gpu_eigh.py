@@ -53,7 +53,8 @@ def test_eigh_large_blocks(gpu_engine, mixed_engine, mode, n):
     """Blocks of the two-channel workload's size (up to ~4300 rows): the
     one-CTA reflector solver streaming the matrix from global memory, with
     its bisection and inverse iteration, in FP64 (no refinement) and FP32
-    followed by the FP64-accurate refinement.  (The plain FP64 path solves
+    followed by the FP64-accurate refinement (one or two extra Newton steps
+    above 1536 / 3072 rows, no FP64 re-solve).  (The plain FP64 path solves
     blocks above its reflector kernel's limit, about 2880 rows, with tred2 +
     QL in global memory, minutes per block: not run here.)"""
     eng = gpu_engine if mode == "fp64" else mixed_engine
@@ -66,6 +67,7 @@ def test_eigh_large_blocks(gpu_engine, mixed_engine, mode, n):
     q, _ = np.linalg.qr(rng.standard_normal((n, n)))
     g = (q * d) @ q.T
     g = 0.5 * (g + g.T)
+    before = eng.fallback_count()
     for m in (h, g):
         (w, U), = eng.eigh_batched([m])
         scale = max(1.0, np.abs(m).max())
@@ -73,6 +75,8 @@ def test_eigh_large_blocks(gpu_engine, mixed_engine, mode, n):
         assert np.abs(w - wr).max() <= 1e-12 * scale * n ** 0.5, (mode, n)
         assert np.abs(U.T @ U - np.eye(n)).max() <= 1e-12 * n ** 0.5, (mode, n)
         assert np.abs(m @ U - U * w).max() <= 1e-11 * scale * n ** 0.5, (mode, n)
+    # the mixed path refined these blocks itself (no FP64 re-solve)
+    assert eng.fallback_count() == before, (mode, n)
 
 
 @pytest.mark.parametrize("sizes", [[240, 300, 420], [480, 640], [706]])

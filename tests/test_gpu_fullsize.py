@@ -125,10 +125,12 @@ def test_two_channel_workload_nk4096_mixed(mixed_engine):
     above its reflector kernel's limit (about 2880 rows) with tred2 + QL in
     global memory, minutes per block, so it is not run at this size."""
     fx = golden("ref_c3_twochannel_nk4096")
+    before = mixed_engine.fallback_count()
     out = workloads.run_nrg(mixed_engine, "twochannel", 4096, 5, 4.0, V=0.12, eps=-0.3, U=0.6)
     try:
         check_eigs(fx, out["eig"], 4.0)
         for i in range(5):
             assert np.array_equal(np.array(out["kept"][i]), fx["kept%d" % i]), i
+        assert mixed_engine.fallback_count() == before  # refined, not re-solved in FP64
     finally:
         out["run"].close()

@@ -140,48 +140,63 @@ def serving_run(engine, rate, n, seed=2024, max_active=None, workers=None):
             "arrivals": "Poisson, seeded; every request the full workload run (FDM + thermodynamics)"}
 
 
-def serving_mix_run(engine, rate, n, seed=None, max_active=None, workers=None, budget=160 * 10 ** 9):
-    """The serving mix: n seeded requests (60 % SIAM, 25 % Kondo, 15 %
-    two-channel RG flows; workloads.serving_mix) arriving as a seeded Poisson
-    stream at `rate` per second into a server with an HBM admission budget
-    of `budget` bytes."""
+def serving_mix_run(engine, n, seed=None, max_active=None, workers=None, budget=160 * 10 ** 9, load=0.8):
+    """The serving mix: 2 n seeded requests (60 % SIAM, 25 % Kondo, 15 %
+    two-channel RG flows; workloads.serving_mix) into a server with an HBM
+    admission budget of `budget` bytes, in two phases on fresh servers:
+    the first n submitted at once give the mix's capacity (runs/s); the
+    next n arrive as a seeded Poisson stream at `load` x that capacity, and
+    their latencies are reported (an arrival rate above the capacity would
+    measure queueing, not serving)."""
     import threading
     import numpy as np
     from nrgplusplus_gb300 import api, workloads
     seed = workloads.SERVING_SEED if seed is None else seed
     max_active = BATCH if max_active is None else max_active
     workers = ENGINES if workers is None else workers
-    mix = workloads.serving_mix(n, seed)
+    mix = workloads.serving_mix(2 * n, seed)
     reqs = [workloads.mix_request(p) for p in mix]
+
+    def phase(rs, gaps):
+        srv = api.Server(engine, max_active=max_active, workers=workers, hbm_budget_bytes=budget)
+        ids = []
+
+        def arrivals():
+            for g, r in zip(gaps, rs):
+                if g > 0:
+                    time.sleep(float(g))
+                ids.append(srv.submit(**r))
+
+        t0 = time.perf_counter()
+        th = threading.Thread(target=arrivals)
+        th.start()
+        th.join()
+        for i in ids:
+            srv.wait(i, 3600.0)
+            srv.result(i)
+        wall = time.perf_counter() - t0
+        st = srv.stats()
+        srv.close()
+        return st, wall
+
+    st1, w1 = phase(reqs[:n], [0.0] * n)
+    capacity = st1["completed"] / w1
+    rate = load * capacity
     gaps = np.random.default_rng(seed + 1).exponential(1.0 / rate, size=n)
-    srv = api.Server(engine, max_active=max_active, workers=workers, hbm_budget_bytes=budget)
-    ids = []
-
-    def arrivals():
-        for g, r in zip(gaps, reqs):
-            time.sleep(float(g))
-            ids.append(srv.submit(**r))
-
-    t0 = time.perf_counter()
-    th = threading.Thread(target=arrivals)
-    th.start()
-    th.join()
-    for i in ids:
-        srv.wait(i, 3600.0)
-        srv.result(i)
-    wall = time.perf_counter() - t0
-    st = srv.stats()
-    srv.close()
+    st, wall = phase(reqs[n:], gaps)
     fam = {}
     for p in mix:
         fam.setdefault(p["kind"], []).append(p["nkeep"])
-    return {"requests": n, "arrival_rate_per_s": rate, "seed": seed, "hbm_budget_bytes": budget,
+    return {"requests": n, "capacity_runs_per_s": capacity, "capacity_requests": n, "arrival_rate_per_s": rate,
+            "load": load, "seed": seed, "hbm_budget_bytes": budget,
             "max_active_per_worker": max_active, "workers": workers,
             "families": {k: {"count": len(v), "nkeep": sorted(set(v))} for k, v in fam.items()},
             "runs_per_s": st["completed"] / wall, "p50_latency_s": st["p50_latency_s"],
             "p99_latency_s": st["p99_latency_s"], "mean_latency_s": st["mean_latency_s"],
-            "max_active_seen": int(st["max_active_seen"]), "failed": int(st["failed"]),
-            "what": "RG flows (all eigenvalues per site) of the seeded mix, 30-50 sites each"}
+            "max_active_seen": int(st["max_active_seen"]), "failed": int(st["failed"]) + int(st1["failed"]),
+            "what": "RG flows (all eigenvalues per site) of the seeded mix, 30-50 sites each: capacity from "
+                    "the first requests submitted at once, latencies of the next ones arriving at `load` "
+                    "x capacity"}
 
 
 def _dist():
@@ -506,13 +521,26 @@ def _measured(key, fallback):
         return fallback, "of fallback (%s)" % key
 
 
-def measure_fp64_peak():
+def measure_fp32_peak():
+    """FP32 (CUDA-core) peak of this GPU: cuBLAS SGEMM 8192^3 with TF32 off,
+    measured like measure_fp64_peak."""
+    import torch
+    old = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = False
+    try:
+        return measure_fp64_peak(torch.float32)
+    finally:
+        torch.backends.cuda.matmul.allow_tf32 = old
+
+
+def measure_fp64_peak(dtype=None):
     """FP64 peak of this GPU: cuBLAS DGEMM 8192^3 through torch.matmul, best
     of 5 after 2 warm-ups, CUDA events on torch's stream (2 N^3 flops)."""
     import torch
+    dtype = dtype or torch.float64
     n = 8192
-    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
-    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    a = torch.randn(n, n, dtype=dtype, device="cuda")
+    b = torch.randn(n, n, dtype=dtype, device="cuda")
     c = torch.empty_like(a)
     for _ in range(2):
         torch.matmul(a, b, out=c)
@@ -529,9 +557,11 @@ def measure_fp64_peak():
     return 2.0 * n ** 3 / (best * 1e-3) / 1e12
 
 
-def kernel_models(fp64_peak):
+def kernel_models(fp64_peak, fp32_peak=None):
     """Per kernel: (bound, peak, unit, multiplier from the recorded work to the
     unit's numerator, peak source, per-launch work definition)."""
+    fp32, fp32_src = ((fp32_peak, "of measured (cuBLAS SGEMM 8192^3, TF32 off, in this run)") if fp32_peak
+                      else (FP32_PEAK_TFLOPS, "of nominal GB300 FP32"))
     bf16, bf16_src = _measured("bf16_tflops_sustained", 1700.0)
     hbm, hbm_src = _measured("hbm_gbs", 6800.0)
     fp64 = ("fp64", fp64_peak, "TFLOP/s", 1e-12, "of measured (cuBLAS DGEMM 8192^3 in this run)",
@@ -539,9 +569,9 @@ def kernel_models(fp64_peak):
     return {
         "k_gemm_f64": fp64,
         "k_eig_f64": fp64,
-        "k_eig_bi_f32": ("fp32", FP32_PEAK_TFLOPS, "TFLOP/s", 1e-12, "of nominal GB300 FP32",
+        "k_eig_bi_f32": ("fp32", fp32, "TFLOP/s", 1e-12, fp32_src,
                          "(4/3) n^3 per block (Householder reduction)"),
-        "k_reflect": ("fp32", FP32_PEAK_TFLOPS, "TFLOP/s", 1e-12, "of nominal GB300 FP32",
+        "k_reflect": ("fp32", fp32, "TFLOP/s", 1e-12, fp32_src,
                       "2 n^3 per block (Householder reflectors applied to the tridiagonal eigenvectors)"),
         "k_gemm_oz": ("tensor", bf16, "TFLOP/s", 1e-12, bf16_src,
                       "useful work: 2MNK per FP64-accurate product; the bf16 digit-plane products it "
@@ -581,10 +611,10 @@ def _roofline(name, ms, work, n, models):
             "peak_source": src, "launches": n, "ms_total": ms, "per_launch": per}
 
 
-def roofline_from(kt, wc, fp64_peak):
+def roofline_from(kt, wc, fp64_peak, fp32_peak=None):
     """Roofline of the kernel with the largest share of the batch, every
     modelled kernel's own line, and the tensor-pipe view of k_gemm_oz."""
-    models = kernel_models(fp64_peak)
+    models = kernel_models(fp64_peak, fp32_peak)
     known = {k: v for k, v in kt.items() if k in models}
     top = max(known.items(), key=lambda kv: kv[1][0])
     rf = _roofline(top[0], *top[1], models)
@@ -757,7 +787,8 @@ def main():
     ap.add_argument("--no-serving", action="store_true", help="skip the serving-loop measurement")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--serving-requests", type=int, default=24)
-    ap.add_argument("--mix-requests", type=int, default=32, help="requests of the serving mix (0: skip)")
+    ap.add_argument("--mix-requests", type=int, default=32,
+                    help="requests of the serving mix, half for its capacity, half timed (0: skip)")
     ap.add_argument("--sites", type=int, default=0,
                     help="Wilson sites per run (default: the workload's; fewer only for profiling captures)")
     args = ap.parse_args()
@@ -780,6 +811,7 @@ def main():
     torch.cuda.set_device(local)
     build(verbose=False)
     fp64_peak = measure_fp64_peak()
+    fp32_peak = measure_fp32_peak()
     engines = [api.Engine(api.PREC_MIXED, device=local) for _ in range(ENGINES)]
     engine = engines[0]
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
@@ -789,7 +821,8 @@ def main():
             torch.distributed.barrier()
         torch.cuda.synchronize()
 
-    log("workload", NAME, "engines", ENGINES, "runs per engine", BATCH, "FP64 peak %.3f TFLOP/s" % fp64_peak)
+    log("workload", NAME, "engines", ENGINES, "runs per engine", BATCH,
+        "FP64 peak %.3f TFLOP/s, FP32 peak %.1f TFLOP/s" % (fp64_peak, fp32_peak))
     got_mixed = None
     for w in range(max(1, args.warmup)):
         _, _, got = step(engines, e2e=False, collect=(w == 0 and not reduced))
@@ -815,7 +848,7 @@ def main():
     path["F_rot_per_run"] = work["F_rot"] / (runs * args.steps)
     path["frac_of_fp64_peak"] = path["achieved"] / fp64_peak
     kt, wc = kernel_profile(engine)
-    rf = roofline_from(kt, wc, fp64_peak)
+    rf = roofline_from(kt, wc, fp64_peak, fp32_peak)
     log("kernels (ms per engine batch):", {k: round(v[0], 1) for k, v in kt.items()})
     rf["path"] = path
     fallbacks = sum(e.fallback_count() for e in engines)
@@ -835,8 +868,7 @@ def main():
         serving = serving_run(engine, 0.8 * runs / per, args.serving_requests)
         log("serving:", serving)
         if args.mix_requests > 0:
-            rate = 0.8 * sweep["mixed_runs_per_s"] if sweep else 2.0
-            mix = serving_mix_run(engine, rate, args.mix_requests)
+            mix = serving_mix_run(engine, max(2, args.mix_requests // 2))
             log("serving mix:", mix)
     engine.close()
     plain, got_fp64 = None, None
@@ -848,7 +880,7 @@ def main():
         t64 = max_over_ranks([sum(t64s)])[0] / len(t64s)
         log("fp64: %.3f s/step" % t64)
         kt64, wc64 = kernel_profile(e64s[0], b64)
-        rf64 = roofline_from(kt64, wc64, fp64_peak)
+        rf64 = roofline_from(kt64, wc64, fp64_peak, fp32_peak)
         p64 = path_roofline(work64, sum(t64s), fp64_peak, "of measured (cuBLAS DGEMM 8192^3 in this run)",
                             "fp64")
         p64["F_eig_per_run"] = work64["F_eig"] / (ENGINES * b64 * len(t64s))

@@ -1059,11 +1059,17 @@ static MixedStatus mixed_eigensolve(nrg_engine *e, std::vector<DevBlock *> &blks
         count_launch(e);
         post_launch("refine check");
       }
-      Prof pf(e, "k_oa_final");
-      launch_oa_final(at<RefineBlock>(dp, orb), int(nb), max_n, kClusterTau, at<int>(dp, ost),
-                      at<int>(dp, oflag), s);
+      {
+        Prof pf(e, "k_oa_final");
+        launch_oa_final(at<RefineBlock>(dp, orb), int(nb), max_n, kClusterTau, at<int>(dp, ost),
+                        at<int>(dp, oflag), s);
+        count_launch(e);
+        post_launch("refine final");
+      }
+      Prof pf(e, "k_oa_bigcl");
+      launch_oa_bigcl(at<RefineBlock>(dp, orb), int(nb), max_n, kClusterTau, at<int>(dp, ost), s);
       count_launch(e);
-      post_launch("refine final");
+      post_launch("refine long clusters");
       break;
     }
     {

@@ -1024,7 +1024,130 @@ void launch(const EigBlock *blocks, int nblocks, int max_n, int max_n_smem, int 
   k_eig<T><<<nblocks, kThreads, bytes, s>>>(blocks, max_n_smem, status, gate);
 }
 
+// ------------------------------------------------------------------------
+// Rayleigh-Ritz on the refinement's long clusters.  The final refinement
+// pass (k_refine.cu) diagonalises chains of near-degenerate levels (gaps
+// within tau) of up to 64 levels in shared memory; a block with a longer
+// chain gets status 3 and comes here: per chain of c levels (c <= 1024) the
+// c x c matrix S_CC = X_C^T H X_C (from S, in the sorted order) is
+// diagonalised in FP64 by the solver above (tred2 + QL, in the block's free
+// E2 buffer), and U_C = X_C Q, E_C = the sorted eigenvalues.  On success the
+// status returns to 0; a chain above 1024 levels or a QL failure sets 2 (the
+// FP64 re-solve of the whole block follows).
+constexpr int kSmallCluster = 64;      // the final pass's own limit (k_refine.cu)
+constexpr int kBigCluster = 1024;
+
+__global__ void __launch_bounds__(kThreads, 1)
+k_oa_bigcl(const RefineBlock *__restrict__ blocks, double tau_rel, int *status) {
+  if (status[blockIdx.x] != 3) return;
+  extern __shared__ __align__(16) char smem[];
+  __shared__ int ncl;
+  const RefineBlock B = blocks[blockIdx.x];
+  const int n = B.n, tid = threadIdx.x;
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    char *q = smem + off;
+    off += (bytes + 15) & ~size_t(15);
+    return q;
+  };
+  double *lam = reinterpret_cast<double *>(take(sizeof(double) * n));
+  int *perm = reinterpret_cast<int *>(take(sizeof(int) * n));
+  int *cl = reinterpret_cast<int *>(take(sizeof(int) * (n + 2)));
+  double *d = reinterpret_cast<double *>(take(sizeof(double) * kBigCluster));
+  double *e = reinterpret_cast<double *>(take(sizeof(double) * kBigCluster));
+  double *u = reinterpret_cast<double *>(take(sizeof(double) * kBigCluster));
+  double *p = reinterpret_cast<double *>(take(sizeof(double) * kBigCluster));
+  double *red = reinterpret_cast<double *>(take(sizeof(double) * (kWarps + 1)));
+  int *vof = reinterpret_cast<int *>(take(sizeof(int) * kBigCluster));
+  Ctl *ctl = reinterpret_cast<Ctl *>(take(sizeof(Ctl)));
+  auto sym = [&](int i, int j) { return i <= j ? B.S[int64_t(i) * B.ld + j] : B.S[int64_t(j) * B.ld + i]; };
+  // the final pass's Rayleigh quotients, tau, order and chains
+  double local = 0.0;
+  for (int i = tid; i < n; i += kThreads) {
+    const double l = B.S[int64_t(i) * B.ld + i] / B.G[int64_t(i) * B.ld + i];
+    lam[i] = l;
+    local = fmax(local, fabs(l));
+  }
+  const double tau = tau_rel * fmax(1.0, -block_min<double>(-local, red));
+  for (int i = tid; i < n; i += kThreads) {
+    const double x = lam[i];
+    int r = 0;
+    for (int j = 0; j < n; ++j) {
+      const double y = lam[j];
+      r += (y < x) || (y == x && j < i);
+    }
+    perm[r] = i;
+  }
+  __syncthreads();
+  if (tid == 0) {
+    int c = 0, k = 0;
+    while (k < n) {
+      int q = k + 1;
+      while (q < n && lam[perm[q]] - lam[perm[q - 1]] <= tau) ++q;
+      if (q - k > kSmallCluster) {
+        cl[2 * c] = k;
+        cl[2 * c + 1] = q;
+        ++c;
+      }
+      k = q;
+    }
+    ncl = c;
+  }
+  __syncthreads();
+  for (int q = 0; q < ncl; ++q) {
+    const int a0 = cl[2 * q], c = cl[2 * q + 1] - a0;
+    if (c > kBigCluster) {
+      if (tid == 0) status[blockIdx.x] = 2;
+      return;
+    }
+    double *A = B.E2;  // c x c, leading dimension c
+    for (int64_t idx = tid; idx < int64_t(c) * c; idx += kThreads) {
+      const int r = int(idx / c), s = int(idx - int64_t(r) * c);
+      A[idx] = sym(perm[a0 + r], perm[a0 + s]);
+    }
+    __syncthreads();
+    tred2_reduce<double>(A, c, c, d, e, u, p, red, true);
+    tred2_accumulate<double>(A, c, c, d, p);
+    ql_vectors<double>(A, c, c, d, e, u, p, ctl);
+    __syncthreads();
+    if (ctl->err) {
+      if (tid == 0) status[blockIdx.x] = 2;
+      return;
+    }
+    // eigenvector v is row v of A; vof[k] = the one of rank k (ascending)
+    for (int v = tid; v < c; v += kThreads) {
+      const double x = d[v];
+      int r = 0;
+      for (int j = 0; j < c; ++j) {
+        const double y = d[j];
+        r += (y < x) || (y == x && j < v);
+      }
+      vof[r] = v;
+    }
+    __syncthreads();
+    for (int k = tid; k < c; k += kThreads) B.Eout[a0 + k] = d[vof[k]];
+    for (int64_t idx = tid; idx < int64_t(n) * c; idx += kThreads) {
+      const int r = int(idx / c), k = int(idx - int64_t(r) * c);
+      const double *ev = A + int64_t(vof[k]) * c, *xr = B.X + int64_t(r) * B.ld;
+      double acc = 0.0;
+      for (int m = 0; m < c; ++m) acc = fma(xr[perm[a0 + m]], ev[m], acc);
+      B.U[int64_t(r) * B.ldu + a0 + k] = acc;
+    }
+    __syncthreads();
+  }
+  if (tid == 0) status[blockIdx.x] = 0;
+}
+
 }  // namespace
+
+void launch_oa_bigcl(const RefineBlock *blocks, int nblocks, int max_n, double tau_rel, int *status,
+                     cudaStream_t s) {
+  if (nblocks == 0) return;
+  const size_t bytes = 16 * 16 + sizeof(double) * max_n + sizeof(int) * (2 * size_t(max_n) + 2) +
+                       sizeof(double) * (4 * kBigCluster + kWarps + 1) + sizeof(int) * kBigCluster + sizeof(Ctl);
+  ensure_smem_limit(reinterpret_cast<const void *>(k_oa_bigcl), int(bytes));
+  k_oa_bigcl<<<nblocks, kThreads, bytes, s>>>(blocks, tau_rel, status);
+}
 
 int eig_smem_limit_f64() { return smem_limit<double>(); }
 int eig_smem_limit_f32() { return smem_limit<float>(kBiVecs); }

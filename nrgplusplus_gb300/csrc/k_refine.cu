@@ -148,8 +148,9 @@ k_oa_check(const RefineBlock *__restrict__ blocks, const int2 *__restrict__ tile
 // Final Rayleigh-Ritz pass: eigenvalues, cluster diagonalisation, sorted
 // output (E ascending, U columns in the same order).  status[b] = 2 when
 // the refinement has not converged (non-finite Rayleigh quotients or a
-// remaining correction above kConvTol) or a cluster exceeds kMaxCluster; the
-// host then re-solves the block in FP64.
+// remaining correction above kConvTol): the block is re-solved in FP64.
+// Chains longer than kMaxCluster are left as plain columns with status 3
+// for k_oa_bigcl, which diagonalises them and clears the status.
 __global__ void __launch_bounds__(kThreads)
 k_oa_final(const RefineBlock *__restrict__ blocks, double tau_rel, int *status, const int *flag) {
   extern __shared__ __align__(16) double sm[];
@@ -212,9 +213,9 @@ k_oa_final(const RefineBlock *__restrict__ blocks, double tau_rel, int *status, 
   __syncthreads();
   for (int q = 0; q < ncl; ++q) {
     const int a = cl[2 * q], c = cl[2 * q + 1] - a;
-    if (c > kMaxCluster) {
-      if (threadIdx.x == 0) status[blockIdx.x] = 2;
-      return;
+    if (c > kMaxCluster) {  // left to k_oa_bigcl (k_eig.cu)
+      if (threadIdx.x == 0) status[blockIdx.x] = 3;
+      continue;
     }
     for (int idx = threadIdx.x; idx < c * c; idx += kThreads) {
       const int p = idx / c, s = idx - p * c;

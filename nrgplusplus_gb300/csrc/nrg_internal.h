@@ -122,11 +122,16 @@ void launch_oa_update(const RefineBlock *blocks, const int2 *tiles, int ntiles, 
 // converged or a Rayleigh quotient is not finite.
 void launch_oa_check(const RefineBlock *blocks, const int2 *tiles, int ntiles, int max_n, double tau_rel,
                      int *flag, cudaStream_t s);
-// status[b] = 2: flagged by launch_oa_check, or a near-degenerate cluster
-// too large for the in-kernel Jacobi; the block is re-solved with the FP64
-// solver.
+// status[b] = 2: flagged by launch_oa_check; the block is re-solved with
+// the FP64 solver.  status[b] = 3: a chain of near-degenerate levels too long
+// for the in-kernel Jacobi, left to launch_oa_bigcl.
 void launch_oa_final(const RefineBlock *blocks, int nblocks, int max_n, double tau_rel, int *status,
                      const int *flag, cudaStream_t s);
+// Blocks with status 3 (a chain of near-degenerate levels longer than the
+// final pass's 64): Rayleigh-Ritz on each such chain (up to 1024 levels) in
+// FP64, status back to 0, or 2 when it cannot (k_eig.cu).
+void launch_oa_bigcl(const RefineBlock *blocks, int nblocks, int max_n, double tau_rel, int *status,
+                     cudaStream_t s);
 int refine_max_n();
 
 // ----------------------------------------------------------- grouped GEMM

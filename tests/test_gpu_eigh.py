@@ -79,6 +79,29 @@ def test_eigh_large_blocks(gpu_engine, mixed_engine, mode, n):
     assert eng.fallback_count() == before, (mode, n)
 
 
+@pytest.mark.parametrize("chain", [100, 300])
+def test_long_near_degenerate_chain(mixed_engine, chain):
+    """A chain of `chain` levels 1e-7 |H| apart (consecutive gaps inside the
+    refinement's cluster threshold, far above its 64-level in-kernel limit)
+    among well-separated levels: the long-cluster Rayleigh-Ritz pass
+    diagonalises it in FP64, with no FP64 re-solve of the block."""
+    rng = np.random.default_rng(chain)
+    n = 600
+    d = np.sort(rng.uniform(-5, 5, n - chain))
+    d = np.concatenate([d, 1.234 + 1e-6 * np.arange(chain)])
+    q, _ = np.linalg.qr(rng.standard_normal((n, n)))
+    m = (q * d) @ q.T
+    m = 0.5 * (m + m.T)
+    before = mixed_engine.fallback_count()
+    (w, U), = mixed_engine.eigh_batched([m])
+    wr = np.linalg.eigvalsh(m)
+    scale = np.abs(m).max()
+    assert np.abs(w - wr).max() <= 1e-12 * scale * n ** 0.5
+    assert np.abs(U.T @ U - np.eye(n)).max() <= 1e-12 * n ** 0.5
+    assert np.abs(m @ U - U * w).max() <= 1e-11 * scale * n ** 0.5
+    assert mixed_engine.fallback_count() == before
+
+
 @pytest.mark.parametrize("sizes", [[240, 300, 420], [480, 640], [706]])
 def test_cluster_and_one_cta_solvers_agree(monkeypatch, sizes):
     """The thread-block-cluster solver (blocks above one SM's shared memory;

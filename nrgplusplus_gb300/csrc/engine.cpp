@@ -746,9 +746,10 @@ constexpr int kFirstStepPlanes = 5;
 // the device status arrays
 // (in `hold`), which the caller reads at its next synchronisation.
 struct MixedStatus {
-  const int *refine = nullptr;  // per block: 0 ok, 2 re-solved in FP64
+  const int *refine = nullptr;  // per block: 0 ok; re-solved in FP64: 2 not converged, 4 chain too long
   const int *fp64 = nullptr;    // per block: FP64 re-solve status (0 ok)
   int nb = 0;
+  std::vector<int> dims;        // block sizes (for the NRG_DEBUG_FALLBACK report)
 };
 
 struct F64Solve {
@@ -1110,14 +1111,15 @@ static MixedStatus mixed_eigensolve(nrg_engine *e, std::vector<DevBlock *> &blks
     count_launch(e);
     post_launch("eigensolve f64 (refinement fallback)");
   }
-  return MixedStatus{at<int>(dp, ost), at<int>(dp, ost64), int(nb)};
+  return MixedStatus{at<int>(dp, ost), at<int>(dp, ost64), int(nb), dims};
 }
 
 // Host copies of a MixedStatus, filled by enqueue() and checked after the
 // caller's synchronisation.
 struct MixedCheck {
-  std::vector<int> refine, fp64;
+  std::vector<int> refine, fp64, dims;
   void enqueue(const MixedStatus &m, cudaStream_t s) {
+    dims = m.dims;
     refine.assign(m.nb, 0);
     fp64.assign(m.nb, 0);
     if (m.nb == 0) return;
@@ -1129,8 +1131,12 @@ struct MixedCheck {
   void check(nrg_engine *e) const {
     for (size_t b = 0; b < refine.size(); ++b) {
       if (refine[b] == 1) fail(NRG_E_EIG, "FP32 block eigensolver did not converge");
-      if (refine[b] == 2) {
+      if (refine[b] == 2 || refine[b] == 4) {
         ++e->fallback_blocks;
+        static const bool report = std::getenv("NRG_DEBUG_FALLBACK") != nullptr;
+        if (report)
+          std::fprintf(stderr, "nrg: FP64 re-solve of a block of %d rows (%s)\n", b < dims.size() ? dims[b] : -1,
+                       refine[b] == 2 ? "refinement not converged" : "near-degenerate chain above 1024 levels");
         if (fp64[b]) fail(NRG_E_EIG, "block eigensolver did not converge (FP64 re-solve)");
       }
     }

@@ -619,7 +619,7 @@ template <typename T>
 __global__ void __launch_bounds__(kThreads, 1)
 k_eig(const EigBlock *__restrict__ blocks, int max_n_smem, int *status, const int *gate) {
   extern __shared__ __align__(16) char smem[];
-  if (gate && gate[blockIdx.x] != 2) return;  // re-solve only the flagged blocks
+  if (gate && gate[blockIdx.x] != 2 && gate[blockIdx.x] != 4) return;  // re-solve only the flagged blocks
   const EigBlock B = blocks[blockIdx.x];
   const int n = B.n;
   if (n == 0) return;
@@ -1032,8 +1032,8 @@ void launch(const EigBlock *blocks, int nblocks, int max_n, int max_n_smem, int 
 // c x c matrix S_CC = X_C^T H X_C (from S, in the sorted order) is
 // diagonalised in FP64 by the solver above (tred2 + QL, in the block's free
 // E2 buffer), and U_C = X_C Q, E_C = the sorted eigenvalues.  On success the
-// status returns to 0; a chain above 1024 levels or a QL failure sets 2 (the
-// FP64 re-solve of the whole block follows).
+// status returns to 0; a chain above 1024 levels or a QL failure sets 4 (the
+// FP64 re-solve of the whole block follows, as for status 2).
 constexpr int kSmallCluster = 64;      // the final pass's own limit (k_refine.cu)
 constexpr int kBigCluster = 1024;
 
@@ -1097,7 +1097,7 @@ k_oa_bigcl(const RefineBlock *__restrict__ blocks, double tau_rel, int *status) 
   for (int q = 0; q < ncl; ++q) {
     const int a0 = cl[2 * q], c = cl[2 * q + 1] - a0;
     if (c > kBigCluster) {
-      if (tid == 0) status[blockIdx.x] = 2;
+      if (tid == 0) status[blockIdx.x] = 4;
       return;
     }
     double *A = B.E2;  // c x c, leading dimension c
@@ -1111,7 +1111,7 @@ k_oa_bigcl(const RefineBlock *__restrict__ blocks, double tau_rel, int *status) 
     ql_vectors<double>(A, c, c, d, e, u, p, ctl);
     __syncthreads();
     if (ctl->err) {
-      if (tid == 0) status[blockIdx.x] = 2;
+      if (tid == 0) status[blockIdx.x] = 4;
       return;
     }
     // eigenvector v is row v of A; vof[k] = the one of rank k (ascending)

@@ -918,6 +918,34 @@ static MixedStatus mixed_eigensolve(nrg_engine *e, std::vector<DevBlock *> &blks
     eb64[b].ld = blks[b]->ld;
     eb64[b].ldu = blks[b]->ld;
   }
+  // The FP64 re-solve of the blocks whose refinement failed (gated on the
+  // device by their status), as the plain FP64 path solves them: blocks above
+  // the reflector kernel's limit by tred2 + QL in global memory, those above
+  // shared memory by the FP64 reflector solver (scratch allocated here), the
+  // rest by tred2 + QL in shared memory.  The blocks are sorted by size,
+  // largest first, so each set is a range: [0, fb_huge), [fb_huge, fb_refl),
+  // [fb_refl, nb).
+  int fb_huge = 0, fb_tw = 8, fb_panel = 1;
+  while (fb_huge < int(nb) && eb64[fb_huge].n > reflect_max_n(true)) ++fb_huge;
+  int fb_refl = fb_huge;
+  while (fb_refl < int(nb) && eb64[fb_refl].n > e->eig_smem_f64) ++fb_refl;
+  std::vector<int2> fb_tiles;
+  if (fb_refl > fb_huge) {
+    reflect_config(eb64[fb_huge].n, &fb_tw, &fb_panel, true);
+    int64_t wsz = 0;
+    for (int b = fb_huge; b < fb_refl; ++b) wsz += int64_t(eb64[b].n) * eb64[b].ld;
+    DevPtr w = dalloc(e, 3 * wsz * sizeof(double) + 16);
+    hold.push_back(w);
+    double *base = static_cast<double *>(w->ptr);
+    int64_t o = 0;
+    for (int b = fb_huge; b < fb_refl; ++b) {
+      eb64[b].W64 = base + o;
+      eb64[b].V64 = base + wsz + o;
+      eb64[b].Bt64 = base + 2 * wsz + o;
+      o += int64_t(eb64[b].n) * eb64[b].ld;
+      for (int tn = 0; tn < (eb64[b].n + fb_tw - 1) / fb_tw; ++tn) fb_tiles.push_back(make_int2(b - fb_huge, tn));
+    }
+  }
   // blocks above the one-CTA shared-memory limit that a cluster's distributed
   // shared memory holds go to k_eig_cluster, the others to k_eig_bi
   std::vector<EigBlock> eb_one, eb_cl;
@@ -936,7 +964,7 @@ static MixedStatus mixed_eigensolve(nrg_engine *e, std::vector<DevBlock *> &blks
     }
   }
   Arena a;
-  size_t oeb = a.add(eb), ost = a.add(stat), oeb64 = a.add(eb64), ost64 = a.add(stat);
+  size_t oeb = a.add(eb), ost = a.add(stat), oeb64 = a.add(eb64), ost64 = a.add(stat), ofbt = a.add(fb_tiles);
   std::vector<size_t> obt(rplans.size());
   for (size_t p = 0; p < rplans.size(); ++p) obt[p] = a.add(rtiles[p]);
   const size_t orb = a.add(rb);  // filled per step below (host copy re-uploaded)
@@ -1106,9 +1134,23 @@ static MixedStatus mixed_eigensolve(nrg_engine *e, std::vector<DevBlock *> &blks
   }
   {
     Prof pf(e, "k_eig_f64_fallback");
-    launch_eig_f64(at<EigBlock>(dp, oeb64), int(nb), max_n, e->eig_smem_f64, at<int>(dp, ost64), s,
-                   at<int>(dp, ost));
-    count_launch(e);
+    const EigBlock *d64 = at<EigBlock>(dp, oeb64);
+    int *st64 = at<int>(dp, ost64), *gate = at<int>(dp, ost);
+    if (fb_huge > 0) {
+      launch_eig_f64(d64, fb_huge, eb64[0].n, e->eig_smem_f64, st64, s, gate);
+      count_launch(e);
+    }
+    if (fb_refl > fb_huge) {
+      launch_eig_bisect_f64(d64 + fb_huge, fb_refl - fb_huge, eb64[fb_huge].n, e->eig_smem_f64, s, gate + fb_huge);
+      launch_reflect(d64 + fb_huge, at<int2>(dp, ofbt), int(fb_tiles.size()), eb64[fb_huge].n, fb_tw, fb_panel, s,
+                     true, gate + fb_huge);
+      count_launch(e, 2);
+    }
+    if (int(nb) > fb_refl) {
+      launch_eig_f64(d64 + fb_refl, int(nb) - fb_refl, eb64[fb_refl].n, e->eig_smem_f64, st64 + fb_refl, s,
+                     gate + fb_refl);
+      count_launch(e);
+    }
     post_launch("eigensolve f64 (refinement fallback)");
   }
   return MixedStatus{at<int>(dp, ost), at<int>(dp, ost64), int(nb), dims};

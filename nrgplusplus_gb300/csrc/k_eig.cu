@@ -777,8 +777,9 @@ __device__ __forceinline__ double rnorm_t(double x) { return 1.0 / sqrt(fmax(x, 
 // no refinement after it.
 template <typename T>
 __global__ void __launch_bounds__(kThreads, 1)
-k_eig_bi(const EigBlock *__restrict__ blocks, int max_n_smem, int smem_total) {
+k_eig_bi(const EigBlock *__restrict__ blocks, int max_n_smem, int smem_total, const int *gate) {
   extern __shared__ __align__(16) char smem[];
+  if (gate && gate[blockIdx.x] != 2 && gate[blockIdx.x] != 4) return;  // re-solve only the flagged blocks
   const EigBlock B = blocks[blockIdx.x];
   const int n = B.n;
   if (n == 0) return;
@@ -937,12 +938,13 @@ template <> __device__ __forceinline__ const double *refl_V<double>(const EigBlo
 
 template <typename T, int TW>
 __global__ void __launch_bounds__(256)
-k_reflect(const EigBlock *__restrict__ blocks, const int2 *__restrict__ tiles, int panel) {
+k_reflect(const EigBlock *__restrict__ blocks, const int2 *__restrict__ tiles, int panel, const int *gate) {
   constexpr int CPW = TW / 8;  // columns per warp
   constexpr int XP = TW + 1;   // odd row pitch: lane-strided rows hit distinct banks
   extern __shared__ __align__(16) unsigned char rsm_raw[];
   T *rsm = reinterpret_cast<T *>(rsm_raw);
   const int2 t = tiles[blockIdx.x];
+  if (gate && gate[t.x] != 2 && gate[t.x] != 4) return;  // re-solve only the flagged blocks
   const EigBlock B = blocks[t.x];
   const T *Wm = refl_W<T>(B), *Vm = refl_V<T>(B);
   const int n = B.n, c0 = t.y * TW;
@@ -1168,13 +1170,14 @@ void launch_eig_f64(const EigBlock *blocks, int nblocks, int max_n, int max_n_sm
 }
 
 template <typename T>
-static void launch_bisect(const EigBlock *blocks, int nblocks, int max_n, int max_n_smem, cudaStream_t s) {
+static void launch_bisect(const EigBlock *blocks, int nblocks, int max_n, int max_n_smem, cudaStream_t s,
+                          const int *gate = nullptr) {
   if (nblocks == 0) return;
   ensure_smem_limit(reinterpret_cast<const void *>(k_eig_bi<T>), kSmemBytes);
   size_t bytes = smem_bytes<T>(max_n, max_n <= max_n_smem, kBiVecs);
   if (max_n > max_n_smem) bytes = std::max(bytes, smem_bytes<T>(max_n_smem, true, kBiVecs));
   if (bytes > size_t(kSmemBytes)) bytes = kSmemBytes;
-  k_eig_bi<T><<<nblocks, kThreads, bytes, s>>>(blocks, max_n_smem, int(bytes));
+  k_eig_bi<T><<<nblocks, kThreads, bytes, s>>>(blocks, max_n_smem, int(bytes), gate);
 }
 
 void launch_eig_bisect_f32(const EigBlock *blocks, int nblocks, int max_n, int max_n_smem,
@@ -1183,8 +1186,8 @@ void launch_eig_bisect_f32(const EigBlock *blocks, int nblocks, int max_n, int m
 }
 
 void launch_eig_bisect_f64(const EigBlock *blocks, int nblocks, int max_n, int max_n_smem,
-                           cudaStream_t s) {
-  launch_bisect<double>(blocks, nblocks, max_n, max_n_smem, s);
+                           cudaStream_t s, const int *gate) {
+  launch_bisect<double>(blocks, nblocks, max_n, max_n_smem, s, gate);
 }
 
 bool reflect_config(int max_n, int *tw, int *panel, bool fp64) {
@@ -1217,28 +1220,28 @@ int reflect_max_n(bool fp64) {
 }
 
 template <typename T, int TW> static void reflect_launch(const EigBlock *blocks, const int2 *tiles, int ntiles,
-                                                         int panel, size_t bytes, cudaStream_t s) {
+                                                         int panel, size_t bytes, cudaStream_t s, const int *gate) {
   ensure_smem_limit(reinterpret_cast<const void *>(k_reflect<T, TW>), int(kReflectSmem));
-  k_reflect<T, TW><<<ntiles, 256, bytes, s>>>(blocks, tiles, panel);
+  k_reflect<T, TW><<<ntiles, 256, bytes, s>>>(blocks, tiles, panel, gate);
 }
 
 template <typename T>
 static void reflect_dispatch(const EigBlock *blocks, const int2 *tiles, int ntiles, int max_n, int tw, int panel,
-                             cudaStream_t s) {
+                             cudaStream_t s, const int *gate) {
   const size_t bytes = reflect_bytes(max_n, tw, panel, sizeof(T));
   switch (tw) {
-    case 64: reflect_launch<T, 64>(blocks, tiles, ntiles, panel, bytes, s); break;
-    case 32: reflect_launch<T, 32>(blocks, tiles, ntiles, panel, bytes, s); break;
-    case 16: reflect_launch<T, 16>(blocks, tiles, ntiles, panel, bytes, s); break;
-    default: reflect_launch<T, 8>(blocks, tiles, ntiles, panel, bytes, s); break;
+    case 64: reflect_launch<T, 64>(blocks, tiles, ntiles, panel, bytes, s, gate); break;
+    case 32: reflect_launch<T, 32>(blocks, tiles, ntiles, panel, bytes, s, gate); break;
+    case 16: reflect_launch<T, 16>(blocks, tiles, ntiles, panel, bytes, s, gate); break;
+    default: reflect_launch<T, 8>(blocks, tiles, ntiles, panel, bytes, s, gate); break;
   }
 }
 
 void launch_reflect(const EigBlock *blocks, const int2 *tiles, int ntiles, int max_n, int tw, int panel,
-                    cudaStream_t s, bool fp64) {
+                    cudaStream_t s, bool fp64, const int *gate) {
   if (ntiles == 0) return;
-  if (fp64) reflect_dispatch<double>(blocks, tiles, ntiles, max_n, tw, panel, s);
-  else reflect_dispatch<float>(blocks, tiles, ntiles, max_n, tw, panel, s);
+  if (fp64) reflect_dispatch<double>(blocks, tiles, ntiles, max_n, tw, panel, s, gate);
+  else reflect_dispatch<float>(blocks, tiles, ntiles, max_n, tw, panel, s, gate);
 }
 void launch_eig_f32(const EigBlock *blocks, int nblocks, int max_n, int max_n_smem, int *status,
                     cudaStream_t s) {

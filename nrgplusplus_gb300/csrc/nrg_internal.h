@@ -71,9 +71,10 @@ struct EigBlock {
 void launch_eig_bisect_f32(const EigBlock *blocks, int nblocks, int max_n, int max_n_smem,
                            cudaStream_t s);
 // The same solver in FP64 (W64, V64, Bt64): the plain path's blocks above the
-// shared-memory limit.
+// shared-memory limit, and the mixed path's FP64 re-solve of such blocks
+// (with a gate: only blocks with gate[b] == 2 or 4 are solved).
 void launch_eig_bisect_f64(const EigBlock *blocks, int nblocks, int max_n, int max_n_smem,
-                           cudaStream_t s);
+                           cudaStream_t s, const int *gate = nullptr);
 // fp64: the FP64 reflector solver's buffers (W64, V64) and tiles.
 bool reflect_config(int max_n, int *tw, int *panel, bool fp64 = false);
 int reflect_max_n(bool fp64 = false);
@@ -81,12 +82,12 @@ int reflect_max_n(bool fp64 = false);
 // largest reflector panel that does)
 bool reflect_fits(int max_n, int tw, int *panel, bool fp64 = false);
 void launch_reflect(const EigBlock *blocks, const int2 *tiles, int ntiles, int max_n, int tw, int panel,
-                    cudaStream_t s, bool fp64 = false);
+                    cudaStream_t s, bool fp64 = false, const int *gate = nullptr);
 // FP64 Householder tridiagonalisation + implicit QL, one CTA per block.
 // status[b] != 0 if block b hit the QL iteration cap.
 // max_n: largest block of the launch; blocks with n <= max_n_smem are solved
 // in shared memory, larger ones in their own global buffer.  With a gate,
-// only blocks with gate[b] == 2 are solved (the others return at once).
+// only blocks with gate[b] == 2 or 4 are solved (the others return at once).
 void launch_eig_f64(const EigBlock *blocks, int nblocks, int max_n, int max_n_smem, int *status,
                     cudaStream_t s, const int *gate = nullptr);
 // Same algorithm in FP32 (mixed path first stage); writes U and E in FP64.

@@ -787,7 +787,7 @@ def main():
     ap.add_argument("--no-serving", action="store_true", help="skip the serving-loop measurement")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--serving-requests", type=int, default=24)
-    ap.add_argument("--mix-requests", type=int, default=32,
+    ap.add_argument("--mix-requests", type=int, default=16,
                     help="requests of the serving mix, half for its capacity, half timed (0: skip)")
     ap.add_argument("--sites", type=int, default=0,
                     help="Wilson sites per run (default: the workload's; fewer only for profiling captures)")

@@ -921,10 +921,12 @@ static MixedStatus mixed_eigensolve(nrg_engine *e, std::vector<DevBlock *> &blks
   // The FP64 re-solve of the blocks whose refinement failed (gated on the
   // device by their status), as the plain FP64 path solves them: blocks above
   // the reflector kernel's limit by tred2 + QL in global memory, those above
-  // shared memory by the FP64 reflector solver (scratch allocated here), the
-  // rest by tred2 + QL in shared memory.  The blocks are sorted by size,
-  // largest first, so each set is a range: [0, fb_huge), [fb_huge, fb_refl),
-  // [fb_refl, nb).
+  // shared memory by the FP64 reflector solver, the rest by tred2 + QL in
+  // shared memory.  The blocks are sorted by size, largest first, so each set
+  // is a range: [0, fb_huge), [fb_huge, fb_refl), [fb_refl, nb).  The
+  // reflector solver works in buffers free by then: its reflectors in H (the
+  // reduction reads H in place), V and the pivots in the refinement's Y and E
+  // buffers of the block.
   int fb_huge = 0, fb_tw = 8, fb_panel = 1;
   while (fb_huge < int(nb) && eb64[fb_huge].n > reflect_max_n(true)) ++fb_huge;
   int fb_refl = fb_huge;
@@ -932,17 +934,10 @@ static MixedStatus mixed_eigensolve(nrg_engine *e, std::vector<DevBlock *> &blks
   std::vector<int2> fb_tiles;
   if (fb_refl > fb_huge) {
     reflect_config(eb64[fb_huge].n, &fb_tw, &fb_panel, true);
-    int64_t wsz = 0;
-    for (int b = fb_huge; b < fb_refl; ++b) wsz += int64_t(eb64[b].n) * eb64[b].ld;
-    DevPtr w = dalloc(e, 3 * wsz * sizeof(double) + 16);
-    hold.push_back(w);
-    double *base = static_cast<double *>(w->ptr);
-    int64_t o = 0;
     for (int b = fb_huge; b < fb_refl; ++b) {
-      eb64[b].W64 = base + o;
-      eb64[b].V64 = base + wsz + o;
-      eb64[b].Bt64 = base + 2 * wsz + o;
-      o += int64_t(eb64[b].n) * eb64[b].ld;
+      eb64[b].W64 = blks[b]->H;
+      eb64[b].V64 = P(my, off[b]);
+      eb64[b].Bt64 = P(me2, off[b]);
       for (int tn = 0; tn < (eb64[b].n + fb_tw - 1) / fb_tw; ++tn) fb_tiles.push_back(make_int2(b - fb_huge, tn));
     }
   }

@@ -682,7 +682,7 @@ def output_errors(engine, got_mixed, got_fp64):
             spectra.append(engine.broaden(e, h, om, 0.6))
     out = {"vs_reference": {}, "tolerances": {
         "eig": "|dE| <= max(1e-10, 1e-14 Lambda^(N/2)) per site N (the reference's own FP64 noise); "
-               "north-star target 1e-9", "spectral": "1e-6 of the maximum", "entropy": "1e-8"}}
+               "the headline target is 1e-9", "spectral": "1e-6 of the maximum", "entropy": "1e-8"}}
     for name, got in (("mixed", got_mixed), ("fp64", got_fp64)):
         if got:
             out["vs_reference"][name] = _compare(got, eigs, spectra, th["entropy"], th["specificHeat"], T)

@@ -1,7 +1,7 @@
 // Oracle driver: runs the reference's own NRG engine (headers compiled
 // unchanged from the reference tree by oracle/build_ref.sh) on one workload
 // and writes every result array to a flat binary file of named float64
-// arrays.  Test infrastructure only: it is the checker, never the product.
+// arrays.  Test infrastructure only: it checks the engine and is never part of it.
 //
 // The loop mirrors the reference's example drivers:
 //   examples/rgflowSIAM/main.cpp:27-42       (SIAM forward RG flow)

@@ -1,8 +1,9 @@
 """CPU oracle: numpy restatement of the reference's NRG hot path.
 
 TEST INFRASTRUCTURE ONLY.  Only ``tests/``, ``__graft_entry__.smoke()`` and the
-CPU-baseline leg of ``bench.py`` may import this module, and only as the
-checker (or the timed CPU baseline); the product path never calls it.
+CPU-baseline leg of ``bench.py`` may import this module, and only to check
+the engine's results (or as the timed CPU baseline); the product path never
+calls it.
 
 Parity is pinned two ways: against the golden vectors the reference shipped
 (examples/entropyKondo/resultsJ0.250000.h5 and resultsZero.h5: per-iteration

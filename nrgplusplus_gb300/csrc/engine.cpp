@@ -662,7 +662,7 @@ static std::vector<ReflectPlan> reflect_plans(nrg_engine *e, uint64_t key, int m
     int pn = 1;
     if (reflect_fits(max_n, it->second.tw, &pn, fp64)) return {{it->second.tw, std::min(pn, it->second.panel)}};
   }
-  for (int tw : {64, 32, 16, 8}) {
+  for (int tw : {64, 32, 16, 8, 4}) {
     int pn = 1;
     if (!reflect_fits(max_n, tw, &pn, fp64)) continue;
     out.push_back({tw, pn});
@@ -777,7 +777,7 @@ static F64Solve fp64_eigensolve(nrg_engine *e, std::vector<EigBlock> eb, std::ve
     std::vector<int> eligible64;
     int64_t wsz = 0;
     for (auto &b : eb) {
-      if (b.n > e->eig_smem_f64 && reflect_config(b.n, &tw64, &panel64, true)) {
+      if (b.n > e->eig_smem_f64 && b.n <= eig_bi_max_n(true) && reflect_config(b.n, &tw64, &panel64, true)) {
         rs.push_back(b);
         wsz += int64_t(b.n) * b.ld;
         max_r64 = std::max(max_r64, b.n);
@@ -928,7 +928,8 @@ static MixedStatus mixed_eigensolve(nrg_engine *e, std::vector<DevBlock *> &blks
   // reduction reads H in place), V and the pivots in the refinement's Y and E
   // buffers of the block.
   int fb_huge = 0, fb_tw = 8, fb_panel = 1;
-  while (fb_huge < int(nb) && eb64[fb_huge].n > reflect_max_n(true)) ++fb_huge;
+  const int fb_max = std::min(reflect_max_n(true), eig_bi_max_n(true));
+  while (fb_huge < int(nb) && eb64[fb_huge].n > fb_max) ++fb_huge;
   int fb_refl = fb_huge;
   while (fb_refl < int(nb) && eb64[fb_refl].n > e->eig_smem_f64) ++fb_refl;
   std::vector<int2> fb_tiles;

@@ -939,8 +939,9 @@ template <> __device__ __forceinline__ const double *refl_V<double>(const EigBlo
 template <typename T, int TW>
 __global__ void __launch_bounds__(256)
 k_reflect(const EigBlock *__restrict__ blocks, const int2 *__restrict__ tiles, int panel, const int *gate) {
-  constexpr int CPW = TW / 8;  // columns per warp
-  constexpr int XP = TW + 1;   // odd row pitch: lane-strided rows hit distinct banks
+  constexpr int CPW = TW >= 8 ? TW / 8 : 1;  // columns per warp
+  constexpr int NWC = TW >= 8 ? 8 : TW;      // warps with columns (TW = 4, the largest blocks: 4)
+  constexpr int XP = TW + 1;                 // odd row pitch: lane-strided rows hit distinct banks
   extern __shared__ __align__(16) unsigned char rsm_raw[];
   T *rsm = reinterpret_cast<T *>(rsm_raw);
   const int2 t = tiles[blockIdx.x];
@@ -968,7 +969,7 @@ k_reflect(const EigBlock *__restrict__ blocks, const int2 *__restrict__ tiles, i
       if (lane == 0) hs[q - p0] = src[q];
     }
     __syncthreads();
-    for (int q = p0; q < p1; ++q) {
+    for (int q = p0; q < p1 && warp < NWC; ++q) {
       const T h = hs[q - p0];
       if (h == T(0)) continue;
       const T *uq = Up + size_t(q - p0) * n;
@@ -1192,7 +1193,7 @@ void launch_eig_bisect_f64(const EigBlock *blocks, int nblocks, int max_n, int m
 
 bool reflect_config(int max_n, int *tw, int *panel, bool fp64) {
   const size_t el = fp64 ? sizeof(double) : sizeof(float);
-  for (int w = 64; w >= 8; w /= 2) {
+  for (int w = 64; w >= 4; w /= 2) {
     if (reflect_bytes(max_n, w, 1, el) > kReflectSmem) continue;
     int pn = 32;
     while (pn > 1 && reflect_bytes(max_n, w, pn, el) > kReflectSmem) --pn;
@@ -1215,7 +1216,19 @@ bool reflect_fits(int max_n, int tw, int *panel, bool fp64) {
 int reflect_max_n(bool fp64) {
   const size_t el = fp64 ? sizeof(double) : sizeof(float);
   int n = 8;
-  while (reflect_bytes(n + 1, 8, 1, el) <= kReflectSmem) ++n;
+  while (reflect_bytes(n + 1, 4, 1, el) <= kReflectSmem) ++n;
+  return n;
+}
+
+// Largest block the reflector solver's reduction takes (its shared vectors
+// of n; the matrix streams from global memory).
+int eig_bi_max_n(bool fp64) {
+  int n = 64;
+  if (fp64) {
+    while (smem_bytes<double>(n + 1, false, kBiVecs) <= size_t(kSmemBytes)) ++n;
+  } else {
+    while (smem_bytes<float>(n + 1, false, kBiVecs) <= size_t(kSmemBytes)) ++n;
+  }
   return n;
 }
 
@@ -1233,7 +1246,8 @@ static void reflect_dispatch(const EigBlock *blocks, const int2 *tiles, int ntil
     case 64: reflect_launch<T, 64>(blocks, tiles, ntiles, panel, bytes, s, gate); break;
     case 32: reflect_launch<T, 32>(blocks, tiles, ntiles, panel, bytes, s, gate); break;
     case 16: reflect_launch<T, 16>(blocks, tiles, ntiles, panel, bytes, s, gate); break;
-    default: reflect_launch<T, 8>(blocks, tiles, ntiles, panel, bytes, s, gate); break;
+    case 8: reflect_launch<T, 8>(blocks, tiles, ntiles, panel, bytes, s, gate); break;
+    default: reflect_launch<T, 4>(blocks, tiles, ntiles, panel, bytes, s, gate); break;
   }
 }
 

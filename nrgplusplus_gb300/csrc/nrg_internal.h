@@ -65,7 +65,7 @@ struct EigBlock {
 // E (FP64), the Householder reflectors into W (row i: u_i in columns 0..i-1,
 // h_i on the diagonal) and the tridiagonal eigenvectors into V; then
 // launch_reflect writes U = Q V (FP64) by applying the reflectors to V.
-// reflect_config picks the column-tile width tw (64, 32, 16 or 8) and the
+// reflect_config picks the column-tile width tw (64, 32, 16, 8 or 4) and the
 // reflector panel for the largest block of a launch (false: too large);
 // tiles: (block, column tile of width tw).
 void launch_eig_bisect_f32(const EigBlock *blocks, int nblocks, int max_n, int max_n_smem,
@@ -78,6 +78,8 @@ void launch_eig_bisect_f64(const EigBlock *blocks, int nblocks, int max_n, int m
 // fp64: the FP64 reflector solver's buffers (W64, V64) and tiles.
 bool reflect_config(int max_n, int *tw, int *panel, bool fp64 = false);
 int reflect_max_n(bool fp64 = false);
+// largest block the reflector solver's reduction (k_eig_bi) takes
+int eig_bi_max_n(bool fp64);
 // whether column tiles of width tw fit for blocks up to max_n (and the
 // largest reflector panel that does)
 bool reflect_fits(int max_n, int tw, int *panel, bool fp64 = false);

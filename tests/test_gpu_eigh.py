@@ -48,15 +48,14 @@ def test_eigh_batched(gpu_engine, mixed_engine, mode):
         assert np.abs(h @ U - U * w).max() <= 1e-11 * scale * max(1, n) ** 0.5, (mode, n)
 
 
-@pytest.mark.parametrize("mode,n", [("fp64", 1500), ("mixed", 1500), ("mixed", 4300)])
+@pytest.mark.parametrize("mode,n", [("fp64", 1500), ("mixed", 1500), ("mixed", 4300), ("fp64", 4300)])
 def test_eigh_large_blocks(gpu_engine, mixed_engine, mode, n):
     """Blocks of the two-channel workload's size (up to ~4300 rows): the
     one-CTA reflector solver streaming the matrix from global memory, with
     its bisection and inverse iteration, in FP64 (no refinement) and FP32
     followed by the FP64-accurate refinement (one or two extra Newton steps
-    above 1536 / 3072 rows, no FP64 re-solve).  (The plain FP64 path solves
-    blocks above its reflector kernel's limit, about 2880 rows, with tred2 +
-    QL in global memory, minutes per block: not run here.)"""
+    above 1536 / 3072 rows, no FP64 re-solve); at 4300 rows the FP64
+    back-transform runs on 4-column tiles."""
     eng = gpu_engine if mode == "fp64" else mixed_engine
     rng = np.random.default_rng(n)
     a = rng.standard_normal((n, n))

@@ -5,7 +5,7 @@
   spectrum, entropy and specific heat, against the reference's own outputs
   (tests/golden/ref_c2_siam_*_nk1024, ref_siam_*_nk2048);
 * the two-channel workload at its own size (Lambda=4, Nkeep=4096, blocks up
-  to 4279 rows), mixed path, over its first five sites, against the
+  to 4279 rows), both paths, over its first five sites, against the
   reference's run (tests/golden/ref_c3_twochannel_nk4096);
 * instances of the seeded parameter sweep stepped together in one batch
   (different Lambda, Nkeep and lengths), against the reference's outputs for
@@ -118,18 +118,17 @@ def test_superconducting_bath_against_reference(gpu_engine, mixed_engine, path):
         out["run"].close()
 
 
-def test_two_channel_workload_nk4096_mixed(mixed_engine):
-    """Blocks of up to 4279 rows (four per site above 4100): the FP32
-    reflector solver streaming them from global memory, then the
-    FP64-accurate refinement.  A few of the largest blocks have chains of
-    near-degenerate levels longer than the refinement's 64-level cluster
-    limit and are re-solved in FP64 (the engine's fallback, counted by
-    fallback_count), which is most of this test's time.  The plain FP64
-    path would solve the blocks
-    above its reflector kernel's limit (about 2880 rows) with tred2 + QL in
-    global memory, minutes per block, so it is not run at this size."""
+@pytest.mark.parametrize("path", ["mixed", "fp64"])
+def test_two_channel_workload_nk4096(gpu_engine, mixed_engine, path):
+    """Blocks of up to 4279 rows (four per site above 4100).  Mixed path: the
+    FP32 reflector solver streaming them from global memory, then the
+    FP64-accurate refinement; a few blocks miss its convergence test and are
+    re-solved in FP64 (the engine's fallback, counted by fallback_count).
+    Plain FP64 path: every block above shared memory by the FP64 reflector
+    solver (4-column back-transform tiles for the largest)."""
+    eng = gpu_engine if path == "fp64" else mixed_engine
     fx = golden("ref_c3_twochannel_nk4096")
-    out = workloads.run_nrg(mixed_engine, "twochannel", 4096, 5, 4.0, V=0.12, eps=-0.3, U=0.6)
+    out = workloads.run_nrg(eng, "twochannel", 4096, 5, 4.0, V=0.12, eps=-0.3, U=0.6)
     try:
         check_eigs(fx, out["eig"], 4.0)
         for i in range(5):

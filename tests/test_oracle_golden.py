@@ -16,8 +16,8 @@ from oracle.nrg_oracle import (FdmSpectrumOracle, NrgOracle, broaden, siam_run,
                                temperature_grid)
 
 
-def _check_eigs(fx, eigs, lam, offset=0):
-    return check_eigs(fx, eigs, lam, offset)
+def _check_eigs(fx, eigs, lam, offset=0, niter=None):
+    return check_eigs(fx, eigs, lam, offset, niter=niter)
 
 
 CV_RTOL = 1e-5  # specific heat, max relative error over T >= 2.6e-7
@@ -67,6 +67,19 @@ def test_ref_twochannel_rgflow():
     res = siam_run(imp, M.two_channel(), 256, 8, 4.0, V=0.12, full_fdag=False)
     _check_eigs(fx, res["eig"], 4.0)
     for i in range(8):
+        assert np.array_equal(np.array(res["kept"][i]), fx["kept%d" % i]), i
+
+
+def test_ref_twochannel_nk4096_first_sites():
+    """The oracle at the two-channel workload's own size (Lambda=4,
+    Nkeep=4096): through the first truncation (site 2: 65,792 states in
+    blocks up to 4144 rows), every eigenvalue and kept count against the
+    reference's run."""
+    fx = golden("ref_c3_twochannel_nk4096")
+    imp = M.duplicate_ops(M.spinhalf(-0.3, 0.6), 2)
+    res = siam_run(imp, M.two_channel(), 4096, 3, 4.0, V=0.12, full_fdag=False)
+    _check_eigs(fx, res["eig"], 4.0, niter=3)
+    for i in range(3):
         assert np.array_equal(np.array(res["kept"][i]), fx["kept%d" % i]), i
 
 
